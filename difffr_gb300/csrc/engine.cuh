@@ -1,0 +1,238 @@
+// engine.cuh — host orchestration of the DiffDFSPH step on one GPU (one CUDA stream
+// per context). Engine<T> is instantiated for float and double fluid arithmetic in
+// engine_fp32.cu / engine_fp64.cu; the C ABI (abi.cu) only sees EngineBase.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/dfsph.h"
+#include "engine_api.h"
+#include "common.cuh"
+#include "kernels_fluid.cuh"
+#include "kernels_rigid.cuh"
+
+namespace dfsph {
+
+// ----------------------------------------------------------------- device buffer
+template <class E>
+struct DBuf {
+  E *p = nullptr;
+  size_t n = 0;
+  void alloc(size_t count) {
+    free();
+    n = count;
+    if (count) DF_CK(cudaMalloc(&p, count * sizeof(E)));
+  }
+  void free() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  ~DBuf() { free(); }
+};
+
+// int exclusive scan in place over n entries: out[k] = sum_{j<k} in[j]
+static __global__ void k_scan_block(int n, int *__restrict__ data, int *__restrict__ block_sums) {
+  constexpr int ITEMS = 4;
+  __shared__ int warp_tot[32];
+  const int base = (blockIdx.x * blockDim.x + threadIdx.x) * ITEMS;
+  int v[ITEMS];
+  int s = 0;
+#pragma unroll
+  for (int k = 0; k < ITEMS; k++) { v[k] = (base + k < n) ? data[base + k] : 0; s += v[k]; }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int inc = s;
+  for (int o = 1; o < 32; o <<= 1) { int t = __shfl_up_sync(0xffffffffu, inc, o); if (lane >= o) inc += t; }
+  if (lane == 31) warp_tot[w] = inc;
+  __syncthreads();
+  if (w == 0) {
+    const int nw = blockDim.x >> 5;
+    int t = lane < nw ? warp_tot[lane] : 0;
+    int ti = t;
+    for (int o = 1; o < 32; o <<= 1) { int u = __shfl_up_sync(0xffffffffu, ti, o); if (lane >= o) ti += u; }
+    if (lane < nw) warp_tot[lane] = ti - t;
+    if (lane == nw - 1 && block_sums) block_sums[blockIdx.x] = ti;
+  }
+  __syncthreads();
+  int run = warp_tot[w] + inc - s;
+#pragma unroll
+  for (int k = 0; k < ITEMS; k++) { if (base + k < n) data[base + k] = run; run += v[k]; }
+}
+static __global__ void k_scan_add(int n, int *__restrict__ data, const int *__restrict__ block_sums) {
+  constexpr int ITEMS = 4;
+  const int base = (blockIdx.x * blockDim.x + threadIdx.x) * ITEMS;
+  const int add = block_sums[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < ITEMS; k++) if (base + k < n) data[base + k] += add;
+}
+
+struct Scanner {
+  static constexpr int THREADS = 1024, PER_BLOCK = THREADS * 4;
+  std::vector<DBuf<int>> levels;
+  void prepare(size_t n) {
+    levels.clear();
+    size_t m = n;
+    while (true) {
+      size_t blocks = (m + PER_BLOCK - 1) / PER_BLOCK;
+      levels.emplace_back();
+      levels.back().alloc(std::max<size_t>(blocks, 1));
+      if (blocks <= 1) break;
+      m = blocks;
+    }
+  }
+  // exclusive scan of data[0..n)
+  void run(int *data, int n, cudaStream_t s, int64_t &launches, int level = 0) {
+    const int blocks = (n + PER_BLOCK - 1) / PER_BLOCK;
+    int *bs = levels[level].p;
+    k_scan_block<<<blocks, THREADS, 0, s>>>(n, data, blocks > 1 ? bs : nullptr);
+    launches++;
+    if (blocks > 1) {
+      run(bs, blocks, s, launches, level + 1);
+      k_scan_add<<<blocks, THREADS, 0, s>>>(n, data, bs);
+      launches++;
+    }
+  }
+};
+
+// ----------------------------------------------------------------- engine
+template <class T>
+class Engine : public EngineBase {
+ public:
+  explicit Engine(const dfsph_scene *sc);
+  ~Engine() override;
+
+  int step(int nsteps, dfsph_step_stats *st) override;
+  void reset() override;
+  void reset_gradient() override;
+  void set_rigid_init(int b, const double *v, const double *w) override;
+  void get_rigid_init(int b, double *v, double *w) override;
+  void get_rigid_state(int b, double *x, double *q, double *v, double *w) override;
+  void set_rigid_velocity(int b, const double *v, const double *w) override;
+  void get_rigid_force(int b, double *F, double *Tq) override;
+  void get_rigid_mass(int b, double *m, double *I) override;
+  void get_rigid_grad(int b, double *out) override;
+  void get_net_jacobians(int b, double *out) override;
+  void backward(const double *dL, double *out) override;
+  int64_t tape_length() override { return tape_len_; }
+  void copy_field(int f, double *dst, int64_t n) override;
+  void set_field(int f, const double *src, int64_t n) override;
+  void counts(int64_t *nf, int64_t *nb) override { *nf = n_; *nb = ns_ + nd_; }
+  void neighbors(int which, int64_t *start, int32_t *idx, int64_t *total) override;
+  void get_time(double *t, int64_t *sc) override { *t = t_; *sc = step_count_; }
+  void synchronize() override { DF_CK(cudaStreamSynchronize(stream_)); }
+  int64_t launches() override { return launches_; }
+  void record_event(int slot) override;
+  double event_elapsed(int a, int b) override;
+  void profile_enable(bool on) override;
+  void profile_read(int k, int64_t *launches, double *ms, int64_t *units) override;
+
+ private:
+  // configuration
+  dfsph_params P_;
+  FluidConsts<T> fc_;
+  RigidConsts rc_;
+  PairConsts<T> pcP_, pcD_;
+  int n_ = 0, ns_ = 0, nd_ = 0, nb_ = 0, kbf_ = 128;
+  int ncell_ = 0;
+  cudaStream_t stream_ = nullptr;
+  int64_t launches_ = 0;
+
+  // host copies
+  std::vector<double> x_init_, v_init_;
+  std::vector<BodyState> body_init_;
+  std::vector<double> init_v_, init_w_;  // per body
+  std::vector<int> body_dyn_, body_anim0_;
+  std::vector<int> static_orig_;   // sorted static index -> boundary index (body-concatenated)
+  std::vector<int> dyn_orig_;      // body-order dynamic index -> boundary index
+  std::vector<int> boundary_is_dyn_, boundary_slot_;  // boundary index -> (dynamic?, slot)
+
+  // fluid (sorted order), double-buffered where the sort gathers
+  DBuf<V4<T>> x_[2], v_[2];
+  DBuf<T> kappa_[2], kappaV_[2];
+  DBuf<int> perm_[2];
+  int cur_ = 0;
+  DBuf<T> kk_, rho_, alpha_, rhoAdv_;
+  DBuf<V4<T>> sumgrad_;
+  DBuf<int> fcount_, flist_, bcount_, blist_;
+  DBuf<int> key_, rank_, order_, cstartF_;
+  // boundary
+  DBuf<V4<T>> bx_, bv_;       // [ns + nd] static (fixed) then dynamic (cell-sorted copy)
+  DBuf<int> cstartS_, cstartD_;
+  DBuf<V4<T>> xd_, vd_, x0d_;  // dynamic, body order
+  DBuf<int> bodyd_, keyD_, rankD_, orderD_, dynSortedToBody_, bfcount_, bflist_;
+  DBuf<double> acc_;
+  DBuf<T> psi_;
+  DBuf<BodyState> bs_;
+  // reductions and flags
+  DBuf<double> partials_, resid_;
+  double *resid_host_ = nullptr;  // pinned, mapped
+  double *resid_host_dev_ = nullptr;
+  DBuf<int> err_;
+  Scanner scan_;
+  // adjoint tape
+  DBuf<double> tape_;
+  int64_t tape_len_ = 0, tape_cap_ = 0;
+
+  // trajectory state (host)
+  double t_ = 0.0;
+  int64_t step_count_ = 0;
+  bool finished_ = false;
+  std::vector<int> anim_;  // current animated flags (host mirror of the begin-step logic)
+  int last_iters_ = 0, last_iters_v_ = 0;
+  double last_err_ = 0.0, last_err_v_ = 0.0;
+
+  // timing: user event slots and per-kernel-class event pairs
+  cudaEvent_t ev_[8] = {};
+  struct ProfRec { int k; cudaEvent_t a, b; int64_t units; };
+  bool prof_on_ = false;
+  std::vector<ProfRec> pending_;
+  std::vector<cudaEvent_t> pool_;
+  cudaEvent_t open_ev_ = nullptr;
+  int64_t prof_launches_[DFSPH_K_COUNT] = {};
+  double prof_ms_[DFSPH_K_COUNT] = {};
+  int64_t prof_units_[DFSPH_K_COUNT] = {};
+  cudaEvent_t take_event() {
+    if (pool_.empty()) { cudaEvent_t e; DF_CK(cudaEventCreate(&e)); return e; }
+    cudaEvent_t e = pool_.back(); pool_.pop_back(); return e;
+  }
+  void pbegin() {
+    if (!prof_on_) return;
+    open_ev_ = take_event();
+    DF_CK(cudaEventRecord(open_ev_, stream_));
+  }
+  void pend(int k, int64_t units) {
+    if (!prof_on_ || !open_ev_) return;
+    cudaEvent_t b = take_event();
+    DF_CK(cudaEventRecord(b, stream_));
+    pending_.push_back({k, open_ev_, b, units});
+    open_ev_ = nullptr;
+  }
+  void resolve_profile();
+
+  int blocks(int n, int t = 256) const { return (n + t - 1) / t; }
+  void launched(int k = 1) { launches_ += k; }
+  void check_launch() { DF_CK(cudaGetLastError()); }
+
+  void sort_fluid();
+  void sort_dynamic();
+  void sort_points(const V4<T> *pts, int count, int *key, int *rank, int *cstart, int *order);
+  void compute_psi();
+  void begin_step();
+  void divergence_solve();
+  void pressure_solve();
+  void rigid_end();
+  double read_residual();
+  void grow_tape();
+  void upload_fluid_initial();
+  void body_state_download(std::vector<BodyState> &out);
+  void body_state_upload(const std::vector<BodyState> &in);
+  void check_error_word();
+};
+
+}  // namespace dfsph

@@ -1,0 +1,948 @@
+// engine_impl.cuh — Engine<T> member definitions (included by engine_fp32.cu / engine_fp64.cu).
+#pragma once
+#include "engine.cuh"
+
+namespace dfsph {
+
+namespace {
+inline void rotate_unit_q(const double q[4], const double p[3], double out[3]) {
+  // v + w (2 u x v) + u x (2 u x v), the rotation of a unit quaternion
+  const double u[3] = {q[1], q[2], q[3]};
+  double uv[3] = {u[1] * p[2] - u[2] * p[1], u[2] * p[0] - u[0] * p[2], u[0] * p[1] - u[1] * p[0]};
+  for (int k = 0; k < 3; k++) uv[k] += uv[k];
+  const double uuv[3] = {u[1] * uv[2] - u[2] * uv[1], u[2] * uv[0] - u[0] * uv[2], u[0] * uv[1] - u[1] * uv[0]};
+  for (int k = 0; k < 3; k++) out[k] = p[k] + q[0] * uv[k] + uuv[k];
+}
+inline void q_to_R_h(const double *q, double *R) {
+  const double w = q[0], x = q[1], y = q[2], z = q[3];
+  const double tx = 2 * x, ty = 2 * y, tz = 2 * z;
+  const double twx = tx * w, twy = ty * w, twz = tz * w, txx = tx * x, txy = ty * x, txz = tz * x;
+  const double tyy = ty * y, tyz = tz * y, tzz = tz * z;
+  R[0] = 1 - (tyy + tzz); R[1] = txy - twz; R[2] = txz + twy;
+  R[3] = txy + twz; R[4] = 1 - (txx + tzz); R[5] = tyz - twx;
+  R[6] = txz - twy; R[7] = tyz + twx; R[8] = 1 - (txx + tyy);
+}
+inline void inv3_h(const double *m, double *r) {
+  const double c00 = m[4] * m[8] - m[5] * m[7];
+  const double c01 = m[5] * m[6] - m[3] * m[8];
+  const double c02 = m[3] * m[7] - m[4] * m[6];
+  const double det = m[0] * c00 + m[1] * c01 + m[2] * c02;
+  const double id = 1.0 / det;
+  r[0] = c00 * id; r[1] = (m[2] * m[7] - m[1] * m[8]) * id; r[2] = (m[1] * m[5] - m[2] * m[4]) * id;
+  r[3] = c01 * id; r[4] = (m[0] * m[8] - m[2] * m[6]) * id; r[5] = (m[3] * m[2] - m[0] * m[5]) * id;
+  r[6] = c02 * id; r[7] = (m[6] * m[1] - m[0] * m[7]) * id; r[8] = (m[0] * m[4] - m[3] * m[1]) * id;
+}
+inline void world_inertia(BodyState &B) {
+  double R[9], RI[9];
+  q_to_R_h(B.q, R);
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) RI[3 * i + j] = R[3 * i] * B.I0[j] + R[3 * i + 1] * B.I0[3 + j] + R[3 * i + 2] * B.I0[6 + j];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) B.I[3 * i + j] = RI[3 * i] * R[3 * j] + RI[3 * i + 1] * R[3 * j + 1] + RI[3 * i + 2] * R[3 * j + 2];
+  inv3_h(B.I, B.Iinv);
+}
+inline void chain_state_reset(BodyState &B) {
+  for (int k = 0; k < NSTATE * 6; k++) B.G[k] = 0.0;
+  for (int k = 0; k < 3; k++) { B.G[(7 + k) * 6 + k] = 1.0; B.G[(10 + k) * 6 + 3 + k] = 1.0; }
+  for (int k = 0; k < NJAC; k++) B.nets[k] = 0.0;
+}
+}  // namespace
+
+template <class T>
+Engine<T>::Engine(const dfsph_scene *sc) {
+  if (!sc) throw DfsphException(DFSPH_ERR_INVALID_ARG, "scene is NULL");
+  if (sc->struct_size != (int)sizeof(dfsph_scene)) throw DfsphException(DFSPH_ERR_INVALID_ARG, "dfsph_scene.struct_size mismatch");
+  P_ = sc->params;
+  if (P_.struct_size != (int)sizeof(dfsph_params)) throw DfsphException(DFSPH_ERR_INVALID_ARG, "dfsph_params.struct_size mismatch");
+  if (!(P_.particle_radius > 0) || !(P_.time_step > 0) || !(P_.density0 > 0))
+    throw DfsphException(DFSPH_ERR_INVALID_ARG, "particle_radius, time_step and density0 must be positive");
+  if (sc->n_fluid < 0 || sc->n_fluid > (int64_t)INT32_MAX / 2) throw DfsphException(DFSPH_ERR_INVALID_ARG, "n_fluid out of range");
+  if (sc->n_fluid > 0 && !sc->fluid_x) throw DfsphException(DFSPH_ERR_INVALID_ARG, "fluid_x is NULL");
+  if (sc->n_bodies < 0 || sc->n_bodies > DFSPH_MAX_BODIES) throw DfsphException(DFSPH_ERR_INVALID_ARG, "n_bodies out of range");
+  if (sc->n_bodies > 0 && !sc->bodies) throw DfsphException(DFSPH_ERR_INVALID_ARG, "bodies is NULL");
+  if (P_.gradient_mode < 0 || P_.gradient_mode > 2) throw DfsphException(DFSPH_ERR_INVALID_ARG, "gradient_mode");
+  if (P_.max_iterations < 1 || P_.max_iterations_v < 1 || P_.min_iterations < 0)
+    throw DfsphException(DFSPH_ERR_INVALID_ARG, "iteration limits");
+  n_ = (int)sc->n_fluid;
+  nb_ = sc->n_bodies;
+
+  // ---- constants (in the fluid scalar type, as the reference's Real)
+  const T r = (T)P_.particle_radius;
+  const T h = T(4) * r;
+  const T pi = (T)M_PI;
+  const T h3 = h * h * h;
+  fc_.n = n_;
+  fc_.kc.h = h;
+  fc_.kc.k = T(8) / (pi * h3);
+  fc_.kc.l = T(48) / (pi * h3);
+  fc_.kc.w0 = fc_.kc.k;  // W(0) = k (6*0 - 6*0 + 1)
+  fc_.h2 = h * h;
+  fc_.rho0 = (T)P_.density0;
+  const T diam = T(2) * r;
+  fc_.V = T(0.8) * diam * diam * diam;
+  fc_.m = fc_.V * fc_.rho0;
+  fc_.dt = (T)P_.time_step;
+  fc_.invH = T(1) / fc_.dt;
+  fc_.invH2 = T(1) / (fc_.dt * fc_.dt);
+  fc_.eps = T(1.0e-5);
+  fc_.visc = (T)P_.viscosity;
+  fc_.gx = (T)P_.gravity[0]; fc_.gy = (T)P_.gravity[1]; fc_.gz = (T)P_.gravity[2];
+  fc_.kf = P_.max_fluid_neighbors > 0 ? P_.max_fluid_neighbors : 96;
+  fc_.kb = P_.max_boundary_neighbors > 0 ? P_.max_boundary_neighbors : 96;
+  // gradient coefficients: computeGradient's Real 1/dt/dt, 1/dt and the unsigned copy of :1266
+  const T cg2 = T(1) / fc_.dt / fc_.dt, cg1 = T(1) / fc_.dt;
+  pcP_.cReal = cg2;
+  pcD_.cReal = cg1;
+  pcP_.cTrunc = P_.truncate_gradient_coeff ? (T)(unsigned int)cg2 : cg2;
+  pcD_.cTrunc = P_.truncate_gradient_coeff ? (T)(unsigned int)cg1 : cg1;
+  pcP_.optimize_rotation = pcD_.optimize_rotation = P_.optimize_rotation;
+  rc_.dt = (double)fc_.dt;
+  rc_.gx = (double)fc_.gx; rc_.gy = (double)fc_.gy; rc_.gz = (double)fc_.gz;
+  rc_.gradient_mode = P_.gradient_mode;
+  rc_.gyroscopic = P_.rigid_body_mode == DFSPH_RB_GYROSCOPIC;
+  rc_.optimize_rotation = P_.optimize_rotation;
+  rc_.enable_gradient = P_.enable_gradient;
+
+  // ---- bodies (mass model of Dynamic3dRigidBody::determineMassProperties, :184-213)
+  std::vector<double> static_world;  // xyz
+  std::vector<int> static_orig_unsorted;
+  std::vector<double> dyn_local;
+  std::vector<int> dyn_body;
+  int boundary_index = 0;
+  const double rr = (double)r;
+  for (int b = 0; b < nb_; b++) {
+    const dfsph_body_desc &d = sc->bodies[b];
+    if (d.n_samples < 0 || (d.n_samples > 0 && !d.samples)) throw DfsphException(DFSPH_ERR_INVALID_ARG, "body samples");
+    BodyState B;
+    std::memset(&B, 0, sizeof(B));
+    const double qn = std::sqrt(d.rotation[0] * d.rotation[0] + d.rotation[1] * d.rotation[1] +
+                                d.rotation[2] * d.rotation[2] + d.rotation[3] * d.rotation[3]);
+    if (!(qn > 0)) throw DfsphException(DFSPH_ERR_INVALID_ARG, "body rotation quaternion is zero");
+    for (int k = 0; k < 4; k++) B.q[k] = d.rotation[k] / qn;
+    for (int k = 0; k < 3; k++) B.x[k] = d.translation[k];
+    const double vol = static_cast<double>(4.0 / 3.0 * M_PI) * rr * rr * rr;
+    const double dm = vol * d.density;
+    for (int s = 0; s < d.n_samples; s++) {
+      const double p[3] = {d.samples[3 * s], d.samples[3 * s + 1], d.samples[3 * s + 2]};
+      const double pp = p[0] * p[0] + p[1] * p[1] + p[2] * p[2];
+      B.mass += dm;
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) B.I0[3 * i + j] += dm * ((i == j ? pp : 0.0) - p[i] * p[j]);
+    }
+    B.invMass = B.mass > 0 ? 1.0 / B.mass : 0.0;
+    B.dyn = d.is_dynamic ? 1 : 0;
+    B.anim = d.is_animated ? 1 : 0;
+    world_inertia(B);
+    chain_state_reset(B);
+    body_dyn_.push_back(B.dyn);
+    body_anim0_.push_back(B.anim);
+    init_v_.insert(init_v_.end(), d.init_velocity, d.init_velocity + 3);
+    init_w_.insert(init_w_.end(), d.init_angular_velocity, d.init_angular_velocity + 3);
+    if (B.dyn) {
+      B.dstart = nd_;
+      B.dcount = (int)d.n_samples;
+      for (int s = 0; s < d.n_samples; s++) {
+        for (int k = 0; k < 3; k++) dyn_local.push_back((double)(T)d.samples[3 * s + k]);
+        dyn_body.push_back(b);
+        dyn_orig_.push_back(boundary_index + s);
+      }
+      nd_ += (int)d.n_samples;
+    } else {
+      for (int s = 0; s < d.n_samples; s++) {
+        const double p[3] = {(double)(T)d.samples[3 * s], (double)(T)d.samples[3 * s + 1], (double)(T)d.samples[3 * s + 2]};
+        double w[3];
+        rotate_unit_q(B.q, p, w);
+        for (int k = 0; k < 3; k++) static_world.push_back((double)(T)(w[k] + B.x[k]));
+        static_orig_unsorted.push_back(boundary_index + s);
+      }
+      ns_ += (int)d.n_samples;
+    }
+    boundary_index += (int)d.n_samples;
+    body_init_.push_back(B);
+  }
+  anim_ = body_anim0_;
+  boundary_is_dyn_.assign(boundary_index, 0);
+  boundary_slot_.assign(boundary_index, 0);
+
+  // ---- grid over fluid + boundary (+ dynamic bodies' reach), padded
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  auto grow = [&](const double *p) { for (int k = 0; k < 3; k++) { lo[k] = std::min(lo[k], p[k]); hi[k] = std::max(hi[k], p[k]); } };
+  for (int i = 0; i < n_; i++) grow(sc->fluid_x + 3 * i);
+  for (size_t s = 0; s < static_world.size() / 3; s++) grow(&static_world[3 * s]);
+  for (int b = 0; b < nb_; b++)
+    if (body_init_[b].dyn) {
+      const dfsph_body_desc &d = sc->bodies[b];
+      for (int s = 0; s < d.n_samples; s++) {
+        double w[3], p[3] = {d.samples[3 * s], d.samples[3 * s + 1], d.samples[3 * s + 2]};
+        rotate_unit_q(body_init_[b].q, p, w);
+        for (int k = 0; k < 3; k++) w[k] += body_init_[b].x[k];
+        grow(w);
+      }
+    }
+  if (lo[0] > hi[0]) { for (int k = 0; k < 3; k++) { lo[k] = 0; hi[k] = 1; } }
+  double cell = (double)h * (1.0 + 1e-4);
+  const double pad = 3.0 * cell;
+  double ext[3];
+  for (int k = 0; k < 3; k++) { lo[k] -= pad; hi[k] += pad; ext[k] = hi[k] - lo[k]; }
+  const double max_cells = 64.0 * 1024 * 1024;
+  while ((ext[0] / cell + 1) * (ext[1] / cell + 1) * (ext[2] / cell + 1) > max_cells) cell *= 1.25;
+  fc_.grid.ox = (T)lo[0]; fc_.grid.oy = (T)lo[1]; fc_.grid.oz = (T)lo[2];
+  fc_.grid.inv_cell = (T)(1.0 / cell);
+  fc_.grid.nx = (int)std::ceil(ext[0] / cell) + 1;
+  fc_.grid.ny = (int)std::ceil(ext[1] / cell) + 1;
+  fc_.grid.nz = (int)std::ceil(ext[2] / cell) + 1;
+  ncell_ = fc_.grid.nx * fc_.grid.ny * fc_.grid.nz;
+
+  DF_CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  scan_.prepare((size_t)ncell_ + 1);
+
+  // ---- fluid buffers
+  x_init_.assign(sc->fluid_x, sc->fluid_x + 3 * (size_t)n_);
+  v_init_.assign(3 * (size_t)n_, 0.0);
+  if (sc->fluid_v) v_init_.assign(sc->fluid_v, sc->fluid_v + 3 * (size_t)n_);
+  const size_t N = std::max(n_, 1);
+  for (int k = 0; k < 2; k++) { x_[k].alloc(N); v_[k].alloc(N); kappa_[k].alloc(N); kappaV_[k].alloc(N); perm_[k].alloc(N); }
+  kk_.alloc(N); rho_.alloc(N); alpha_.alloc(N); rhoAdv_.alloc(N); sumgrad_.alloc(N);
+  fcount_.alloc(N); bcount_.alloc(N);
+  flist_.alloc(N * (size_t)fc_.kf);
+  blist_.alloc(N * (size_t)fc_.kb);
+  key_.alloc(N); rank_.alloc(N); order_.alloc(N);
+  cstartF_.alloc((size_t)ncell_ + 1);
+  cstartS_.alloc((size_t)ncell_ + 1);
+  cstartD_.alloc((size_t)ncell_ + 1);
+  partials_.alloc((size_t)blocks(std::max(n_, 1)));
+  resid_.alloc(4);
+  err_.alloc(1);
+  DF_CK(cudaHostAlloc((void **)&resid_host_, 4 * sizeof(double), cudaHostAllocMapped));
+  DF_CK(cudaHostGetDevicePointer((void **)&resid_host_dev_, resid_host_, 0));
+  DF_CK(cudaMemsetAsync(err_.p, 0, sizeof(int), stream_));
+
+  // ---- boundary buffers
+  const size_t NB = std::max(ns_ + nd_, 1);
+  bx_.alloc(NB); bv_.alloc(NB); psi_.alloc(NB);
+  const size_t ND = std::max(nd_, 1);
+  xd_.alloc(ND); vd_.alloc(ND); x0d_.alloc(ND); bodyd_.alloc(ND); keyD_.alloc(ND); rankD_.alloc(ND);
+  orderD_.alloc(ND); dynSortedToBody_.alloc(ND); bfcount_.alloc(ND); bflist_.alloc(ND * (size_t)kbf_);
+  acc_.alloc(ND * ACC_STRIDE);
+  bs_.alloc(std::max(nb_, 1));
+  DF_CK(cudaMemsetAsync(bv_.p, 0, NB * sizeof(V4<T>), stream_));
+  DF_CK(cudaMemsetAsync(acc_.p, 0, ND * ACC_STRIDE * sizeof(double), stream_));
+  if (nd_ > 0) {
+    std::vector<V4<T>> x0h(nd_);
+    for (int d = 0; d < nd_; d++) x0h[d] = V4<T>{(T)dyn_local[3 * d], (T)dyn_local[3 * d + 1], (T)dyn_local[3 * d + 2], T(0)};
+    DF_CK(cudaMemcpyAsync(x0d_.p, x0h.data(), nd_ * sizeof(V4<T>), cudaMemcpyHostToDevice, stream_));
+    DF_CK(cudaMemcpyAsync(bodyd_.p, dyn_body.data(), nd_ * sizeof(int), cudaMemcpyHostToDevice, stream_));
+    DF_CK(cudaMemsetAsync(xd_.p, 0, nd_ * sizeof(V4<T>), stream_));
+    for (int d = 0; d < nd_; d++) { boundary_is_dyn_[dyn_orig_[d]] = 1; boundary_slot_[dyn_orig_[d]] = d; }
+  }
+  // static samples: sorted by cell once
+  DF_CK(cudaMemsetAsync(cstartS_.p, 0, ((size_t)ncell_ + 1) * sizeof(int), stream_));
+  if (ns_ > 0) {
+    std::vector<V4<T>> sh(ns_);
+    for (int s = 0; s < ns_; s++) sh[s] = V4<T>{(T)static_world[3 * s], (T)static_world[3 * s + 1], (T)static_world[3 * s + 2], T(0)};
+    DBuf<V4<T>> tmp; tmp.alloc(ns_);
+    DBuf<int> k1, k2, k3;
+    k1.alloc(ns_); k2.alloc(ns_); k3.alloc(ns_);
+    DF_CK(cudaMemcpyAsync(tmp.p, sh.data(), ns_ * sizeof(V4<T>), cudaMemcpyHostToDevice, stream_));
+    sort_points(tmp.p, ns_, k1.p, k2.p, cstartS_.p, k3.p);
+    std::vector<int> order(ns_);
+    DF_CK(cudaMemcpyAsync(order.data(), k3.p, ns_ * sizeof(int), cudaMemcpyDeviceToHost, stream_));
+    DF_CK(cudaStreamSynchronize(stream_));
+    std::vector<V4<T>> sorted(ns_);
+    static_orig_.resize(ns_);
+    for (int s = 0; s < ns_; s++) {
+      sorted[s] = sh[order[s]];
+      static_orig_[s] = static_orig_unsorted[order[s]];
+      boundary_is_dyn_[static_orig_[s]] = 0;
+      boundary_slot_[static_orig_[s]] = s;
+    }
+    DF_CK(cudaMemcpyAsync(bx_.p, sorted.data(), ns_ * sizeof(V4<T>), cudaMemcpyHostToDevice, stream_));
+    DF_CK(cudaStreamSynchronize(stream_));
+  } else {
+    // keep the empty table's scan consistent (all zero)
+  }
+  if (nd_ > 0 && P_.enable_gradient) {
+    tape_cap_ = 256;
+    tape_.alloc((size_t)tape_cap_ * nb_ * NSTATE * NSTATE);
+  }
+  reset();
+}
+
+template <class T>
+Engine<T>::~Engine() {
+  if (stream_) cudaStreamSynchronize(stream_);
+  for (auto &e : ev_) if (e) cudaEventDestroy(e);
+  for (auto &r : pending_) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+  for (auto &e : pool_) cudaEventDestroy(e);
+  if (resid_host_) cudaFreeHost(resid_host_);
+  if (stream_) cudaStreamDestroy(stream_);
+}
+
+template <class T>
+void Engine<T>::sort_points(const V4<T> *pts, int count, int *key, int *rank, int *cstart, int *order) {
+  DF_CK(cudaMemsetAsync(cstart, 0, ((size_t)ncell_ + 1) * sizeof(int), stream_));
+  if (count == 0) return;
+  k_cell_keys<T><<<blocks(count), 256, 0, stream_>>>(count, pts, fc_.grid, key, rank, cstart, err_.p);
+  launched();
+  scan_.run(cstart, ncell_ + 1, stream_, launches_);
+  k_scatter_order<<<blocks(count), 256, 0, stream_>>>(count, key, rank, cstart, order);
+  k_cell_insertion_sort<<<blocks(ncell_), 256, 0, stream_>>>(ncell_, cstart, order);
+  launched(2);
+  check_launch();
+}
+
+template <class T>
+void Engine<T>::sort_fluid() {
+  if (n_ == 0) {
+    DF_CK(cudaMemsetAsync(cstartF_.p, 0, ((size_t)ncell_ + 1) * sizeof(int), stream_));
+    return;
+  }
+  pbegin();
+  sort_points(x_[cur_].p, n_, key_.p, rank_.p, cstartF_.p, order_.p);
+  const int nx = 1 - cur_;
+  k_gather_fluid<T><<<blocks(n_), 256, 0, stream_>>>(n_, order_.p, x_[cur_].p, v_[cur_].p, kappa_[cur_].p,
+                                                     kappaV_[cur_].p, perm_[cur_].p, x_[nx].p, v_[nx].p,
+                                                     kappa_[nx].p, kappaV_[nx].p, perm_[nx].p);
+  launched();
+  pend(DFSPH_K_SORT, n_);
+  cur_ = nx;
+}
+
+template <class T>
+void Engine<T>::sort_dynamic() {
+  if (nd_ == 0) return;
+  pbegin();
+  sort_points(xd_.p, nd_, keyD_.p, rankD_.p, cstartD_.p, orderD_.p);
+  k_gather_dynamic<T><<<blocks(nd_), 256, 0, stream_>>>(nd_, ns_, orderD_.p, xd_.p, vd_.p, bx_.p, bv_.p,
+                                                        dynSortedToBody_.p);
+  launched();
+  pend(DFSPH_K_SORT, nd_);
+}
+
+template <class T>
+void Engine<T>::compute_psi() {
+  if (ns_ + nd_ == 0) return;
+  k_boundary_psi<T><<<blocks(ns_ + nd_), 256, 0, stream_>>>(fc_, ns_, nd_, bx_.p, cstartS_.p,
+                                                            nd_ ? cstartD_.p : nullptr, psi_.p);
+  k_set_psi<T><<<blocks(ns_ + nd_), 256, 0, stream_>>>(ns_, nd_, psi_.p, bx_.p, xd_.p, dynSortedToBody_.p);
+  launched(2);
+  check_launch();
+}
+
+template <class T>
+void Engine<T>::upload_fluid_initial() {
+  cur_ = 0;
+  if (n_ == 0) return;
+  std::vector<V4<T>> xh(n_), vh(n_);
+  std::vector<int> ph(n_);
+  for (int i = 0; i < n_; i++) {
+    xh[i] = V4<T>{(T)x_init_[3 * i], (T)x_init_[3 * i + 1], (T)x_init_[3 * i + 2], T(0)};
+    vh[i] = V4<T>{(T)v_init_[3 * i], (T)v_init_[3 * i + 1], (T)v_init_[3 * i + 2], T(0)};
+    ph[i] = i;
+  }
+  DF_CK(cudaMemcpyAsync(x_[0].p, xh.data(), n_ * sizeof(V4<T>), cudaMemcpyHostToDevice, stream_));
+  DF_CK(cudaMemcpyAsync(v_[0].p, vh.data(), n_ * sizeof(V4<T>), cudaMemcpyHostToDevice, stream_));
+  DF_CK(cudaMemcpyAsync(perm_[0].p, ph.data(), n_ * sizeof(int), cudaMemcpyHostToDevice, stream_));
+  DF_CK(cudaMemsetAsync(kappa_[0].p, 0, n_ * sizeof(T), stream_));
+  DF_CK(cudaMemsetAsync(kappaV_[0].p, 0, n_ * sizeof(T), stream_));
+  DF_CK(cudaMemsetAsync(rho_.p, 0, n_ * sizeof(T), stream_));
+  DF_CK(cudaMemsetAsync(alpha_.p, 0, n_ * sizeof(T), stream_));
+  DF_CK(cudaMemsetAsync(rhoAdv_.p, 0, n_ * sizeof(T), stream_));
+  DF_CK(cudaMemsetAsync(sumgrad_.p, 0, n_ * sizeof(V4<T>), stream_));
+  DF_CK(cudaMemsetAsync(fcount_.p, 0, n_ * sizeof(int), stream_));
+  DF_CK(cudaMemsetAsync(bcount_.p, 0, n_ * sizeof(int), stream_));
+  // perm[1] must also be a valid permutation before the first gather
+  DF_CK(cudaMemcpyAsync(perm_[1].p, ph.data(), n_ * sizeof(int), cudaMemcpyHostToDevice, stream_));
+  DF_CK(cudaStreamSynchronize(stream_));
+}
+
+template <class T>
+void Engine<T>::body_state_download(std::vector<BodyState> &out) {
+  out.resize(nb_);
+  if (nb_ == 0) return;
+  DF_CK(cudaStreamSynchronize(stream_));
+  DF_CK(cudaMemcpy(out.data(), bs_.p, nb_ * sizeof(BodyState), cudaMemcpyDeviceToHost));
+}
+template <class T>
+void Engine<T>::body_state_upload(const std::vector<BodyState> &in) {
+  if (nb_ == 0) return;
+  DF_CK(cudaMemcpyAsync(bs_.p, in.data(), nb_ * sizeof(BodyState), cudaMemcpyHostToDevice, stream_));
+  DF_CK(cudaStreamSynchronize(stream_));
+}
+
+template <class T>
+void Engine<T>::reset() {
+  DF_CK(cudaStreamSynchronize(stream_));
+  upload_fluid_initial();
+  std::vector<BodyState> bsv = body_init_;  // pose x0/q0, v = omega = 0 (Dynamic3dRigidBody::reset)
+  anim_ = body_anim0_;
+  body_state_upload(bsv);
+  if (nd_ > 0) {
+    k_boundary_update<T><<<blocks(nd_), 256, 0, stream_>>>(bs_.p, nd_, x0d_.p, bodyd_.p, xd_.p, vd_.p, 0);
+    launched();
+    DF_CK(cudaMemsetAsync(acc_.p, 0, (size_t)nd_ * ACC_STRIDE * sizeof(double), stream_));
+  }
+  sort_dynamic();
+  compute_psi();
+  DF_CK(cudaMemsetAsync(err_.p, 0, sizeof(int), stream_));
+  t_ = 0.0;
+  step_count_ = 0;
+  finished_ = false;
+  tape_len_ = 0;
+  DF_CK(cudaStreamSynchronize(stream_));
+}
+
+template <class T>
+void Engine<T>::reset_gradient() {
+  std::vector<BodyState> bsv;
+  body_state_download(bsv);
+  for (auto &B : bsv) chain_state_reset(B);
+  body_state_upload(bsv);
+  if (nd_ > 0) DF_CK(cudaMemsetAsync(acc_.p, 0, (size_t)nd_ * ACC_STRIDE * sizeof(double), stream_));
+  tape_len_ = 0;
+  DF_CK(cudaStreamSynchronize(stream_));
+}
+
+// TimeStepDiffDFSPH::beginStep (:353-430)
+template <class T>
+void Engine<T>::begin_step() {
+  step_count_++;
+  if (nb_ == 0) return;
+  BeginCmd cmd;
+  std::memset(&cmd, 0, sizeof(cmd));
+  cmd.n = nb_;
+  const double uat = P_.uniform_accelerate_rb_time, dt = P_.time_step;
+  for (int b = 0; b < nb_; b++) {
+    if (!body_dyn_[b]) { cmd.anim[b] = anim_[b]; continue; }
+    if (P_.release_rigid_body_mode) {
+      if (b == 1) {
+        if (t_ <= uat + dt) {
+          if (uat > 1e-3) anim_[b] = 1;
+          cmd.set[b] = 1;
+        } else {
+          cmd.set[b] = 1;
+          for (int k = 0; k < 3; k++) { cmd.v[b][k] = init_v_[3 * b + k]; cmd.w[b][k] = init_w_[3 * b + k]; }
+          anim_[b] = 0;
+        }
+      }
+    } else {
+      if (t_ <= uat + dt) {
+        double fac = 1.0;
+        if (uat > 1e-3) { fac = (t_ / uat) > 1.0 ? 1.0 : (t_ / uat); anim_[b] = 1; }
+        cmd.set[b] = 1;
+        for (int k = 0; k < 3; k++) { cmd.v[b][k] = fac * init_v_[3 * b + k]; cmd.w[b][k] = fac * init_w_[3 * b + k]; }
+      } else {
+        anim_[b] = 0;
+      }
+    }
+    cmd.anim[b] = anim_[b];
+  }
+  k_rigid_begin<<<1, 32, 0, stream_>>>(bs_.p, cmd);
+  launched();
+}
+
+template <class T>
+double Engine<T>::read_residual() {
+  DF_CK(cudaStreamSynchronize(stream_));
+  const int e = (int)resid_host_[1];
+  if (e) check_error_word();
+  return resid_host_[0];
+}
+
+template <class T>
+void Engine<T>::check_error_word() {
+  int e = 0;
+  DF_CK(cudaMemcpy(&e, err_.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) {
+    std::string m = "device error word:";
+    if (e & ERR_FLUID_LIST_OVERFLOW) m += " fluid neighbour list overflow (raise max_fluid_neighbors);";
+    if (e & ERR_BOUNDARY_LIST_OVERFLOW) m += " boundary neighbour list overflow (raise max_boundary_neighbors);";
+    if (e & ERR_BF_LIST_OVERFLOW) m += " dynamic-boundary fluid list overflow;";
+    if (e & ERR_NONFINITE_POSITION) m += " non-finite particle position;";
+    throw DfsphException(DFSPH_ERR_DEVICE, m);
+  }
+}
+
+// divergenceSolve (TimeStepDiffDFSPH.cpp:770-881)
+template <class T>
+void Engine<T>::divergence_solve() {
+  const int nbk = blocks(n_);
+  V4<T> *X = x_[cur_].p, *V = v_[cur_].p;
+  T *kV = kappaV_[cur_].p;
+  const int ndw = blocks(nd_ * 32, 128);
+  if (P_.use_divergence_warmstart) {
+    { pbegin(); k_density_pass<T, PASS_DIVERGENCE_WARM><<<nbk, 256, 0, stream_>>>(fc_, X, V, bx_.p, bv_.p, flist_.p, fcount_.p,
+                                                                     blist_.p, bcount_.p, rho_.p, alpha_.p,
+                                                                     rhoAdv_.p, kk_.p, kV, nullptr); pend(DFSPH_K_DENSITY_PASS, n_); }
+    if (nd_) { pbegin(); k_pairs<T, 1, true, false><<<ndw, 128, 0, stream_>>>(fc_, pcD_, nd_, xd_.p, vd_.p, x0d_.p, bodyd_.p, bs_.p,
+                                                                   bflist_.p, bfcount_.p, X, V, alpha_.p, rhoAdv_.p,
+                                                                   sumgrad_.p, kV, acc_.p); pend(DFSPH_K_PAIRS, nd_); }
+    { pbegin(); k_velocity_pass<T, 0><<<nbk, 256, 0, stream_>>>(fc_, X, V, bx_.p, flist_.p, fcount_.p, blist_.p, bcount_.p, kk_.p,
+                                                    nullptr); pend(DFSPH_K_VELOCITY_PASS, n_); }
+    launched(nd_ ? 3 : 2);
+  }
+  { pbegin(); k_density_pass<T, PASS_DIVERGENCE><<<nbk, 256, 0, stream_>>>(fc_, X, V, bx_.p, bv_.p, flist_.p, fcount_.p, blist_.p,
+                                                               bcount_.p, rho_.p, alpha_.p, rhoAdv_.p, kk_.p, nullptr,
+                                                               nullptr); pend(DFSPH_K_DENSITY_PASS, n_); }
+  launched();
+  int it = 0;
+  bool chk = false;
+  double avg = 0.0;
+  const T eta = (T(1) / fc_.dt) * (T)P_.max_error_v * T(0.01) * fc_.rho0;
+  const int maxIt = P_.max_iterations_v;
+  while ((!chk || it < 1) && it < maxIt) {
+    if (nd_) {
+      if (P_.enable_gradient)
+        { pbegin(); k_pairs<T, 1, false, true><<<ndw, 128, 0, stream_>>>(fc_, pcD_, nd_, xd_.p, vd_.p, x0d_.p, bodyd_.p, bs_.p,
+                                                             bflist_.p, bfcount_.p, X, V, alpha_.p, rhoAdv_.p,
+                                                             sumgrad_.p, kk_.p, acc_.p); pend(DFSPH_K_PAIRS, nd_); }
+      else
+        { pbegin(); k_pairs<T, 1, false, false><<<ndw, 128, 0, stream_>>>(fc_, pcD_, nd_, xd_.p, vd_.p, x0d_.p, bodyd_.p, bs_.p,
+                                                              bflist_.p, bfcount_.p, X, V, alpha_.p, rhoAdv_.p,
+                                                              sumgrad_.p, kk_.p, acc_.p); pend(DFSPH_K_PAIRS, nd_); }
+      launched();
+    }
+    if (P_.use_divergence_warmstart)
+      { pbegin(); k_velocity_pass<T, 1><<<nbk, 256, 0, stream_>>>(fc_, X, V, bx_.p, flist_.p, fcount_.p, blist_.p, bcount_.p,
+                                                      kk_.p, kV); pend(DFSPH_K_VELOCITY_PASS, n_); }
+    else
+      { pbegin(); k_velocity_pass<T, 0><<<nbk, 256, 0, stream_>>>(fc_, X, V, bx_.p, flist_.p, fcount_.p, blist_.p, bcount_.p,
+                                                      kk_.p, nullptr); pend(DFSPH_K_VELOCITY_PASS, n_); }
+    const bool need = (it + 1 >= 1) || (it + 1 >= maxIt);
+    { pbegin(); k_density_pass<T, PASS_DIVERGENCE><<<nbk, 256, 0, stream_>>>(fc_, X, V, bx_.p, bv_.p, flist_.p, fcount_.p,
+                                                                 blist_.p, bcount_.p, rho_.p, alpha_.p, rhoAdv_.p,
+                                                                 kk_.p, nullptr, need ? partials_.p : nullptr); pend(DFSPH_K_DENSITY_PASS, n_); }
+    launched(2);
+    if (need) {
+      k_final_sum<<<1, 32, 0, stream_>>>(nbk, partials_.p, 1.0 / (double)std::max(n_, 1), resid_.p, resid_host_dev_,
+                                         err_.p);
+      launched();
+      check_launch();
+      avg = read_residual();
+      chk = (T)avg <= eta;
+    }
+    it++;
+  }
+  last_iters_v_ = it;
+  last_err_v_ = avg;
+}
+
+// pressureSolve (TimeStepDiffDFSPH.cpp:654-768)
+template <class T>
+void Engine<T>::pressure_solve() {
+  const int nbk = blocks(n_);
+  V4<T> *X = x_[cur_].p, *V = v_[cur_].p;
+  T *kP = kappa_[cur_].p;
+  const int ndw = blocks(nd_ * 32, 128);
+  if (P_.use_pressure_warmstart) {
+    { pbegin(); k_density_pass<T, PASS_PRESSURE_WARM><<<nbk, 256, 0, stream_>>>(fc_, X, V, bx_.p, bv_.p, flist_.p, fcount_.p,
+                                                                   blist_.p, bcount_.p, rho_.p, alpha_.p, rhoAdv_.p,
+                                                                   kk_.p, kP, nullptr); pend(DFSPH_K_DENSITY_PASS, n_); }
+    if (nd_) { pbegin(); k_pairs<T, 0, true, false><<<ndw, 128, 0, stream_>>>(fc_, pcP_, nd_, xd_.p, vd_.p, x0d_.p, bodyd_.p, bs_.p,
+                                                                   bflist_.p, bfcount_.p, X, V, alpha_.p, rhoAdv_.p,
+                                                                   sumgrad_.p, kP, acc_.p); pend(DFSPH_K_PAIRS, nd_); }
+    { pbegin(); k_velocity_pass<T, 0><<<nbk, 256, 0, stream_>>>(fc_, X, V, bx_.p, flist_.p, fcount_.p, blist_.p, bcount_.p, kk_.p,
+                                                    nullptr); pend(DFSPH_K_VELOCITY_PASS, n_); }
+    launched(nd_ ? 3 : 2);
+  }
+  { pbegin(); k_density_pass<T, PASS_PRESSURE><<<nbk, 256, 0, stream_>>>(fc_, X, V, bx_.p, bv_.p, flist_.p, fcount_.p, blist_.p,
+                                                             bcount_.p, rho_.p, alpha_.p, rhoAdv_.p, kk_.p, nullptr,
+                                                             nullptr); pend(DFSPH_K_DENSITY_PASS, n_); }
+  launched();
+  int it = 0;
+  bool chk = false;
+  double avg = 0.0;
+  const T eta = (T)P_.max_error * T(0.01) * fc_.rho0;
+  const int minIt = P_.min_iterations, maxIt = P_.max_iterations;
+  while ((!chk || it < minIt) && it < maxIt) {
+    if (nd_) {
+      if (P_.enable_gradient)
+        { pbegin(); k_pairs<T, 0, false, true><<<ndw, 128, 0, stream_>>>(fc_, pcP_, nd_, xd_.p, vd_.p, x0d_.p, bodyd_.p, bs_.p,
+                                                             bflist_.p, bfcount_.p, X, V, alpha_.p, rhoAdv_.p,
+                                                             sumgrad_.p, kk_.p, acc_.p); pend(DFSPH_K_PAIRS, nd_); }
+      else
+        { pbegin(); k_pairs<T, 0, false, false><<<ndw, 128, 0, stream_>>>(fc_, pcP_, nd_, xd_.p, vd_.p, x0d_.p, bodyd_.p, bs_.p,
+                                                              bflist_.p, bfcount_.p, X, V, alpha_.p, rhoAdv_.p,
+                                                              sumgrad_.p, kk_.p, acc_.p); pend(DFSPH_K_PAIRS, nd_); }
+      launched();
+    }
+    if (P_.use_pressure_warmstart)
+      { pbegin(); k_velocity_pass<T, 1><<<nbk, 256, 0, stream_>>>(fc_, X, V, bx_.p, flist_.p, fcount_.p, blist_.p, bcount_.p,
+                                                      kk_.p, kP); pend(DFSPH_K_VELOCITY_PASS, n_); }
+    else
+      { pbegin(); k_velocity_pass<T, 0><<<nbk, 256, 0, stream_>>>(fc_, X, V, bx_.p, flist_.p, fcount_.p, blist_.p, bcount_.p,
+                                                      kk_.p, nullptr); pend(DFSPH_K_VELOCITY_PASS, n_); }
+    const bool need = (it + 1 >= minIt) || (it + 1 >= maxIt);
+    { pbegin(); k_density_pass<T, PASS_PRESSURE><<<nbk, 256, 0, stream_>>>(fc_, X, V, bx_.p, bv_.p, flist_.p, fcount_.p, blist_.p,
+                                                               bcount_.p, rho_.p, alpha_.p, rhoAdv_.p, kk_.p, nullptr,
+                                                               need ? partials_.p : nullptr); pend(DFSPH_K_DENSITY_PASS, n_); }
+    launched(2);
+    if (need) {
+      k_final_sum<<<1, 32, 0, stream_>>>(nbk, partials_.p, 1.0 / (double)std::max(n_, 1), resid_.p, resid_host_dev_,
+                                         err_.p);
+      launched();
+      check_launch();
+      avg = read_residual();
+      chk = (T)avg <= eta;
+    }
+    it++;
+  }
+  last_iters_ = it;
+  last_err_ = avg;
+}
+
+template <class T>
+void Engine<T>::grow_tape() {
+  const int64_t ncap = std::max<int64_t>(tape_cap_ * 2, 256);
+  DBuf<double> nt;
+  nt.alloc((size_t)ncap * nb_ * NSTATE * NSTATE);
+  if (tape_len_ > 0)
+    DF_CK(cudaMemcpyAsync(nt.p, tape_.p, (size_t)tape_len_ * nb_ * NSTATE * NSTATE * sizeof(double),
+                          cudaMemcpyDeviceToDevice, stream_));
+  DF_CK(cudaStreamSynchronize(stream_));
+  std::swap(tape_.p, nt.p);
+  std::swap(tape_.n, nt.n);
+  tape_cap_ = ncap;
+}
+
+// backwardPerStep's chain rule (:493-524) + velocityTimeStep + positionTimeStep +
+// updateBoundaryParticles, all on the device.
+template <class T>
+void Engine<T>::rigid_end() {
+  if (nd_ == 0) return;
+  pbegin();
+  k_body_reduce<T><<<nb_, RED_VALUES * RED_PARTS, 0, stream_>>>(bs_.p, nb_, xd_.p, acc_.p);
+  double *tape_step = nullptr;
+  if (P_.enable_gradient) {
+    if (tape_len_ >= tape_cap_) grow_tape();
+    tape_step = tape_.p + (size_t)tape_len_ * nb_ * NSTATE * NSTATE;
+    tape_len_++;
+  }
+  k_rigid_step<<<nb_, 128, 0, stream_>>>(bs_.p, nb_, rc_, tape_step);
+  k_boundary_update<T><<<blocks(nd_), 256, 0, stream_>>>(bs_.p, nd_, x0d_.p, bodyd_.p, xd_.p, vd_.p, 1);
+  launched(3);
+  pend(DFSPH_K_RIGID, nd_);
+  check_launch();
+}
+
+template <class T>
+int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
+  if (nsteps < 0) throw DfsphException(DFSPH_ERR_INVALID_ARG, "nsteps < 0");
+  int rc = DFSPH_OK;
+  int64_t ti = 0, tv = 0;
+  for (int s = 0; s < nsteps; s++) {
+    begin_step();
+    sort_fluid();
+    sort_dynamic();
+    if (n_ > 0) {
+      { pbegin(); k_lists_density_factor<T><<<blocks(n_), 256, 0, stream_>>>(fc_, x_[cur_].p, cstartF_.p, bx_.p, cstartS_.p,
+                                                                 nd_ ? cstartD_.p : nullptr, ns_, flist_.p, fcount_.p,
+                                                                 blist_.p, bcount_.p, rho_.p, alpha_.p, sumgrad_.p,
+                                                                 err_.p); pend(DFSPH_K_LISTS_DENSITY, n_); }
+      launched();
+      if (nd_) {
+        { pbegin(); k_bf_lists<T><<<blocks(nd_), 256, 0, stream_>>>(fc_, nd_, xd_.p, x_[cur_].p, cstartF_.p, kbf_, bflist_.p,
+                                                        bfcount_.p, err_.p); pend(DFSPH_K_BF_LISTS, nd_); }
+        launched();
+      }
+      check_launch();
+      if (P_.enable_divergence_solver) divergence_solve();
+      else { last_iters_v_ = 0; last_err_v_ = 0.0; }
+      const int nv = 1 - cur_;
+      { pbegin(); k_xsph_advect<T><<<blocks(n_), 256, 0, stream_>>>(fc_, x_[cur_].p, v_[cur_].p, v_[nv].p, flist_.p, fcount_.p,
+                                                        rho_.p, kappaV_[cur_].p,
+                                                        (P_.enable_divergence_solver && P_.use_divergence_warmstart) ? 1 : 0); pend(DFSPH_K_XSPH, n_); }
+      launched();
+      // the advected velocity lives in the other buffer: swap the velocity pair only
+      std::swap(v_[cur_].p, v_[nv].p);
+      pressure_solve();
+      { pbegin(); k_integrate<T><<<blocks(n_), 256, 0, stream_>>>(fc_, x_[cur_].p, v_[cur_].p, kappa_[cur_].p,
+                                                      P_.use_pressure_warmstart ? 1 : 0); pend(DFSPH_K_INTEGRATE, n_); }
+      launched();
+    } else {
+      last_iters_ = last_iters_v_ = 0;
+    }
+    t_ += P_.time_step;
+    rigid_end();
+    finished_ = t_ >= P_.target_time + P_.uniform_accelerate_rb_time;
+    ti += last_iters_;
+    tv += last_iters_v_;
+    if (last_iters_ >= P_.max_iterations || (P_.enable_divergence_solver && last_iters_v_ >= P_.max_iterations_v))
+      rc = DFSPH_ERR_NOT_CONVERGED;
+  }
+  DF_CK(cudaStreamSynchronize(stream_));
+  check_error_word();
+  if (st) {
+    st->steps_done = nsteps;
+    st->pressure_iterations = last_iters_;
+    st->divergence_iterations = last_iters_v_;
+    st->trajectory_finished = finished_ ? 1 : 0;
+    st->pressure_avg_error = last_err_;
+    st->divergence_avg_error = last_err_v_;
+    st->total_pressure_iterations = ti;
+    st->total_divergence_iterations = tv;
+    st->time = t_;
+  }
+  return rc;
+}
+
+// ----------------------------------------------------------------- accessors
+template <class T>
+void Engine<T>::set_rigid_init(int b, const double *v, const double *w) {
+  if (b < 0 || b >= nb_) throw DfsphException(DFSPH_ERR_INVALID_ARG, "body index");
+  for (int k = 0; k < 3; k++) { init_v_[3 * b + k] = v[k]; init_w_[3 * b + k] = w[k]; }
+}
+template <class T>
+void Engine<T>::get_rigid_init(int b, double *v, double *w) {
+  if (b < 0 || b >= nb_) throw DfsphException(DFSPH_ERR_INVALID_ARG, "body index");
+  for (int k = 0; k < 3; k++) { v[k] = init_v_[3 * b + k]; w[k] = init_w_[3 * b + k]; }
+}
+template <class T>
+void Engine<T>::get_rigid_state(int b, double *x, double *q, double *v, double *w) {
+  if (b < 0 || b >= nb_) throw DfsphException(DFSPH_ERR_INVALID_ARG, "body index");
+  BodyState B;
+  DF_CK(cudaStreamSynchronize(stream_));
+  DF_CK(cudaMemcpy(&B, bs_.p + b, sizeof(BodyState), cudaMemcpyDeviceToHost));
+  for (int k = 0; k < 3; k++) { if (x) x[k] = B.x[k]; if (v) v[k] = B.v[k]; if (w) w[k] = B.w[k]; }
+  if (q) for (int k = 0; k < 4; k++) q[k] = B.q[k];
+}
+template <class T>
+void Engine<T>::set_rigid_velocity(int b, const double *v, const double *w) {
+  if (b < 0 || b >= nb_) throw DfsphException(DFSPH_ERR_INVALID_ARG, "body index");
+  std::vector<BodyState> bsv;
+  body_state_download(bsv);
+  for (int k = 0; k < 3; k++) { bsv[b].v[k] = v[k]; bsv[b].w[k] = w[k]; }
+  body_state_upload(bsv);
+  if (nd_ > 0) {
+    k_boundary_update<T><<<blocks(nd_), 256, 0, stream_>>>(bs_.p, nd_, x0d_.p, bodyd_.p, xd_.p, vd_.p, 1);
+    launched();
+    DF_CK(cudaStreamSynchronize(stream_));
+  }
+}
+template <class T>
+void Engine<T>::get_rigid_force(int b, double *F, double *Tq) {
+  if (b < 0 || b >= nb_) throw DfsphException(DFSPH_ERR_INVALID_ARG, "body index");
+  std::vector<BodyState> bsv;
+  body_state_download(bsv);
+  for (int k = 0; k < 3; k++) { F[k] = bsv[b].F[k]; Tq[k] = bsv[b].T[k]; }
+}
+template <class T>
+void Engine<T>::get_rigid_mass(int b, double *m, double *I) {
+  if (b < 0 || b >= nb_) throw DfsphException(DFSPH_ERR_INVALID_ARG, "body index");
+  std::vector<BodyState> bsv;
+  body_state_download(bsv);
+  *m = bsv[b].mass;
+  for (int k = 0; k < 9; k++) I[k] = bsv[b].I[k];
+}
+template <class T>
+void Engine<T>::get_rigid_grad(int b, double *out) {
+  if (b < 0 || b >= nb_) throw DfsphException(DFSPH_ERR_INVALID_ARG, "body index");
+  std::vector<BodyState> bsv;
+  body_state_download(bsv);
+  const double *G = bsv[b].G;
+  double *o = out;
+  // x_v0 x_w0 q_v0 q_w0 v_v0 v_w0 w_v0 w_w0
+  const int r0[4] = {0, 3, 7, 10}, nr[4] = {3, 4, 3, 3};
+  for (int blk = 0; blk < 4; blk++)
+    for (int c0 = 0; c0 < 6; c0 += 3)
+      for (int r = 0; r < nr[blk]; r++)
+        for (int c = 0; c < 3; c++) *o++ = G[(r0[blk] + r) * 6 + c0 + c];
+}
+template <class T>
+void Engine<T>::get_net_jacobians(int b, double *out) {
+  if (b < 0 || b >= nb_) throw DfsphException(DFSPH_ERR_INVALID_ARG, "body index");
+  std::vector<BodyState> bsv;
+  body_state_download(bsv);
+  for (int k = 0; k < NJAC; k++) out[k] = bsv[b].nets[k];
+}
+template <class T>
+void Engine<T>::backward(const double *dL, double *out) {
+  if (!dL || !out) throw DfsphException(DFSPH_ERR_INVALID_ARG, "NULL buffer");
+  std::vector<double> lam(dL, dL + (size_t)NSTATE * nb_), res((size_t)NSTATE * nb_);
+  if (tape_len_ > 0 && nb_ > 0) {
+    DBuf<double> li, lo;
+    li.alloc(lam.size());
+    lo.alloc(lam.size());
+    DF_CK(cudaMemcpyAsync(li.p, lam.data(), lam.size() * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    k_backward<<<nb_, 32, 0, stream_>>>(tape_.p, (int)tape_len_, nb_, li.p, lo.p);
+    launched();
+    check_launch();
+    DF_CK(cudaMemcpyAsync(res.data(), lo.p, res.size() * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    DF_CK(cudaStreamSynchronize(stream_));
+  } else {
+    res = lam;
+  }
+  for (int b = 0; b < nb_; b++)
+    for (int k = 0; k < 6; k++) out[6 * b + k] = res[(size_t)NSTATE * b + 7 + k];
+}
+
+template <class T>
+void Engine<T>::copy_field(int f, double *dst, int64_t n) {
+  DF_CK(cudaStreamSynchronize(stream_));
+  const bool bfield = f == DFSPH_FIELD_BOUNDARY_X || f == DFSPH_FIELD_BOUNDARY_V || f == DFSPH_FIELD_BOUNDARY_PSI;
+  const int comps = (f == DFSPH_FIELD_X || f == DFSPH_FIELD_V || f == DFSPH_FIELD_SUM_GRAD_P ||
+                     f == DFSPH_FIELD_BOUNDARY_X || f == DFSPH_FIELD_BOUNDARY_V) ? 3 : 1;
+  const int64_t rows = bfield ? (ns_ + nd_) : n_;
+  if (f < 0 || f > DFSPH_FIELD_BOUNDARY_PSI) throw DfsphException(DFSPH_ERR_INVALID_ARG, "field id");
+  if (n != rows * comps) throw DfsphException(DFSPH_ERR_INVALID_ARG, "field buffer size mismatch");
+  if (!bfield) {
+    if (n_ == 0) return;
+    std::vector<int> perm(n_);
+    DF_CK(cudaMemcpy(perm.data(), perm_[cur_].p, n_ * sizeof(int), cudaMemcpyDeviceToHost));
+    if (comps == 3) {
+      std::vector<V4<T>> h(n_);
+      const V4<T> *src = f == DFSPH_FIELD_X ? x_[cur_].p : (f == DFSPH_FIELD_V ? v_[cur_].p : sumgrad_.p);
+      DF_CK(cudaMemcpy(h.data(), src, n_ * sizeof(V4<T>), cudaMemcpyDeviceToHost));
+      for (int i = 0; i < n_; i++) {
+        double *o = dst + 3 * (size_t)perm[i];
+        o[0] = h[i].x; o[1] = h[i].y; o[2] = h[i].z;
+      }
+    } else {
+      std::vector<T> h(n_);
+      const T *src = f == DFSPH_FIELD_DENSITY ? rho_.p
+                     : f == DFSPH_FIELD_FACTOR ? alpha_.p
+                     : f == DFSPH_FIELD_KAPPA ? kappa_[cur_].p
+                     : f == DFSPH_FIELD_KAPPA_V ? kappaV_[cur_].p
+                                                : rhoAdv_.p;
+      DF_CK(cudaMemcpy(h.data(), src, n_ * sizeof(T), cudaMemcpyDeviceToHost));
+      for (int i = 0; i < n_; i++) dst[perm[i]] = h[i];
+    }
+    return;
+  }
+  std::vector<V4<T>> sx(ns_), sd(nd_);
+  const bool wantv = f == DFSPH_FIELD_BOUNDARY_V;
+  if (ns_) DF_CK(cudaMemcpy(sx.data(), wantv ? bv_.p : bx_.p, ns_ * sizeof(V4<T>), cudaMemcpyDeviceToHost));
+  if (nd_) DF_CK(cudaMemcpy(sd.data(), wantv ? vd_.p : xd_.p, nd_ * sizeof(V4<T>), cudaMemcpyDeviceToHost));
+  auto put = [&](int orig, const V4<T> &p) {
+    if (f == DFSPH_FIELD_BOUNDARY_PSI) dst[orig] = p.w;
+    else { dst[3 * (size_t)orig] = p.x; dst[3 * (size_t)orig + 1] = p.y; dst[3 * (size_t)orig + 2] = p.z; }
+  };
+  for (int s = 0; s < ns_; s++) put(static_orig_[s], sx[s]);
+  for (int d = 0; d < nd_; d++) put(dyn_orig_[d], sd[d]);
+}
+
+template <class T>
+void Engine<T>::set_field(int f, const double *src, int64_t n) {
+  DF_CK(cudaStreamSynchronize(stream_));
+  const int comps = (f == DFSPH_FIELD_X || f == DFSPH_FIELD_V) ? 3 : 1;
+  if (!(f == DFSPH_FIELD_X || f == DFSPH_FIELD_V || f == DFSPH_FIELD_KAPPA || f == DFSPH_FIELD_KAPPA_V))
+    throw DfsphException(DFSPH_ERR_INVALID_ARG, "field is not settable");
+  if (n != (int64_t)n_ * comps) throw DfsphException(DFSPH_ERR_INVALID_ARG, "field buffer size mismatch");
+  if (n_ == 0) return;
+  std::vector<int> perm(n_);
+  DF_CK(cudaMemcpy(perm.data(), perm_[cur_].p, n_ * sizeof(int), cudaMemcpyDeviceToHost));
+  if (comps == 3) {
+    std::vector<V4<T>> h(n_);
+    for (int i = 0; i < n_; i++) {
+      const double *s = src + 3 * (size_t)perm[i];
+      h[i] = V4<T>{(T)s[0], (T)s[1], (T)s[2], T(0)};
+    }
+    DF_CK(cudaMemcpy(f == DFSPH_FIELD_X ? x_[cur_].p : v_[cur_].p, h.data(), n_ * sizeof(V4<T>), cudaMemcpyHostToDevice));
+  } else {
+    std::vector<T> h(n_);
+    for (int i = 0; i < n_; i++) h[i] = (T)src[perm[i]];
+    DF_CK(cudaMemcpy(f == DFSPH_FIELD_KAPPA ? kappa_[cur_].p : kappaV_[cur_].p, h.data(), n_ * sizeof(T),
+                     cudaMemcpyHostToDevice));
+  }
+}
+
+template <class T>
+void Engine<T>::neighbors(int which, int64_t *start, int32_t *idx, int64_t *total) {
+  DF_CK(cudaStreamSynchronize(stream_));
+  if (step_count_ == 0) throw DfsphException(DFSPH_ERR_STATE, "no neighbour search has run yet");
+  std::vector<std::vector<int32_t>> rows;
+  std::vector<int> perm(std::max(n_, 1));
+  if (n_) DF_CK(cudaMemcpy(perm.data(), perm_[cur_].p, n_ * sizeof(int), cudaMemcpyDeviceToHost));
+  std::vector<int> d2b(std::max(nd_, 1));
+  if (nd_) DF_CK(cudaMemcpy(d2b.data(), dynSortedToBody_.p, nd_ * sizeof(int), cudaMemcpyDeviceToHost));
+  auto bmap = [&](int k) { return k < ns_ ? static_orig_[k] : dyn_orig_[d2b[k - ns_]]; };
+  if (which == DFSPH_NB_FLUID_FLUID || which == DFSPH_NB_FLUID_BOUNDARY) {
+    const int K = which == DFSPH_NB_FLUID_FLUID ? fc_.kf : fc_.kb;
+    std::vector<int> cnt(std::max(n_, 1)), lst((size_t)std::max(n_, 1) * K);
+    if (n_) {
+      DF_CK(cudaMemcpy(cnt.data(), which == DFSPH_NB_FLUID_FLUID ? fcount_.p : bcount_.p, n_ * sizeof(int), cudaMemcpyDeviceToHost));
+      DF_CK(cudaMemcpy(lst.data(), which == DFSPH_NB_FLUID_FLUID ? flist_.p : blist_.p, (size_t)n_ * K * sizeof(int),
+                       cudaMemcpyDeviceToHost));
+    }
+    rows.assign(n_, {});
+    for (int i = 0; i < n_; i++) {
+      auto &r = rows[perm[i]];
+      for (int k = 0; k < cnt[i]; k++) {
+        const int j = lst[(size_t)k * n_ + i];
+        r.push_back(which == DFSPH_NB_FLUID_FLUID ? perm[j] : bmap(j));
+      }
+    }
+  } else if (which == DFSPH_NB_BOUNDARY_FLUID) {
+    rows.assign(ns_ + nd_, {});
+    std::vector<int> cnt(std::max(nd_, 1)), lst((size_t)std::max(nd_, 1) * kbf_);
+    if (nd_) {
+      DF_CK(cudaMemcpy(cnt.data(), bfcount_.p, nd_ * sizeof(int), cudaMemcpyDeviceToHost));
+      DF_CK(cudaMemcpy(lst.data(), bflist_.p, (size_t)nd_ * kbf_ * sizeof(int), cudaMemcpyDeviceToHost));
+    }
+    for (int d = 0; d < nd_; d++) {
+      auto &r = rows[dyn_orig_[d]];
+      for (int k = 0; k < cnt[d]; k++) r.push_back(perm[lst[(size_t)k * nd_ + d]]);
+    }
+  } else {
+    throw DfsphException(DFSPH_ERR_INVALID_ARG, "neighbour set id");
+  }
+  int64_t tot = 0;
+  for (auto &r : rows) { std::sort(r.begin(), r.end()); tot += (int64_t)r.size(); }
+  *total = tot;
+  if (start) {
+    start[0] = 0;
+    for (size_t i = 0; i < rows.size(); i++) start[i + 1] = start[i] + (int64_t)rows[i].size();
+  }
+  if (idx) {
+    int64_t o = 0;
+    for (auto &r : rows) for (int v : r) idx[o++] = v;
+  }
+}
+
+}  // namespace dfsph
+
+namespace dfsph {
+template <class T>
+void Engine<T>::record_event(int slot) {
+  if (slot < 0 || slot >= 8) throw DfsphException(DFSPH_ERR_INVALID_ARG, "event slot");
+  if (!ev_[slot]) DF_CK(cudaEventCreate(&ev_[slot]));
+  DF_CK(cudaEventRecord(ev_[slot], stream_));
+}
+template <class T>
+double Engine<T>::event_elapsed(int a, int b) {
+  if (a < 0 || a >= 8 || b < 0 || b >= 8 || !ev_[a] || !ev_[b]) throw DfsphException(DFSPH_ERR_INVALID_ARG, "event slot");
+  DF_CK(cudaEventSynchronize(ev_[b]));
+  float ms = 0.f;
+  DF_CK(cudaEventElapsedTime(&ms, ev_[a], ev_[b]));
+  return (double)ms;
+}
+template <class T>
+void Engine<T>::resolve_profile() {
+  if (pending_.empty()) return;
+  DF_CK(cudaStreamSynchronize(stream_));
+  for (auto &r : pending_) {
+    float ms = 0.f;
+    DF_CK(cudaEventElapsedTime(&ms, r.a, r.b));
+    prof_launches_[r.k] += 1;
+    prof_ms_[r.k] += ms;
+    prof_units_[r.k] += r.units;
+    pool_.push_back(r.a);
+    pool_.push_back(r.b);
+  }
+  pending_.clear();
+}
+template <class T>
+void Engine<T>::profile_enable(bool on) {
+  resolve_profile();
+  for (int k = 0; k < DFSPH_K_COUNT; k++) { prof_launches_[k] = 0; prof_ms_[k] = 0; prof_units_[k] = 0; }
+  prof_on_ = on;
+}
+template <class T>
+void Engine<T>::profile_read(int k, int64_t *launches, double *ms, int64_t *units) {
+  if (k < 0 || k >= DFSPH_K_COUNT) throw DfsphException(DFSPH_ERR_INVALID_ARG, "kernel class");
+  resolve_profile();
+  if (launches) *launches = prof_launches_[k];
+  if (ms) *ms = prof_ms_[k];
+  if (units) *units = prof_units_[k];
+}
+}  // namespace dfsph

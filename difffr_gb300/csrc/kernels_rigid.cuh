@@ -1,0 +1,637 @@
+// kernels_rigid.cuh — rigid-body side of the step: Akinci2012 pair forces and the
+// reference's per-pair gradient Jacobians (boundary-centric, one warp per dynamic
+// boundary sample), FP64 per-body reductions, the forward-mode chain rule expressed as
+// a 13x13 step matrix, FP64 rigid integration, boundary-sample update and the
+// reverse-mode adjoint sweep over the recorded step matrices.
+#pragma once
+#include "common.cuh"
+#include "kernels_fluid.cuh"
+
+namespace dfsph {
+
+// per-dynamic-sample accumulator row: force[3], then the 78 Jacobian entries in the
+// order Fv Fx Fw (3x3) Fq (3x4) Tw Tv Tx (3x3) Tq (3x4), row-major; padded to 84.
+constexpr int ACC_STRIDE = 84;
+constexpr int ACC_FORCE = 0;
+constexpr int ACC_JAC = 3;
+constexpr int NJAC = 78;
+constexpr int NSTATE = 13;  // x(3) q(4: w,x,y,z) v(3) omega(3)
+
+struct BodyState {
+  double x[3], q[4], v[3], w[3];
+  double mass, invMass;
+  double I0[9], I[9], Iinv[9];
+  double F[3], T[3];      // net fluid force / torque of the last step (BoundaryModel::getForce/getTorque)
+  double nets[NJAC];      // per-step net Jacobians (grad_net_force_to_* / grad_net_torque_to_*)
+  double G[NSTATE * 6];   // forward-mode chain state: rows x q v omega, columns v0 (3) omega0 (3)
+  int dyn, anim, dstart, dcount;  // dynamic samples [dstart, dstart + dcount) in body order
+  int chain_ran;          // 1 if the last step applied the chain rule
+  int pad_;
+};
+
+struct RigidConsts {
+  double dt, gx, gy, gz;
+  int gradient_mode, gyroscopic, optimize_rotation, enable_gradient;
+};
+
+// ------------------------------------------------------------------ small matrices (T)
+template <class T> struct M3 { T a[9]; };
+template <class T> struct M34 { T a[12]; };
+
+template <class T> __device__ __forceinline__ void skew3(V3<T> v, T *m) {
+  m[0] = T(0); m[1] = -v.z; m[2] = v.y;
+  m[3] = v.z; m[4] = T(0); m[5] = -v.x;
+  m[6] = -v.y; m[7] = v.x; m[8] = T(0);
+}
+template <int R, int K, int C, class T> __device__ __forceinline__ void mm(const T *A, const T *B, T *out) {
+#pragma unroll
+  for (int i = 0; i < R; i++)
+#pragma unroll
+    for (int j = 0; j < C; j++) {
+      T s = A[i * K] * B[j];
+#pragma unroll
+      for (int k = 1; k < K; k++) s += A[i * K + k] * B[k * C + j];
+      out[i * C + j] = s;
+    }
+}
+// out = A * B^T for 3x3
+template <class T> __device__ __forceinline__ void mmT3(const T *A, const T *B, T *out) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) out[i * 3 + j] = A[i * 3] * B[j * 3] + A[i * 3 + 1] * B[j * 3 + 1] + A[i * 3 + 2] * B[j * 3 + 2];
+}
+template <class T> __device__ __forceinline__ void inv3(const T *m, T *r) {
+  const T c00 = m[4] * m[8] - m[5] * m[7];
+  const T c01 = m[5] * m[6] - m[3] * m[8];
+  const T c02 = m[3] * m[7] - m[4] * m[6];
+  const T det = m[0] * c00 + m[1] * c01 + m[2] * c02;
+  const T id = T(1) / det;
+  r[0] = c00 * id; r[1] = (m[2] * m[7] - m[1] * m[8]) * id; r[2] = (m[1] * m[5] - m[2] * m[4]) * id;
+  r[3] = c01 * id; r[4] = (m[0] * m[8] - m[2] * m[6]) * id; r[5] = (m[3] * m[2] - m[0] * m[5]) * id;
+  r[6] = c02 * id; r[7] = (m[6] * m[1] - m[0] * m[7]) * id; r[8] = (m[0] * m[4] - m[3] * m[1]) * id;
+}
+// d(R(q) p)/dq, columns (w, x, y, z) (GradientUtils.cpp:9-20)
+template <class T> __device__ __forceinline__ void grad_Rqp(T qw, T qx, T qy, T qz, V3<T> p, T *out) {
+  const V3<T> qv = {qx, qy, qz};
+  const V3<T> pc = cross(p, qv);
+  const T d = dot(qv, p);
+  const T t1[3] = {T(2) * (qw * p.x - pc.x), T(2) * (qw * p.y - pc.y), T(2) * (qw * p.z - pc.z)};
+  const T pv[3] = {p.x, p.y, p.z}, qq[3] = {qx, qy, qz};
+  T sk[9];
+  skew3(p, sk);
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    out[i * 4] = t1[i];
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+      out[i * 4 + 1 + j] = T(2) * ((i == j ? d : T(0)) + qq[i] * pv[j] - pv[i] * qq[j] - qw * sk[i * 3 + j]);
+  }
+}
+// d(R(q)^T p)/dq (GradientUtils.cpp:23-35)
+template <class T> __device__ __forceinline__ void grad_RqTp(T qw, T qx, T qy, T qz, V3<T> p, T *out) {
+  const V3<T> qv = {qx, qy, qz};
+  const V3<T> pc = cross(p, qv);
+  const T d = dot(qv, p);
+  const T t1[3] = {T(2) * (qw * p.x + pc.x), T(2) * (qw * p.y + pc.y), T(2) * (qw * p.z + pc.z)};
+  const T pv[3] = {p.x, p.y, p.z}, qq[3] = {qx, qy, qz};
+  T sk[9];
+  skew3(p, sk);
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    out[i * 4] = t1[i];
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+      out[i * 4 + 1 + j] = T(2) * ((i == j ? d : T(0)) + qq[i] * pv[j] - pv[i] * qq[j] + qw * sk[i * 3 + j]);
+  }
+}
+
+// ------------------------------------------------------------------ pair kernel
+template <class T>
+struct PairConsts {
+  T cReal;    // 1/dt^2 (pressure) or 1/dt (divergence)
+  T cTrunc;   // the same, truncated to unsigned as at TimeStepDiffDFSPH.cpp:1266 (or not)
+  int optimize_rotation;
+};
+
+// One warp per dynamic boundary sample j, lanes over its fluid neighbours i.
+// Force: the Akinci reaction f_ij = -m_i (-dt k_i (-psi_j grad W_ij)) / dt that the
+// fluid-side velocity correction applies (TimeStepDiffDFSPH.cpp:1038-1053, 1139-1196,
+// 1767-1784, 1862-1901), only where |k_i| > eps, k_i the pass's stiffness.
+// Gradient (GRAD): computeRigidBodyGradient + computeGradient (:1226-1482) with the
+// helper derivatives (:1485-1694); the nested neighbour sum of :1632-1694 equals
+// -h sum_grad_p_k (pressure) or -sum_grad_p_k (divergence) exactly, because particle
+// positions do not change between the factor pass and the solver sweeps.
+template <class T, int MODE, bool WARM, bool GRAD>
+static __global__ void __launch_bounds__(128) k_pairs(FluidConsts<T> c, PairConsts<T> pc, int nd,
+                                               const V4<T> *__restrict__ xd, const V4<T> *__restrict__ vd,
+                                               const V4<T> *__restrict__ x0d, const int *__restrict__ bodyd,
+                                               const BodyState *__restrict__ bs, const int *__restrict__ bflist,
+                                               const int *__restrict__ bfcount, const V4<T> *__restrict__ x,
+                                               const V4<T> *__restrict__ v, const T *__restrict__ alpha,
+                                               const T *__restrict__ rhoAdv, const V4<T> *__restrict__ sumgrad,
+                                               const T *__restrict__ kforce, double *__restrict__ acc) {
+  const int d = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (d >= nd) return;
+  const int b = bodyd[d];
+  const BodyState &B = bs[b];
+  if (!B.dyn) return;
+  const bool grad = GRAD && !B.anim;
+  const V4<T> xj4 = xd[d];
+  const V3<T> xj = xyz(xj4);
+  const T psi = xj4.w;
+  const V3<T> vj = xyz(vd[d]);
+  const int cnt = bfcount[d];
+
+  T facc[3] = {T(0), T(0), T(0)};
+  T J[NJAC];
+#pragma unroll
+  for (int k = 0; k < NJAC; k++) J[k] = T(0);
+
+  // per-sample constants of the rotation terms
+  T Grq[12], SoG[12], Srj[9];
+  V3<T> rj = {T(0), T(0), T(0)};
+  if (grad && pc.optimize_rotation) {
+    const T qw = (T)B.q[0], qx = (T)B.q[1], qy = (T)B.q[2], qz = (T)B.q[3];
+    grad_Rqp(qw, qx, qy, qz, xyz(x0d[d]), Grq);
+    T So[9];
+    skew3(V3<T>{(T)B.w[0], (T)B.w[1], (T)B.w[2]}, So);
+    mm<3, 3, 4>(So, Grq, SoG);
+    rj = {xj.x - (T)B.x[0], xj.y - (T)B.x[1], xj.z - (T)B.x[2]};
+    skew3(rj, Srj);
+  }
+
+  for (int k = lane; k < cnt; k += 32) {
+    const int i = bflist[(size_t)k * nd + d];
+    const V4<T> xi4 = x[i];
+    const V3<T> r = {xi4.x - xj.x, xi4.y - xj.y, xi4.z - xj.z};
+    const T rl = sqrt(dot(r, r));
+    const V3<T> g = cubic_gradW(r, rl, c.kc);
+    const V3<T> gpj = (-psi) * g;
+    {
+      const T kF = kforce[i];
+      if (fabs(kF) > c.eps) {
+        const T s = -c.dt * T(1) * kF;
+        facc[0] += (-c.m * (s * gpj.x)) * c.invH;
+        facc[1] += (-c.m * (s * gpj.y)) * c.invH;
+        facc[2] += (-c.m * (s * gpj.z)) * c.invH;
+      }
+    }
+    if (!grad) continue;
+    const T ai = alpha[i], ra = rhoAdv[i];
+    const T b_i = (MODE == 0) ? ra - T(1) : ra;
+    const T ki = b_i * ai * pc.cTrunc;
+    const T sT = -c.dt * T(1) * ki;
+    const V3<T> fT = {(-c.m * (sT * gpj.x)) * c.invH, (-c.m * (sT * gpj.y)) * c.invH, (-c.m * (sT * gpj.z)) * c.invH};
+    const Sym3<T> Hs = cubic_gradGradW(r, rl, c.kc);
+    const V3<T> sg = xyz(sumgrad[i]);
+    const V3<T> dv = xyz(v[i]) - vj;
+    const bool act = (MODE == 0) ? (ra > T(1)) : (ra > T(0));
+    V3<T> gbx = {T(0), T(0), T(0)}, gbv = {T(0), T(0), T(0)}, gbvi = {T(0), T(0), T(0)};
+    if (act) {
+      const V3<T> Hdv = symmul(Hs, dv);
+      if (MODE == 0) {
+        gbx = (T(1) / c.rho0) * gpj - (c.dt * psi) * Hdv;
+        gbv = (-c.dt * psi) * g;
+        gbvi = c.dt * (-sg);
+      } else {
+        gbx = (-psi) * Hdv;
+        gbv = (-psi) * g;
+        gbvi = -sg;
+      }
+    }
+    V3<T> gfx = {T(0), T(0), T(0)};
+    if (!(ai >= T(0))) gfx = (T(2) * ai * ai) * (psi * symmul(Hs, sg));
+    const V3<T> gkx = pc.cReal * (ai * gbx + b_i * gfx);
+    const V3<T> gkv = (ai * pc.cReal) * gbv;
+    const V3<T> gkvi = (ai * pc.cReal) * gbvi;
+    const T gp[3] = {gpj.x, gpj.y, gpj.z};
+    const T kx[3] = {gkx.x, gkx.y, gkx.z}, kv[3] = {gkv.x, gkv.y, gkv.z}, kvi[3] = {gkvi.x, gkvi.y, gkvi.z};
+    const T g2[9] = {psi * Hs.xx, psi * Hs.xy, psi * Hs.xz, psi * Hs.xy, psi * Hs.yy,
+                     psi * Hs.yz, psi * Hs.xz, psi * Hs.yz, psi * Hs.zz};
+    T Fx[9], Mv[9], A[9], Ai[9], Fv[9];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int e = 0; e < 3; e++) {
+        const T gvcx = -(gp[a] * kx[e] + ki * g2[a * 3 + e]);
+        const T gvcv = -(gp[a] * kv[e]);
+        const T gvcvi = -(gp[a] * kvi[e]);
+        Fx[a * 3 + e] = -c.m * gvcx;
+        Mv[a * 3 + e] = -c.m * gvcv;
+        A[a * 3 + e] = (a == e ? T(1) : T(0)) - c.dt * gvcvi;
+      }
+    inv3(A, Ai);
+    mm<3, 3, 3>(Ai, Mv, Fv);
+#pragma unroll
+    for (int k2 = 0; k2 < 9; k2++) { J[k2] += Fv[k2]; J[9 + k2] += Fx[k2]; }
+    if (pc.optimize_rotation) {
+      T Fq[12], t12[12], Fw[9], Tw[9], Sf[9], t12b[12];
+      mm<3, 3, 4>(Fx, Grq, Fq);
+      mm<3, 3, 4>(Fv, SoG, t12);
+#pragma unroll
+      for (int k2 = 0; k2 < 12; k2++) Fq[k2] += t12[k2];
+      mmT3(Fv, Srj, Fw);                       // Fv * skew(rj)^T
+      mm<3, 3, 4>(Srj, Fq, t12);               // skew(rj) * Fq
+      skew3(fT, Sf);
+      T SfT[9] = {Sf[0], Sf[3], Sf[6], Sf[1], Sf[4], Sf[7], Sf[2], Sf[5], Sf[8]};
+      mm<3, 3, 4>(SfT, Grq, t12b);             // skew(force)^T * Grq
+      mm<3, 3, 3>(Srj, Fw, Tw);
+#pragma unroll
+      for (int k2 = 0; k2 < 9; k2++) { J[18 + k2] += Fw[k2]; J[39 + k2] += Tw[k2]; }
+#pragma unroll
+      for (int k2 = 0; k2 < 12; k2++) { J[27 + k2] += Fq[k2]; J[66 + k2] += t12[k2] + t12b[k2]; }
+      T Tv[9], Tx[9];
+      mm<3, 3, 3>(Srj, Fv, Tv);
+      mm<3, 3, 3>(Srj, Fx, Tx);
+#pragma unroll
+      for (int k2 = 0; k2 < 9; k2++) { J[48 + k2] += Tv[k2]; J[57 + k2] += Tx[k2]; }
+    }
+  }
+  // warp reductions (fixed butterfly order), FP32 partials into the FP64 row
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+    for (int o = 16; o > 0; o >>= 1) facc[k] += __shfl_xor_sync(0xffffffffu, facc[k], o);
+  double *row = acc + (size_t)d * ACC_STRIDE;
+  if (lane == 0) {
+    row[ACC_FORCE + 0] += (double)facc[0];
+    row[ACC_FORCE + 1] += (double)facc[1];
+    row[ACC_FORCE + 2] += (double)facc[2];
+  }
+  if (grad) {
+#pragma unroll
+    for (int k = 0; k < NJAC; k++) {
+      T s = J[k];
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) row[ACC_JAC + k] += (double)s;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ per-body reduction
+// One block per body: sums the accumulator rows of its dynamic samples in a fixed
+// order (8 interleaved partials per value, then in order), forms the torque
+// sum (x_j - x_b) x F_j, stores F, T and the net Jacobians, and zeroes the rows
+// (BoundaryModel_Akinci2012::accumulate_and_reset_gradient, :453-497;
+// BoundaryModel::getForceAndTorque / clearForceAndTorque, BoundaryModel.cpp:38-85).
+constexpr int RED_VALUES = 3 + NJAC + 3;  // force, jacobians, torque
+constexpr int RED_PARTS = 8;
+
+template <class T>
+static __global__ void __launch_bounds__(RED_VALUES * RED_PARTS) k_body_reduce(BodyState *__restrict__ bs, int nbodies,
+                                                                        const V4<T> *__restrict__ xd,
+                                                                        double *__restrict__ acc) {
+  __shared__ double part[RED_VALUES * RED_PARTS];
+  const int b = blockIdx.x;
+  if (b >= nbodies) return;
+  BodyState &B = bs[b];
+  if (!B.dyn) return;
+  const int t = threadIdx.x;
+  const int val = t / RED_PARTS, p = t % RED_PARTS;
+  double s = 0.0;
+  if (val < RED_VALUES) {
+    for (int d = B.dstart + p; d < B.dstart + B.dcount; d += RED_PARTS) {
+      const double *row = acc + (size_t)d * ACC_STRIDE;
+      if (val < 3 + NJAC) s += row[val];
+      else {
+        const V4<T> xj = xd[d];
+        const double rx = (double)xj.x - B.x[0], ry = (double)xj.y - B.x[1], rz = (double)xj.z - B.x[2];
+        const double fx = row[0], fy = row[1], fz = row[2];
+        const int comp = val - 3 - NJAC;
+        s += comp == 0 ? ry * fz - rz * fy : (comp == 1 ? rz * fx - rx * fz : rx * fy - ry * fx);
+      }
+    }
+  }
+  part[t] = s;
+  __syncthreads();
+  if (p == 0 && val < RED_VALUES) {
+    double tot = 0.0;
+    for (int k = 0; k < RED_PARTS; k++) tot += part[val * RED_PARTS + k];
+    if (val < 3) B.F[val] = tot;
+    else if (val < 3 + NJAC) B.nets[val - 3] = tot;
+    else B.T[val - 3 - NJAC] = tot;
+  }
+  __syncthreads();
+  for (int k = t; k < B.dcount * ACC_STRIDE; k += blockDim.x) acc[(size_t)B.dstart * ACC_STRIDE + k] = 0.0;
+}
+
+// ------------------------------------------------------------------ chain rule + integration (FP64)
+static __device__ __forceinline__ void q_mul(const double *a, const double *b, double *o) {  // Hamilton, (w,x,y,z)
+  o[0] = a[0] * b[0] - a[1] * b[1] - a[2] * b[2] - a[3] * b[3];
+  o[1] = a[0] * b[1] + a[1] * b[0] + a[2] * b[3] - a[3] * b[2];
+  o[2] = a[0] * b[2] + a[2] * b[0] + a[3] * b[1] - a[1] * b[3];
+  o[3] = a[0] * b[3] + a[3] * b[0] + a[1] * b[2] - a[2] * b[1];
+}
+static __device__ __forceinline__ void q_to_R(const double *q, double *R) {
+  const double w = q[0], x = q[1], y = q[2], z = q[3];
+  const double tx = 2 * x, ty = 2 * y, tz = 2 * z;
+  const double twx = tx * w, twy = ty * w, twz = tz * w, txx = tx * x, txy = ty * x, txz = tz * x;
+  const double tyy = ty * y, tyz = tz * y, tzz = tz * z;
+  R[0] = 1 - (tyy + tzz); R[1] = txy - twz; R[2] = txz + twy;
+  R[3] = txy + twz; R[4] = 1 - (txx + tzz); R[5] = tyz - twx;
+  R[6] = txz - twy; R[7] = tyz + twx; R[8] = 1 - (txx + tyy);
+}
+static __device__ __forceinline__ void mv3(const double *M, const double *v, double *o) {
+  for (int i = 0; i < 3; i++) o[i] = M[3 * i] * v[0] + M[3 * i + 1] * v[1] + M[3 * i + 2] * v[2];
+}
+static __device__ __forceinline__ void cross3(const double *a, const double *b, double *o) {
+  o[0] = a[1] * b[2] - a[2] * b[1]; o[1] = a[2] * b[0] - a[0] * b[2]; o[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+// Coefficients of one step's chain update (BoundaryModel_Akinci2012::perform_chain_rule,
+// :543-889), shared by the 13 columns.
+struct ChainCoef {
+  double R[9], I0[9], I[9], Iinv[9], om[3], Iom[3], temp_v[3];
+  double gRq_a[12], gRTq_a[12];  // for grad_inertia_v(omega, .)
+  double gRq_b[12], gRTq_b[12];  // for grad_inertia_v(Iinv temp_v, .)
+  double Gn[16], Gpq[16], Gpw[12];
+  double invMass;
+};
+
+// gIv(v, Q) = grad_Rqp(q, I0 R^T v) Q + R I0 grad_RqTp(q, v) Q (:513-533) for one column Q.
+static __device__ __forceinline__ void gIv_col(const double *gRq, const double *gRTq, const ChainCoef &C, const double *Q,
+                                        double *o) {
+  double a[3], bq[3], t[3];
+  for (int i = 0; i < 3; i++) {
+    a[i] = gRq[4 * i] * Q[0] + gRq[4 * i + 1] * Q[1] + gRq[4 * i + 2] * Q[2] + gRq[4 * i + 3] * Q[3];
+    bq[i] = gRTq[4 * i] * Q[0] + gRTq[4 * i + 1] * Q[1] + gRTq[4 * i + 2] * Q[2] + gRTq[4 * i + 3] * Q[3];
+  }
+  mv3(C.I0, bq, t);
+  double u[3];
+  mv3(C.R, t, u);
+  for (int i = 0; i < 3; i++) o[i] = a[i] + u[i];
+}
+
+// Applies the chain update to one column s (13) -> o (13).
+static __device__ void chain_column(const BodyState &B, const ChainCoef &C, const RigidConsts &rc, const double *s,
+                             double *o) {
+  const double dt = rc.dt;
+  const double *X = s, *Q = s + 3, *Vv = s + 7, *W = s + 10;
+  double Xn[3], Vn[3], Wn[3], Qn[4];
+  const double *nFv = B.nets, *nFx = B.nets + 9, *nFw = B.nets + 18, *nFq = B.nets + 27;
+  const double *nTw = B.nets + 39, *nTv = B.nets + 48, *nTx = B.nets + 57, *nTq = B.nets + 66;
+  auto m3v = [](const double *M, const double *v, double *out) { mv3(M, v, out); };
+  auto m34v = [](const double *M, const double *v, double *out) {
+    for (int i = 0; i < 3; i++) out[i] = M[4 * i] * v[0] + M[4 * i + 1] * v[1] + M[4 * i + 2] * v[2] + M[4 * i + 3] * v[3];
+  };
+  const bool complete = rc.gradient_mode == 0, rigid_only = rc.gradient_mode == 2;
+  if (!rigid_only) {
+    double gF[3], t1[3], t2[3];
+    m3v(nFv, Vv, gF);
+    m3v(nFw, W, t1);
+    for (int i = 0; i < 3; i++) gF[i] += t1[i];
+    if (complete) {
+      m3v(nFx, X, t1); m34v(nFq, Q, t2);
+      for (int i = 0; i < 3; i++) gF[i] += t1[i] + t2[i];
+    }
+    for (int i = 0; i < 3; i++) Vn[i] = Vv[i] + dt * C.invMass * gF[i];
+    for (int i = 0; i < 3; i++) Xn[i] = X[i] + dt * Vn[i];
+    double gT[3];
+    m3v(nTv, Vn, gT);
+    m3v(nTw, W, t1);
+    for (int i = 0; i < 3; i++) gT[i] += t1[i];
+    if (complete) {
+      m3v(nTx, Xn, t1); m34v(nTq, Q, t2);
+      for (int i = 0; i < 3; i++) gT[i] += t1[i] + t2[i];
+    }
+    double gTau[3];
+    if (rc.gyroscopic) {
+      double g1[3], IW[3], gi[3], sum[3], t3[3];
+      cross3(C.Iom, W, g1);            // skew(I om) W
+      mv3(C.I, W, IW);
+      gIv_col(C.gRq_a, C.gRTq_a, C, Q, gi);
+      for (int i = 0; i < 3; i++) sum[i] = IW[i] + gi[i];
+      cross3(sum, C.om, t3);           // skew(om)^T y = -om x y = y x om
+      for (int i = 0; i < 3; i++) gTau[i] = g1[i] + t3[i] + gT[i];
+    } else {
+      for (int i = 0; i < 3; i++) gTau[i] = gT[i];
+    }
+    double gII[3], tmp[3], iT[3];
+    gIv_col(C.gRq_b, C.gRTq_b, C, Q, tmp);
+    mv3(C.Iinv, tmp, gII);
+    mv3(C.Iinv, gTau, iT);
+    for (int i = 0; i < 3; i++) Wn[i] = W[i] + dt * (gII[i] + iT[i]);
+  } else {
+    for (int i = 0; i < 3; i++) { Vn[i] = Vv[i]; Xn[i] = X[i] + dt * Vv[i]; }
+    if (rc.gyroscopic) {
+      double gII[3], tmp[3], g1[3], IW[3], gi[3], sum[3], t3[3], gL[3], iL[3];
+      gIv_col(C.gRq_b, C.gRTq_b, C, Q, tmp);
+      mv3(C.Iinv, tmp, gII);
+      cross3(C.Iom, W, g1);
+      mv3(C.I, W, IW);
+      gIv_col(C.gRq_a, C.gRTq_a, C, Q, gi);
+      for (int i = 0; i < 3; i++) sum[i] = IW[i] + gi[i];
+      cross3(sum, C.om, t3);
+      for (int i = 0; i < 3; i++) gL[i] = g1[i] + t3[i];
+      mv3(C.Iinv, gL, iL);
+      for (int i = 0; i < 3; i++) Wn[i] = W[i] + dt * (gII[i] + iL[i]);
+    } else {
+      for (int i = 0; i < 3; i++) Wn[i] = W[i];
+    }
+  }
+  if (rc.optimize_rotation) {
+    double inner[4];
+    for (int i = 0; i < 4; i++) {
+      double a = C.Gpw[3 * i] * Wn[0] + C.Gpw[3 * i + 1] * Wn[1] + C.Gpw[3 * i + 2] * Wn[2];
+      double bq = C.Gpq[4 * i] * Q[0] + C.Gpq[4 * i + 1] * Q[1] + C.Gpq[4 * i + 2] * Q[2] + C.Gpq[4 * i + 3] * Q[3];
+      inner[i] = Q[i] + dt / 2.0 * (a + bq);
+    }
+    for (int i = 0; i < 4; i++)
+      Qn[i] = C.Gn[4 * i] * inner[0] + C.Gn[4 * i + 1] * inner[1] + C.Gn[4 * i + 2] * inner[2] + C.Gn[4 * i + 3] * inner[3];
+  } else {
+    for (int i = 0; i < 4; i++) Qn[i] = Q[i];
+  }
+  for (int i = 0; i < 3; i++) { o[i] = Xn[i]; o[7 + i] = Vn[i]; o[10 + i] = Wn[i]; }
+  for (int i = 0; i < 4; i++) o[3 + i] = Qn[i];
+}
+
+static __device__ void grad_Rqp_d(const double *q, const double *p, double *out) {
+  grad_Rqp<double>(q[0], q[1], q[2], q[3], V3<double>{p[0], p[1], p[2]}, out);
+}
+static __device__ void grad_RqTp_d(const double *q, const double *p, double *out) {
+  grad_RqTp<double>(q[0], q[1], q[2], q[3], V3<double>{p[0], p[1], p[2]}, out);
+}
+
+// One block (128 threads) per body: chain rule -> step matrix A (13x13, appended to the
+// tape), G <- A G; then RigidBody3dBoundarySimulator::velocityTimeStep (forces,
+// gyroscopic torque, gravity; :278-320) and positionTimeStep -> animate (:322-344,
+// Dynamic3dRigidBody.h:113-154, 215-235).
+static __global__ void __launch_bounds__(128) k_rigid_step(BodyState *__restrict__ bs, int nbodies, RigidConsts rc,
+                                                    double *__restrict__ tape_step) {
+  __shared__ ChainCoef C;
+  __shared__ double A[NSTATE * NSTATE];
+  __shared__ double Gold[NSTATE * 6];
+  const int b = blockIdx.x;
+  if (b >= nbodies) return;
+  BodyState &B = bs[b];
+  const int t = threadIdx.x;
+  const bool chain = B.dyn && !B.anim && rc.enable_gradient;
+  if (t == 0) B.chain_ran = chain ? 1 : 0;
+  if (chain) {
+    if (t == 0) {
+      q_to_R(B.q, C.R);
+      for (int k = 0; k < 9; k++) { C.I0[k] = B.I0[k]; C.I[k] = B.I[k]; C.Iinv[k] = B.Iinv[k]; }
+      for (int k = 0; k < 3; k++) C.om[k] = B.w[k];
+      mv3(C.I, C.om, C.Iom);
+      C.invMass = 1.0 / (B.mass + 1e-10);
+      // temp_v (:601, :679, :743)
+      if (rc.gradient_mode != 2) {
+        if (rc.gyroscopic) { double cr[3]; cross3(C.Iom, C.om, cr); for (int k = 0; k < 3; k++) C.temp_v[k] = cr[k] + B.T[k]; }
+        else for (int k = 0; k < 3; k++) C.temp_v[k] = B.T[k];
+      } else {
+        if (rc.gyroscopic) cross3(C.Iom, C.om, C.temp_v);
+        else for (int k = 0; k < 3; k++) C.temp_v[k] = 0.0;
+      }
+      // grad_inertia_v operands: v = omega and v = Iinv temp_v
+      double RT[9] = {C.R[0], C.R[3], C.R[6], C.R[1], C.R[4], C.R[7], C.R[2], C.R[5], C.R[8]};
+      double tmp[3], tmp2[3], va[3], vb[3];
+      for (int k = 0; k < 3; k++) va[k] = C.om[k];
+      mv3(C.Iinv, C.temp_v, vb);
+      mv3(RT, va, tmp); mv3(C.I0, tmp, tmp2); grad_Rqp_d(B.q, tmp2, C.gRq_a); grad_RqTp_d(B.q, va, C.gRTq_a);
+      mv3(RT, vb, tmp); mv3(C.I0, tmp, tmp2); grad_Rqp_d(B.q, tmp2, C.gRq_b); grad_RqTp_d(B.q, vb, C.gRTq_b);
+      // rotation block (:827-888)
+      double nom[3];
+      for (int k = 0; k < 3; k++) nom[k] = C.om[k] + rc.dt * vb[k];
+      const double p[4] = {0.0, nom[0], nom[1], nom[2]};
+      double pq[4], nq[4];
+      q_mul(p, B.q, pq);
+      for (int k = 0; k < 4; k++) nq[k] = B.q[k] + rc.dt * 0.5 * pq[k];
+      const double nn = sqrt(nq[0] * nq[0] + nq[1] * nq[1] + nq[2] * nq[2] + nq[3] * nq[3]);
+      double nv[4];
+      for (int k = 0; k < 4; k++) nv[k] = nq[k] / nn;
+      for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) C.Gn[4 * i + j] = ((i == j ? 1.0 : 0.0) - nv[i] * nv[j]) / nn;
+      const double Gpq[16] = {p[0], -p[1], -p[2], -p[3], p[1], p[0], -p[3], p[2],
+                              p[2], p[3], p[0], -p[1], p[3], -p[2], p[1], p[0]};
+      for (int k = 0; k < 16; k++) C.Gpq[k] = Gpq[k];
+      const double *q = B.q;
+      const double Gpw[12] = {-q[1], -q[2], -q[3], q[0], q[3], -q[2], -q[3], q[0], q[1], q[2], -q[1], q[0]};
+      for (int k = 0; k < 12; k++) C.Gpw[k] = Gpw[k];
+    }
+    for (int k = t; k < NSTATE * 6; k += blockDim.x) Gold[k] = B.G[k];
+    __syncthreads();
+    if (t < NSTATE) {
+      double e[NSTATE], col[NSTATE];
+      for (int k = 0; k < NSTATE; k++) e[k] = (k == t) ? 1.0 : 0.0;
+      chain_column(B, C, rc, e, col);
+      for (int k = 0; k < NSTATE; k++) A[k * NSTATE + t] = col[k];
+    }
+    __syncthreads();
+    for (int k = t; k < NSTATE * 6; k += blockDim.x) {
+      const int r = k / 6, cc = k % 6;
+      double s = 0.0;
+      for (int m = 0; m < NSTATE; m++) s += A[r * NSTATE + m] * Gold[m * 6 + cc];
+      B.G[k] = s;
+    }
+    if (tape_step)
+      for (int k = t; k < NSTATE * NSTATE; k += blockDim.x) tape_step[(size_t)b * NSTATE * NSTATE + k] = A[k];
+    __syncthreads();
+  } else if (tape_step) {
+    for (int k = t; k < NSTATE * NSTATE; k += blockDim.x)
+      tape_step[(size_t)b * NSTATE * NSTATE + k] = (k / NSTATE == k % NSTATE) ? 1.0 : 0.0;
+  }
+  if (t == 0 && B.dyn) {
+    const double dt = rc.dt;
+    if (!B.anim) {
+      for (int k = 0; k < 3; k++) B.v[k] += B.invMass * B.F[k] * dt;
+      double d[3], L[3], cr[3];
+      if (rc.gyroscopic) {
+        mv3(B.I, B.w, L);
+        cross3(L, B.w, cr);
+        for (int k = 0; k < 3; k++) cr[k] += B.T[k];
+      } else for (int k = 0; k < 3; k++) cr[k] = B.T[k];
+      mv3(B.Iinv, cr, d);
+      for (int k = 0; k < 3; k++) B.w[k] += d[k] * dt;
+      const double gm[3] = {rc.gx * B.mass, rc.gy * B.mass, rc.gz * B.mass};
+      for (int k = 0; k < 3; k++) B.v[k] += B.invMass * gm[k] * dt;
+    }
+    for (int k = 0; k < 3; k++) B.x[k] += B.v[k] * dt;
+    const double wq[4] = {0.0, B.w[0], B.w[1], B.w[2]};
+    double dq[4];
+    q_mul(wq, B.q, dq);
+    for (int k = 0; k < 4; k++) B.q[k] += dt * 0.5 * dq[k];
+    const double nn = sqrt(B.q[0] * B.q[0] + B.q[1] * B.q[1] + B.q[2] * B.q[2] + B.q[3] * B.q[3]);
+    for (int k = 0; k < 4; k++) B.q[k] /= nn;
+    double R[9], RI[9], RT[9];
+    q_to_R(B.q, R);
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) { RT[3 * i + j] = R[3 * j + i]; }
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) RI[3 * i + j] = R[3 * i] * B.I0[j] + R[3 * i + 1] * B.I0[3 + j] + R[3 * i + 2] * B.I0[6 + j];
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) B.I[3 * i + j] = RI[3 * i] * RT[j] + RI[3 * i + 1] * RT[3 + j] + RI[3 * i + 2] * RT[6 + j];
+    inv3<double>(B.I, B.Iinv);
+  }
+}
+
+// TimeStepDiffDFSPH::beginStep velocity overrides (:379-429), decided on the host.
+struct BeginCmd {
+  int n;
+  int set[DFSPH_MAX_BODIES_DEV];
+  int anim[DFSPH_MAX_BODIES_DEV];
+  double v[DFSPH_MAX_BODIES_DEV][3];
+  double w[DFSPH_MAX_BODIES_DEV][3];
+};
+
+static __global__ void k_rigid_begin(BodyState *__restrict__ bs, BeginCmd cmd) {
+  const int b = threadIdx.x;
+  if (b >= cmd.n) return;
+  BodyState &B = bs[b];
+  if (!B.dyn) return;
+  B.anim = cmd.anim[b];
+  if (cmd.set[b]) {
+    for (int k = 0; k < 3; k++) { B.v[k] = cmd.v[b][k]; B.w[k] = cmd.w[b][k]; }
+  }
+}
+
+// SimulatorBase::updateBoundaryParticles (SimulatorBase.cpp:1827-1857) for dynamic
+// samples: x_j = R(q) x0_j + x_b, v_j = omega x (x_j - x_b) + v_b, in FP64 then stored in T.
+template <class T>
+static __global__ void k_boundary_update(const BodyState *__restrict__ bs, int nd, const V4<T> *__restrict__ x0d,
+                                  const int *__restrict__ bodyd, V4<T> *__restrict__ xd, V4<T> *__restrict__ vd,
+                                  int only_moving) {
+  const int d = blockIdx.x * blockDim.x + threadIdx.x;
+  if (d >= nd) return;
+  const BodyState &B = bs[bodyd[d]];
+  if (only_moving && !(B.dyn || B.anim)) return;
+  const V4<T> p0 = x0d[d];
+  // Quaternion rotation v + w (2 u x v) + u x (2 u x v)
+  const double u[3] = {B.q[1], B.q[2], B.q[3]}, pv[3] = {(double)p0.x, (double)p0.y, (double)p0.z};
+  double uv[3], uuv[3];
+  cross3(u, pv, uv);
+  for (int k = 0; k < 3; k++) uv[k] += uv[k];
+  cross3(u, uv, uuv);
+  double pw[3];
+  for (int k = 0; k < 3; k++) pw[k] = pv[k] + B.q[0] * uv[k] + uuv[k] + B.x[k];
+  const T xs[3] = {(T)pw[0], (T)pw[1], (T)pw[2]};
+  xd[d] = V4<T>{xs[0], xs[1], xs[2], xd[d].w};
+  double rr[3] = {(double)xs[0] - B.x[0], (double)xs[1] - B.x[1], (double)xs[2] - B.x[2]}, vv[3];
+  cross3(B.w, rr, vv);
+  vd[d] = (B.dyn || B.anim) ? V4<T>{(T)(vv[0] + B.v[0]), (T)(vv[1] + B.v[1]), (T)(vv[2] + B.v[2]), T(0)}
+                            : V4<T>{T(0), T(0), T(0), T(0)};
+}
+
+// Reverse sweep: lambda <- A_n^T lambda for n = last..first, one block per body.
+static __global__ void k_backward(const double *__restrict__ tape, int nsteps, int nbodies, const double *__restrict__ lam_in,
+                           double *__restrict__ lam_out) {
+  __shared__ double lam[NSTATE], nl[NSTATE];
+  const int b = blockIdx.x, t = threadIdx.x;
+  if (b >= nbodies) return;
+  if (t < NSTATE) lam[t] = lam_in[b * NSTATE + t];
+  __syncthreads();
+  for (int n = nsteps - 1; n >= 0; n--) {
+    const double *A = tape + ((size_t)n * nbodies + b) * NSTATE * NSTATE;
+    if (t < NSTATE) {
+      double s = 0.0;
+      for (int k = 0; k < NSTATE; k++) s += A[k * NSTATE + t] * lam[k];
+      nl[t] = s;
+    }
+    __syncthreads();
+    if (t < NSTATE) lam[t] = nl[t];
+    __syncthreads();
+  }
+  if (t < NSTATE) lam_out[b * NSTATE + t] = lam[t];
+}
+
+}  // namespace dfsph

@@ -1,0 +1,290 @@
+/*
+ * dfsph.h — C ABI of libdfsph, a GB300 (sm_103a) implementation of DiffFR's
+ * differentiable DFSPH fluid–rigid time step (method "DiffDFSPH", Akinci2012
+ * boundary coupling, forward-mode rigid gradient chain plus a reverse-mode
+ * adjoint over the same chain).
+ *
+ * Conventions
+ *  - Every function returns an int status: DFSPH_OK (0) or a positive error
+ *    code. No C++ exception crosses this boundary. dfsph_last_error() gives a
+ *    human-readable message for the last failing call on the calling thread.
+ *  - A context owns all device memory and one CUDA stream. Calls on one
+ *    context are not thread-safe; distinct contexts are independent.
+ *  - Host buffers are owned by the caller. Positions and velocities cross the
+ *    boundary as row-major double[n][3] in the caller's (original) particle
+ *    order, whatever order the device keeps internally.
+ *  - Quaternions are (w, x, y, z), as the reference's get_quaternion_rb_vec4.
+ *  - Matrices are row-major doubles.
+ *
+ * Each entry point names the reference interface it replaces
+ * (paths relative to the DiffFR repository root).
+ */
+#ifndef DFSPH_H
+#define DFSPH_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DFSPH_ABI_VERSION 1
+
+/* status codes */
+#define DFSPH_OK                  0
+#define DFSPH_ERR_INVALID_ARG     1
+#define DFSPH_ERR_CUDA            2
+#define DFSPH_ERR_NOT_CONVERGED   3  /* solver hit max iterations (informational; state is valid) */
+#define DFSPH_ERR_DEVICE          4  /* device error word set (e.g. neighbour list overflow) */
+#define DFSPH_ERR_OUT_OF_MEMORY   5
+#define DFSPH_ERR_UNSUPPORTED     6
+#define DFSPH_ERR_STATE           7  /* call not valid in the current state */
+
+/* fluid arithmetic precision */
+#define DFSPH_FP32 0
+#define DFSPH_FP64 1
+
+/* reference enum SPH::GradientMode (SPlisHSPlasH/Simulation.h:173) */
+#define DFSPH_GRAD_COMPLETE        0
+#define DFSPH_GRAD_INCOMPLETE      1
+#define DFSPH_GRAD_RIGID_ONLY      2
+
+/* reference enum SPH::RigidBodyMode (SPlisHSPlasH/Simulation.h:174) */
+#define DFSPH_RB_GYROSCOPIC        0
+#define DFSPH_RB_NO_GYROSCOPIC     1
+
+#define DFSPH_MAX_BODIES 16
+
+/*
+ * Scene parameters. Field meanings and defaults follow the reference's
+ * scene "Configuration" keys (SPlisHSPlasH/Utilities/SceneLoader.cpp:41-200)
+ * and the DiffDFSPH parameters (SPlisHSPlasH/DiffDFSPH/TimeStepDiffDFSPH.cpp:90-134,
+ * SPlisHSPlasH/TimeStep.cpp:24-30). dfsph_default_params() fills the defaults.
+ */
+typedef struct dfsph_params {
+  int32_t struct_size;                 /* = sizeof(dfsph_params) */
+  int32_t fluid_precision;             /* DFSPH_FP32 | DFSPH_FP64; rigid state is always FP64 */
+  double  particle_radius;             /* r; kernel support h = 4 r (Simulation.cpp:382-387) */
+  double  density0;                    /* fluid rest density */
+  double  viscosity;                   /* XSPH coefficient, fluid-fluid (Viscosity_XSPH.cpp:66) */
+  double  gravity[3];
+  double  time_step;                   /* fixed dt (cflMethod 0) */
+  int32_t min_iterations;              /* pressure solve, default 2 */
+  int32_t max_iterations;              /* pressure solve, default 100 */
+  double  max_error;                   /* pressure solve, percent, default 0.01 */
+  int32_t max_iterations_v;            /* divergence solve, default 100 */
+  double  max_error_v;                 /* divergence solve, percent, default 0.1 */
+  int32_t enable_divergence_solver;    /* default 1 */
+  int32_t use_pressure_warmstart;      /* default 1 */
+  int32_t use_divergence_warmstart;    /* default 1 */
+  int32_t gradient_mode;               /* DFSPH_GRAD_*, default Incomplete */
+  int32_t rigid_body_mode;             /* DFSPH_RB_*, default gyroscopic */
+  int32_t optimize_rotation;           /* default 1 (TimeStepDiffDFSPH.cpp:108) */
+  int32_t enable_gradient;             /* accumulate pair Jacobians each solver sweep (reference BACKWARD build) */
+  int32_t truncate_gradient_coeff;     /* reproduce the unsigned 1/h^2, 1/h coefficient of
+                                          TimeStepDiffDFSPH.cpp:1266; default 1 */
+  int32_t release_rigid_body_mode;     /* useReleaseRigidBodyMode, default 0 */
+  double  uniform_accelerate_rb_time;  /* uniformAccelerateRBTime, default 0 */
+  double  target_time;                 /* targetTime, default 0.8 */
+  int32_t max_fluid_neighbors;         /* capacity of each fluid particle's fluid list (0 = default 96) */
+  int32_t max_boundary_neighbors;      /* capacity of each fluid particle's boundary list (0 = default 96) */
+} dfsph_params;
+
+/*
+ * One rigid body with Akinci2012 boundary samples (reference: a "RigidBodies"
+ * scene entry, SceneLoader.cpp:95-200; Dynamic3dRigidBody, BoundaryModel_Akinci2012).
+ * Samples are in the body's local frame; world = R(q) sample + translation
+ * (SimulatorBase.cpp:1827-1857). Mass and inertia follow the reference's shell
+ * model (Dynamic3dRigidBody.h:184-213): every sample carries (4/3) pi r^3 * density.
+ */
+typedef struct dfsph_body_desc {
+  int32_t       is_dynamic;
+  int32_t       is_animated;
+  int64_t       n_samples;
+  const double *samples;               /* [n_samples][3] local coordinates */
+  double        translation[3];
+  double        rotation[4];           /* (w, x, y, z) */
+  double        density;
+  double        init_velocity[3];      /* "initVelocity" -> set_init_v_rb */
+  double        init_angular_velocity[3];
+  double        target_x[3];
+} dfsph_body_desc;
+
+typedef struct dfsph_scene {
+  int32_t                struct_size;  /* = sizeof(dfsph_scene) */
+  dfsph_params           params;
+  int64_t                n_fluid;
+  const double          *fluid_x;      /* [n_fluid][3] */
+  const double          *fluid_v;      /* [n_fluid][3] or NULL for zero */
+  int32_t                n_bodies;
+  const dfsph_body_desc *bodies;
+} dfsph_scene;
+
+/* Per-step statistics (reference counters "DFSPH - iterations",
+   "DFSPH - iterationsV", TimeStepDiffDFSPH.cpp:750,863). */
+typedef struct dfsph_step_stats {
+  int32_t steps_done;
+  int32_t pressure_iterations;         /* last step */
+  int32_t divergence_iterations;       /* last step */
+  int32_t trajectory_finished;         /* is_trajectory_finish_callback() after the last step */
+  double  pressure_avg_error;          /* last step, kg/m^3 (rho0 * (rho_adv - 1) averaged) */
+  double  divergence_avg_error;        /* last step */
+  int64_t total_pressure_iterations;   /* summed over the steps of this call */
+  int64_t total_divergence_iterations;
+  double  time;                        /* simulated time after the call */
+} dfsph_step_stats;
+
+/* Fluid fields for dfsph_copy_field (reference FluidModel / SimulationDataDiffDFSPH
+   accessors, SimulationDataDiffDFSPH.h:254-266). Vector fields have 3 components. */
+#define DFSPH_FIELD_X          0  /* position, 3 */
+#define DFSPH_FIELD_V          1  /* velocity, 3 */
+#define DFSPH_FIELD_DENSITY    2
+#define DFSPH_FIELD_FACTOR     3  /* alpha */
+#define DFSPH_FIELD_KAPPA      4
+#define DFSPH_FIELD_KAPPA_V    5
+#define DFSPH_FIELD_DENSITY_ADV 6
+#define DFSPH_FIELD_SUM_GRAD_P 7  /* sum_grad_p_k, 3 */
+#define DFSPH_FIELD_BOUNDARY_X   8   /* boundary positions, 3, body-concatenated order */
+#define DFSPH_FIELD_BOUNDARY_V   9   /* boundary velocities, 3 */
+#define DFSPH_FIELD_BOUNDARY_PSI 10  /* boundary psi volume */
+
+/* Neighbour sets for dfsph_get_neighbors (reference Simulation::numberOfNeighbors /
+   getNeighbor, Simulation.h:526-534). Indices are in the caller's particle order. */
+#define DFSPH_NB_FLUID_FLUID     0   /* fluid i -> fluid j (j != i) */
+#define DFSPH_NB_FLUID_BOUNDARY  1   /* fluid i -> boundary k (all bodies) */
+#define DFSPH_NB_BOUNDARY_FLUID  2   /* dynamic boundary k -> fluid i (rows for static k are empty) */
+
+/* Library */
+int         dfsph_abi_version(void);
+const char *dfsph_last_error(void);
+/* Fills defaults of the reference (see dfsph_params). */
+int         dfsph_default_params(dfsph_params *out);
+
+typedef struct dfsph_ctx dfsph_ctx;
+
+/* Selects the CUDA device that the next dfsph_create uses (the library keeps its own
+   current device; default 0). One process per GPU: call once at start-up. */
+int dfsph_set_device(int32_t device);
+
+/* Replaces SimulatorBase::init + initSimulation + deferredInit for a DiffDFSPH scene
+   (Simulator/SimulatorBase.cpp:494-588, Simulation::setSimulationMethod(5)
+   SPlisHSPlasH/Simulation.cpp:714-719, RigidBody3dBoundarySimulator::initBoundaryData /
+   deferredInit Simulator/RigidBody3dBoundarySimulator.cpp:68-270,
+   Simulation::updateBoundaryVolume Simulation.cpp:831-900). Uses the current CUDA device. */
+int dfsph_create(const dfsph_scene *scene, dfsph_ctx **out);
+int dfsph_destroy(dfsph_ctx *ctx);
+
+/* Replaces SimulatorBase::reset (SimulatorBase.cpp:887-934): fluid back to the
+   scene state, bodies to their initial pose, psi recomputed, gradients reset,
+   time 0. Initial rigid velocities set by dfsph_set_rigid_init are kept. */
+int dfsph_reset(dfsph_ctx *ctx);
+
+/* Replaces nsteps iterations of SimulatorBase::timeStep's inner loop
+   (SimulatorBase.cpp:999-1016): TimeStepDiffDFSPH::step (TimeStepDiffDFSPH.cpp:526-652)
+   followed by RigidBody3dBoundarySimulator::velocityTimeStep and positionTimeStep
+   (RigidBody3dBoundarySimulator.cpp:278-344). stats may be NULL. Returns
+   DFSPH_ERR_NOT_CONVERGED (state valid) if a solve hit its iteration cap. */
+int dfsph_step(dfsph_ctx *ctx, int32_t nsteps, dfsph_step_stats *stats);
+
+/* Replaces TimeStepDiffDFSPH::set_init_v_rb / set_init_omega_rb
+   (pySPlisHSPlasH/DiffDFSPHModule.cpp:63-64). */
+int dfsph_set_rigid_init(dfsph_ctx *ctx, int32_t body, const double v[3], const double omega[3]);
+int dfsph_get_rigid_init(dfsph_ctx *ctx, int32_t body, double v[3], double omega[3]);
+
+/* Replaces BoundaryModel_Akinci2012::get_position_rb / get_quaternion_rb_vec4 /
+   get_velocity_rb / get_angular_velocity_rb (pySPlisHSPlasH/BoundaryModelModule.cpp:68-71).
+   Any output pointer may be NULL. */
+int dfsph_get_rigid_state(dfsph_ctx *ctx, int32_t body, double x[3], double q[4],
+                          double v[3], double omega[3]);
+/* Overwrites a body's current velocity and angular velocity and refreshes its boundary
+   particle velocities, as Dynamic3dRigidBody::setVelocity / setAngularVelocity followed by
+   SimulatorBase::updateBoundaryParticles (SimulatorBase.cpp:1827-1857). */
+int dfsph_set_rigid_velocity(dfsph_ctx *ctx, int32_t body, const double v[3], const double omega[3]);
+
+/* Replaces BoundaryModel::getForce / getTorque (SPlisHSPlasH/BoundaryModel.cpp:56-75):
+   net fluid force and torque on the body from the last step. */
+int dfsph_get_rigid_force(dfsph_ctx *ctx, int32_t body, double force[3], double torque[3]);
+
+/* Body mass and world inertia (Dynamic3dRigidBody::getMass / getInertiaTensorWorld). */
+int dfsph_get_rigid_mass(dfsph_ctx *ctx, int32_t body, double *mass, double inertia[9]);
+
+/* Forward-mode chain state of one body (BoundaryModel_Akinci2012 get_grad_x_to_v0,
+   get_grad_x_to_omega0, get_grad_quaternion_to_v0, get_grad_quaternion_to_omega0,
+   get_grad_v_to_v0, get_grad_v_to_omega0, get_grad_omega_to_v0, get_grad_omega_to_omega0,
+   BoundaryModelModule.cpp:73-80). out[78] = x_v0(3x3) x_w0(3x3) q_v0(4x3) q_w0(4x3)
+   v_v0(3x3) v_w0(3x3) w_v0(3x3) w_w0(3x3), all row-major. */
+int dfsph_get_rigid_grad(dfsph_ctx *ctx, int32_t body, double out[78]);
+
+/* Per-step net Jacobians of the last step (BoundaryModel_Akinci2012 grad_net_force_to_* /
+   grad_net_torque_to_*, BoundaryModel_Akinci2012.cpp:453-497; also what
+   RigidBodyGradientManager::get_grad_net_force_to_vn(R,R) returns, SimulationModule.cpp:406-415).
+   out[78] = F_v F_x F_w (3x3 each) F_q (3x4) T_w T_v T_x (3x3 each) T_q (3x4). */
+int dfsph_get_net_jacobians(dfsph_ctx *ctx, int32_t body, double out[78]);
+
+/* Replaces TimeStepDiffDFSPH::reset_gradient (DiffDFSPHModule.cpp:91): chain state to
+   identity/zero and the recorded per-step adjoint tape cleared. */
+int dfsph_reset_gradient(dfsph_ctx *ctx);
+
+/* Reverse-mode adjoint over the per-step chain matrices recorded since the last
+   dfsph_reset / dfsph_reset_gradient. dL_dstate has 13 doubles per body
+   (dL/dx[3], dL/dq[4] (w,x,y,z), dL/dv[3], dL/domega[3]) for the current state;
+   dL_dinit receives 6 doubles per body (dL/dv0[3], dL/domega0[3]). Equal to
+   contracting dL_dstate with the forward-mode chain state. No reference counterpart:
+   the reference only propagates forward-mode tangents. */
+int dfsph_backward(dfsph_ctx *ctx, const double *dL_dstate, double *dL_dinit);
+int dfsph_tape_length(dfsph_ctx *ctx, int64_t *n_steps);
+
+/* Field export/import in the caller's particle order (FluidModel::getPosition etc.).
+   dst/src are host buffers of n*components doubles. */
+int dfsph_copy_field(dfsph_ctx *ctx, int32_t field, double *dst, int64_t n);
+int dfsph_set_field(dfsph_ctx *ctx, int32_t field, const double *src, int64_t n);
+int dfsph_num_particles(dfsph_ctx *ctx, int64_t *n_fluid, int64_t *n_boundary);
+
+/* Neighbour sets of the last neighbour search as CSR in the caller's order, each row
+   sorted ascending. Call once with idx == NULL to get total; then with buffers.
+   start has n_rows+1 entries. */
+int dfsph_get_neighbors(dfsph_ctx *ctx, int32_t which, int64_t *start, int32_t *idx,
+                        int64_t *total);
+
+/* Simulated time (TimeManager::getTime) and steps since reset (get_step_count). */
+int dfsph_get_time(dfsph_ctx *ctx, double *t, int64_t *step_count);
+
+/* Synchronises the context's stream (for timing from the caller). */
+int dfsph_synchronize(dfsph_ctx *ctx);
+
+/* Kernel launches issued by this context since creation (for launch accounting). */
+int dfsph_launch_count(dfsph_ctx *ctx, int64_t *count);
+
+/* Timing on the context's stream (no reference counterpart; the reference times with
+   host clocks, Utilities/Timing.h:22-37). dfsph_record_event records CUDA event `slot`
+   (0..7) on the stream; dfsph_event_elapsed gives milliseconds between two recorded
+   slots (synchronises on the second). */
+int dfsph_record_event(dfsph_ctx *ctx, int32_t slot);
+int dfsph_event_elapsed(dfsph_ctx *ctx, int32_t slot_a, int32_t slot_b, double *ms);
+
+/* Per-kernel-class device timing with CUDA events around each launch (replaces the
+   reference's START_TIMING/STOP_TIMING_AVG phases, TimeStepDiffDFSPH.cpp:528-651).
+   dfsph_profile_read resolves and returns the totals since profiling was enabled:
+   launches, summed device milliseconds and summed work units (particles, or samples
+   for the boundary kernels). Kernel classes are DFSPH_K_*. */
+#define DFSPH_K_SORT           0
+#define DFSPH_K_LISTS_DENSITY  1
+#define DFSPH_K_BF_LISTS       2
+#define DFSPH_K_DENSITY_PASS   3
+#define DFSPH_K_VELOCITY_PASS  4
+#define DFSPH_K_XSPH           5
+#define DFSPH_K_INTEGRATE      6
+#define DFSPH_K_PAIRS          7
+#define DFSPH_K_RIGID          8
+#define DFSPH_K_COUNT          9
+int dfsph_profile_enable(dfsph_ctx *ctx, int32_t on);
+int dfsph_profile_read(dfsph_ctx *ctx, int32_t kernel_class, int64_t *launches, double *total_ms,
+                       int64_t *units);
+const char *dfsph_kernel_class_name(int32_t kernel_class);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DFSPH_H */

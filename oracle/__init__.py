@@ -1,0 +1,201 @@
+"""CPU oracle of the DiffDFSPH step — test infrastructure only.
+
+Only the tests, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg use this
+package, as the checker. The product (``difffr_gb300``) never imports it.
+"""
+import ctypes
+import os
+import subprocess
+from ctypes import POINTER, c_double, c_float, c_int, c_int32, c_int64, c_void_p
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(_HERE, "dfsph_oracle.cpp")
+LIB = os.path.join(_HERE, "_build", "liboracle_dfsph.so")
+
+MODE_F32 = 0       # <float, float>   the reference's default float build
+MODE_MIXED = 1     # <float, double>  FP32 fluid, FP64 rigid (the GPU split)
+MODE_F64 = 2       # <double, double> the reference's USE_DOUBLE build
+
+
+def build(force=False):
+    """Compiles the oracle with g++ (OpenMP, no FMA contraction so x86 and Arm agree)."""
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+        return LIB
+    cmd = ["g++", "-O3", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+           "-o", LIB, SRC]
+    subprocess.check_call(cmd)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = ctypes.CDLL(LIB)
+        from difffr_gb300 import _abi
+        dp = POINTER(c_double)
+        L.orc_create.argtypes = [POINTER(_abi.DfsphScene), c_int]
+        L.orc_create.restype = c_void_p
+        L.orc_destroy.argtypes = [c_void_p]
+        L.orc_set_threads.argtypes = [c_int]
+        L.orc_set_threads.restype = c_int
+        L.orc_step.argtypes = [c_void_p, c_int, POINTER(_abi.DfsphStepStats)]
+        L.orc_copy_field.argtypes = [c_void_p, c_int, dp]
+        L.orc_set_field.argtypes = [c_void_p, c_int, dp]
+        for n in ("orc_get_rigid_state",):
+            getattr(L, n).argtypes = [c_void_p, c_int, dp, dp, dp, dp]
+        for n in ("orc_get_rigid_force", "orc_get_rigid_mass", "orc_set_rigid_init", "orc_set_rigid_velocity"):
+            getattr(L, n).argtypes = [c_void_p, c_int, dp, dp]
+        for n in ("orc_get_rigid_grad", "orc_get_net_jacobians"):
+            getattr(L, n).argtypes = [c_void_p, c_int, dp]
+        L.orc_get_neighbors.argtypes = [c_void_p, c_int, POINTER(c_int64), POINTER(c_int32), POINTER(c_int64)]
+        L.orc_reset.argtypes = [c_void_p]
+        L.orc_reset_gradient.argtypes = [c_void_p]
+        L.orc_num_particles.argtypes = [c_void_p, POINTER(c_int64), POINTER(c_int64)]
+        L.orc_get_time.argtypes = [c_void_p]
+        L.orc_get_time.restype = c_double
+        L.orc_kernel_eval.argtypes = [c_double, c_int, dp, dp, dp, dp]
+        fp = POINTER(c_float)
+        L.orc_kernel_eval_f.argtypes = [c_float, c_int, fp, fp, fp, fp]
+        L.orc_quat_eval.argtypes = [c_int, dp, dp, dp, dp, dp, dp]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(POINTER(c_double))
+
+
+class Oracle:
+    """The oracle simulation behind the same scene description as the GPU library."""
+
+    def __init__(self, scene, mode=None, threads=None):
+        from difffr_gb300 import _abi
+        L = lib()
+        if threads:
+            L.orc_set_threads(int(threads))
+        if mode is None:
+            mode = MODE_F64 if scene.params.fluid_precision == _abi.DFSPH_FP64 else MODE_MIXED
+        self._cs = _abi.CScene(scene)
+        self.h = L.orc_create(self._cs.ref(), int(mode))
+        if not self.h:
+            raise RuntimeError("oracle creation failed")
+        self.L = L
+        self.scene = scene
+        nf, nb = c_int64(), c_int64()
+        L.orc_num_particles(self.h, ctypes.byref(nf), ctypes.byref(nb))
+        self.n_fluid, self.n_boundary = nf.value, nb.value
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.orc_destroy(self.h)
+            self.h = None
+
+    def step(self, n=1):
+        from difffr_gb300 import _abi
+        st = _abi.DfsphStepStats()
+        rc = self.L.orc_step(self.h, int(n), ctypes.byref(st))
+        d = st.as_dict()
+        d["rc"] = rc
+        return d
+
+    def field(self, f):
+        from difffr_gb300 import _abi
+        n = self.n_boundary if f in _abi.BOUNDARY_FIELDS else self.n_fluid
+        c = _abi.FIELD_COMPONENTS.get(f, 1)
+        out = np.zeros(n * c, dtype=np.float64)
+        rc = self.L.orc_copy_field(self.h, int(f), _p(out))
+        assert rc == 0
+        return out.reshape(n, c) if c > 1 else out
+
+    def set_field(self, f, data):
+        d = np.ascontiguousarray(data, dtype=np.float64).ravel()
+        assert self.L.orc_set_field(self.h, int(f), _p(d)) == 0
+
+    def rigid_state(self, b):
+        x, q, v, w = (np.zeros(k) for k in (3, 4, 3, 3))
+        assert self.L.orc_get_rigid_state(self.h, b, _p(x), _p(q), _p(v), _p(w)) == 0
+        return x, q, v, w
+
+    def rigid_force(self, b):
+        F, T = np.zeros(3), np.zeros(3)
+        assert self.L.orc_get_rigid_force(self.h, b, _p(F), _p(T)) == 0
+        return F, T
+
+    def rigid_mass(self, b):
+        m, I = np.zeros(1), np.zeros(9)
+        assert self.L.orc_get_rigid_mass(self.h, b, _p(m), _p(I)) == 0
+        return m[0], I.reshape(3, 3)
+
+    def rigid_grad(self, b):
+        o = np.zeros(78)
+        assert self.L.orc_get_rigid_grad(self.h, b, _p(o)) == 0
+        return o
+
+    def net_jacobians(self, b):
+        o = np.zeros(78)
+        assert self.L.orc_get_net_jacobians(self.h, b, _p(o)) == 0
+        return o
+
+    def set_rigid_init(self, b, v, w):
+        v = np.asarray(v, dtype=np.float64); w = np.asarray(w, dtype=np.float64)
+        assert self.L.orc_set_rigid_init(self.h, b, _p(v), _p(w)) == 0
+
+    def set_rigid_velocity(self, b, v, w):
+        v = np.asarray(v, dtype=np.float64); w = np.asarray(w, dtype=np.float64)
+        assert self.L.orc_set_rigid_velocity(self.h, b, _p(v), _p(w)) == 0
+
+    def neighbors(self, which):
+        tot = c_int64()
+        rc = self.L.orc_get_neighbors(self.h, int(which), None, None, ctypes.byref(tot))
+        assert rc == 0, rc
+        rows = self.n_fluid if which in (0, 1) else self.n_boundary
+        start = np.zeros(rows + 1, dtype=np.int64)
+        idx = np.zeros(tot.value, dtype=np.int32)
+        self.L.orc_get_neighbors(self.h, int(which), start.ctypes.data_as(POINTER(c_int64)),
+                                 idx.ctypes.data_as(POINTER(c_int32)), ctypes.byref(tot))
+        return start, idx
+
+    def reset(self):
+        self.L.orc_reset(self.h)
+
+    def reset_gradient(self):
+        self.L.orc_reset_gradient(self.h)
+
+    def time(self):
+        return self.L.orc_get_time(self.h)
+
+
+def kernel_eval(h, r):
+    """Oracle cubic kernel (double): W, gradW, gradGradW at offsets r[n,3]."""
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    n = r.shape[0]
+    W, G, H = np.zeros(n), np.zeros((n, 3)), np.zeros((n, 3, 3))
+    lib().orc_kernel_eval(float(h), n, _p(r), _p(W), _p(G), _p(H))
+    return W, G, H
+
+
+def kernel_eval_f(h, r):
+    """Oracle cubic kernel (float)."""
+    r = np.ascontiguousarray(r, dtype=np.float32)
+    n = r.shape[0]
+    W, G, H = np.zeros(n, np.float32), np.zeros((n, 3), np.float32), np.zeros((n, 3, 3), np.float32)
+    fp = lambda a: a.ctypes.data_as(POINTER(c_float))
+    lib().orc_kernel_eval_f(float(h), n, fp(r), fp(W), fp(G), fp(H))
+    return W, G, H
+
+
+def quat_eval(q, p):
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    p = np.ascontiguousarray(p, dtype=np.float64)
+    n = q.shape[0]
+    a, b, c, d = np.zeros((n, 3, 4)), np.zeros((n, 3, 4)), np.zeros((n, 4, 4)), np.zeros((n, 4, 3))
+    lib().orc_quat_eval(n, _p(q), _p(p), _p(a), _p(b), _p(c), _p(d))
+    return a, b, c, d
