@@ -102,6 +102,8 @@ def make_scene(args, enable_gradient=1, seed=0):
     from difffr_gb300 import scene as scn
     if args.config == 1:
         sc = scn.dam_break_sphere(seed=seed, enable_gradient=enable_gradient)
+    elif args.config == 5:
+        sc = scn.dam_break_sphere(n=(64, 64, 64), seed=seed, enable_gradient=enable_gradient)
     elif args.config == 0:
         sc = scn.config0(precision=0, seed=seed, enable_gradient=enable_gradient)
     elif args.config == 2:
@@ -311,7 +313,8 @@ def main():
     args.config_name = {0: "tank_sphere_8k (20^3 lattice, r 0.025)",
                         1: "dam_break_sphere_1M (100^3 lattice, r 0.005, 2.4x1.2x1.2 box, R 0.05 sphere)",
                         2: "pool_ellipsoid_250k (125x16x125, r 0.004)",
-                        4: "billiards_on_water_4M (200x100x200, r 0.0025, 2 spheres)"}[args.config]
+                        4: "billiards_on_water_4M (200x100x200, r 0.0025, 2 spheres)",
+                        5: "dam_break_sphere_262k (64^3 lattice, r 0.005; reduced copy for profiling)"}[args.config]
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

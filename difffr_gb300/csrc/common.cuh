@@ -52,7 +52,7 @@ template <class T> __device__ __forceinline__ T dist2_rn(T dx, T dy, T dz) {
 // CubicKernel (SPlisHSPlasH/SPHKernels.h:16-176). k = 8/(pi h^3), l = 48/(pi h^3).
 template <class T>
 struct Cubic {
-  T h, k, l, w0;
+  T h, k, l, w0, invh;
 };
 
 template <class T> __device__ __forceinline__ T cubic_W(T rl, const Cubic<T> &c) {
@@ -82,6 +82,51 @@ template <class T> __device__ __forceinline__ V3<T> cubic_gradW(V3<T> r, T rl, c
   }
   return {T(0), T(0), T(0)};
 }
+
+// Kernel terms from the squared distance d2 of a neighbour pair (d2 < h^2):
+//   KEval<T>::W(d2) = W(|r|),  KEval<T>::G(d2) = g with gradW(r) = g r.
+// double: IEEE sqrt and divisions in the reference's order (SPHKernels.h:37-102).
+// float:  one rsqrt and multiplications by 1/h; differs from the IEEE form by a few ulp.
+template <class T> struct KEval;
+template <> struct KEval<double> {
+  static __device__ __forceinline__ double W(double d2, const Cubic<double> &c) { return cubic_W(sqrt(d2), c); }
+  static __device__ __forceinline__ double G(double d2, const Cubic<double> &c) {
+    const double rl = sqrt(d2);
+    const double q = rl / c.h;
+    if ((rl > 1.0e-5) && (q <= 1.0)) {
+      const double inv = 1.0 / (rl * c.h);
+      double s;
+      if (q <= 0.5) s = c.l * q * (3.0 * q - 2.0);
+      else { const double f = 1.0 - q; s = c.l * (-f * f); }
+      return s * inv;
+    }
+    return 0.0;
+  }
+};
+template <> struct KEval<float> {
+  static __device__ __forceinline__ float W(float d2, const Cubic<float> &c) {
+    const float rl = d2 * rsqrtf(d2);  // d2 = 0 gives NaN -> q <= 1 false; handled below
+    const float q = d2 > 0.f ? rl * c.invh : 0.f;
+    float res = 0.f;
+    if (q <= 1.f) {
+      if (q <= 0.5f) { const float q2 = q * q; res = c.k * (6.f * q2 * q - 6.f * q2 + 1.f); }
+      else { const float f = 1.f - q; res = c.k * (2.f * (f * f * f)); }
+    }
+    return res;
+  }
+  static __device__ __forceinline__ float G(float d2, const Cubic<float> &c) {
+    const float rinv = rsqrtf(d2);
+    const float rl = d2 * rinv;
+    const float q = rl * c.invh;
+    if ((rl > 1.0e-5f) && (q <= 1.f)) {
+      float s;
+      if (q <= 0.5f) s = c.l * q * (3.f * q - 2.f);
+      else { const float f = 1.f - q; s = c.l * (-f * f); }
+      return s * rinv * c.invh;
+    }
+    return 0.f;
+  }
+};
 
 // Symmetric 3x3 Hessian stored as xx, xy, xz, yy, yz, zz.
 template <class T> struct Sym3 { T xx, xy, xz, yy, yz, zz; };

@@ -20,10 +20,19 @@
 namespace dfsph {
 
 // ----------------------------------------------------------------- device buffer
+// Owning device allocation; move-only (a copy would free the same pointer twice).
 template <class E>
 struct DBuf {
   E *p = nullptr;
   size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  DBuf(DBuf &&o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DBuf &operator=(DBuf &&o) noexcept {
+    if (this != &o) { free(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+    return *this;
+  }
   void alloc(size_t count) {
     free();
     n = count;
@@ -77,6 +86,7 @@ struct Scanner {
   std::vector<DBuf<int>> levels;
   void prepare(size_t n) {
     levels.clear();
+    levels.reserve(8);
     size_t m = n;
     while (true) {
       size_t blocks = (m + PER_BLOCK - 1) / PER_BLOCK;
@@ -153,16 +163,17 @@ class Engine : public EngineBase {
   std::vector<int> boundary_is_dyn_, boundary_slot_;  // boundary index -> (dynamic?, slot)
 
   // fluid (sorted order), double-buffered where the sort gathers
-  DBuf<V4<T>> x_[2], v_[2];
+  DBuf<Rec<T>> R_[2];
+  DBuf<V4<T>> Q_;
   DBuf<T> kappa_[2], kappaV_[2];
   DBuf<int> perm_[2];
   int cur_ = 0;
-  DBuf<T> kk_, rho_, alpha_, rhoAdv_;
+  DBuf<T> rho_, alpha_, rhoAdv_;
   DBuf<V4<T>> sumgrad_;
   DBuf<int> fcount_, flist_, bcount_, blist_;
   DBuf<int> key_, rank_, order_, cstartF_;
   // boundary
-  DBuf<V4<T>> bx_, bv_;       // [ns + nd] static (fixed) then dynamic (cell-sorted copy)
+  DBuf<Rec<T>> BR_;           // [ns + nd] static (fixed) then dynamic (cell-sorted copy)
   DBuf<int> cstartS_, cstartD_;
   DBuf<V4<T>> xd_, vd_, x0d_;  // dynamic, body order
   DBuf<int> bodyd_, keyD_, rankD_, orderD_, dynSortedToBody_, bfcount_, bflist_;
@@ -221,11 +232,13 @@ class Engine : public EngineBase {
 
   void sort_fluid();
   void sort_dynamic();
-  void sort_points(const V4<T> *pts, int count, int *key, int *rank, int *cstart, int *order);
+  void sort_points(const V4<T> *pts, int stride, int count, int *key, int *rank, int *cstart, int *order);
   void compute_psi();
   void begin_step();
-  void divergence_solve();
-  void pressure_solve();
+  void solve(bool pressure);
+  void launch_density(int mode, T *kappa_io, bool partials);
+  void launch_velocity(T *kappa_acc);
+  void launch_pairs(bool pressure, bool warm, bool grad);
   void rigid_end();
   double read_residual();
   void grow_tape();

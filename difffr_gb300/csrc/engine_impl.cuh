@@ -56,7 +56,8 @@ Engine<T>::Engine(const dfsph_scene *sc) {
   if (P_.struct_size != (int)sizeof(dfsph_params)) throw DfsphException(DFSPH_ERR_INVALID_ARG, "dfsph_params.struct_size mismatch");
   if (!(P_.particle_radius > 0) || !(P_.time_step > 0) || !(P_.density0 > 0))
     throw DfsphException(DFSPH_ERR_INVALID_ARG, "particle_radius, time_step and density0 must be positive");
-  if (sc->n_fluid < 0 || sc->n_fluid > (int64_t)INT32_MAX / 2) throw DfsphException(DFSPH_ERR_INVALID_ARG, "n_fluid out of range");
+  // neighbour passes index LPP threads per particle in int: keep n * LPP below 2^31
+  if (sc->n_fluid < 0 || sc->n_fluid > (int64_t)INT32_MAX / 8) throw DfsphException(DFSPH_ERR_INVALID_ARG, "n_fluid out of range");
   if (sc->n_fluid > 0 && !sc->fluid_x) throw DfsphException(DFSPH_ERR_INVALID_ARG, "fluid_x is NULL");
   if (sc->n_bodies < 0 || sc->n_bodies > DFSPH_MAX_BODIES) throw DfsphException(DFSPH_ERR_INVALID_ARG, "n_bodies out of range");
   if (sc->n_bodies > 0 && !sc->bodies) throw DfsphException(DFSPH_ERR_INVALID_ARG, "bodies is NULL");
@@ -76,6 +77,7 @@ Engine<T>::Engine(const dfsph_scene *sc) {
   fc_.kc.k = T(8) / (pi * h3);
   fc_.kc.l = T(48) / (pi * h3);
   fc_.kc.w0 = fc_.kc.k;  // W(0) = k (6*0 - 6*0 + 1)
+  fc_.kc.invh = T(1) / h;
   fc_.h2 = h * h;
   fc_.rho0 = (T)P_.density0;
   const T diam = T(2) * r;
@@ -87,8 +89,9 @@ Engine<T>::Engine(const dfsph_scene *sc) {
   fc_.eps = T(1.0e-5);
   fc_.visc = (T)P_.viscosity;
   fc_.gx = (T)P_.gravity[0]; fc_.gy = (T)P_.gravity[1]; fc_.gz = (T)P_.gravity[2];
-  fc_.kf = P_.max_fluid_neighbors > 0 ? P_.max_fluid_neighbors : 96;
-  fc_.kb = P_.max_boundary_neighbors > 0 ? P_.max_boundary_neighbors : 96;
+  // list capacities, rounded up to whole 16-byte groups for the vector loads
+  fc_.kf = ((P_.max_fluid_neighbors > 0 ? P_.max_fluid_neighbors : 96) + 3) / 4 * 4;
+  fc_.kb = ((P_.max_boundary_neighbors > 0 ? P_.max_boundary_neighbors : 96) + 3) / 4 * 4;
   // gradient coefficients: computeGradient's Real 1/dt/dt, 1/dt and the unsigned copy of :1266
   const T cg2 = T(1) / fc_.dt / fc_.dt, cg1 = T(1) / fc_.dt;
   pcP_.cReal = cg2;
@@ -201,16 +204,18 @@ Engine<T>::Engine(const dfsph_scene *sc) {
   v_init_.assign(3 * (size_t)n_, 0.0);
   if (sc->fluid_v) v_init_.assign(sc->fluid_v, sc->fluid_v + 3 * (size_t)n_);
   const size_t N = std::max(n_, 1);
-  for (int k = 0; k < 2; k++) { x_[k].alloc(N); v_[k].alloc(N); kappa_[k].alloc(N); kappaV_[k].alloc(N); perm_[k].alloc(N); }
-  kk_.alloc(N); rho_.alloc(N); alpha_.alloc(N); rhoAdv_.alloc(N); sumgrad_.alloc(N);
+  for (int k = 0; k < 2; k++) { R_[k].alloc(N); kappa_[k].alloc(N); kappaV_[k].alloc(N); perm_[k].alloc(N); }
+  Q_.alloc(N);
+  rho_.alloc(N); alpha_.alloc(N); rhoAdv_.alloc(N); sumgrad_.alloc(N);
   fcount_.alloc(N); bcount_.alloc(N);
-  flist_.alloc(N * (size_t)fc_.kf);
-  blist_.alloc(N * (size_t)fc_.kb);
+  // +8 entries: a batched 16-byte load may read up to 7 entries past a short last row
+  flist_.alloc(N * (size_t)fc_.kf + 8);
+  blist_.alloc(N * (size_t)fc_.kb + 8);
   key_.alloc(N); rank_.alloc(N); order_.alloc(N);
   cstartF_.alloc((size_t)ncell_ + 1);
   cstartS_.alloc((size_t)ncell_ + 1);
   cstartD_.alloc((size_t)ncell_ + 1);
-  partials_.alloc((size_t)blocks(std::max(n_, 1)));
+  partials_.alloc((size_t)blocks(std::max(n_, 1) * LPP));
   resid_.alloc(4);
   err_.alloc(1);
   DF_CK(cudaHostAlloc((void **)&resid_host_, 4 * sizeof(double), cudaHostAllocMapped));
@@ -219,13 +224,13 @@ Engine<T>::Engine(const dfsph_scene *sc) {
 
   // ---- boundary buffers
   const size_t NB = std::max(ns_ + nd_, 1);
-  bx_.alloc(NB); bv_.alloc(NB); psi_.alloc(NB);
+  BR_.alloc(NB); psi_.alloc(NB);
   const size_t ND = std::max(nd_, 1);
   xd_.alloc(ND); vd_.alloc(ND); x0d_.alloc(ND); bodyd_.alloc(ND); keyD_.alloc(ND); rankD_.alloc(ND);
   orderD_.alloc(ND); dynSortedToBody_.alloc(ND); bfcount_.alloc(ND); bflist_.alloc(ND * (size_t)kbf_);
   acc_.alloc(ND * ACC_STRIDE);
   bs_.alloc(std::max(nb_, 1));
-  DF_CK(cudaMemsetAsync(bv_.p, 0, NB * sizeof(V4<T>), stream_));
+  DF_CK(cudaMemsetAsync(BR_.p, 0, NB * sizeof(Rec<T>), stream_));
   DF_CK(cudaMemsetAsync(acc_.p, 0, ND * ACC_STRIDE * sizeof(double), stream_));
   if (nd_ > 0) {
     std::vector<V4<T>> x0h(nd_);
@@ -244,7 +249,7 @@ Engine<T>::Engine(const dfsph_scene *sc) {
     DBuf<int> k1, k2, k3;
     k1.alloc(ns_); k2.alloc(ns_); k3.alloc(ns_);
     DF_CK(cudaMemcpyAsync(tmp.p, sh.data(), ns_ * sizeof(V4<T>), cudaMemcpyHostToDevice, stream_));
-    sort_points(tmp.p, ns_, k1.p, k2.p, cstartS_.p, k3.p);
+    sort_points(tmp.p, 1, ns_, k1.p, k2.p, cstartS_.p, k3.p);
     std::vector<int> order(ns_);
     DF_CK(cudaMemcpyAsync(order.data(), k3.p, ns_ * sizeof(int), cudaMemcpyDeviceToHost, stream_));
     DF_CK(cudaStreamSynchronize(stream_));
@@ -256,7 +261,9 @@ Engine<T>::Engine(const dfsph_scene *sc) {
       boundary_is_dyn_[static_orig_[s]] = 0;
       boundary_slot_[static_orig_[s]] = s;
     }
-    DF_CK(cudaMemcpyAsync(bx_.p, sorted.data(), ns_ * sizeof(V4<T>), cudaMemcpyHostToDevice, stream_));
+    std::vector<Rec<T>> srec(ns_);
+    for (int q = 0; q < ns_; q++) srec[q] = Rec<T>{sorted[q], V4<T>{T(0), T(0), T(0), T(0)}};
+    DF_CK(cudaMemcpyAsync(BR_.p, srec.data(), ns_ * sizeof(Rec<T>), cudaMemcpyHostToDevice, stream_));
     DF_CK(cudaStreamSynchronize(stream_));
   } else {
     // keep the empty table's scan consistent (all zero)
@@ -279,10 +286,10 @@ Engine<T>::~Engine() {
 }
 
 template <class T>
-void Engine<T>::sort_points(const V4<T> *pts, int count, int *key, int *rank, int *cstart, int *order) {
+void Engine<T>::sort_points(const V4<T> *pts, int stride, int count, int *key, int *rank, int *cstart, int *order) {
   DF_CK(cudaMemsetAsync(cstart, 0, ((size_t)ncell_ + 1) * sizeof(int), stream_));
   if (count == 0) return;
-  k_cell_keys<T><<<blocks(count), 256, 0, stream_>>>(count, pts, fc_.grid, key, rank, cstart, err_.p);
+  k_cell_keys<T><<<blocks(count), 256, 0, stream_>>>(count, pts, stride, fc_.grid, key, rank, cstart, err_.p);
   launched();
   scan_.run(cstart, ncell_ + 1, stream_, launches_);
   k_scatter_order<<<blocks(count), 256, 0, stream_>>>(count, key, rank, cstart, order);
@@ -298,11 +305,11 @@ void Engine<T>::sort_fluid() {
     return;
   }
   pbegin();
-  sort_points(x_[cur_].p, n_, key_.p, rank_.p, cstartF_.p, order_.p);
+  sort_points(reinterpret_cast<const V4<T> *>(R_[cur_].p), 2, n_, key_.p, rank_.p, cstartF_.p, order_.p);
   const int nx = 1 - cur_;
-  k_gather_fluid<T><<<blocks(n_), 256, 0, stream_>>>(n_, order_.p, x_[cur_].p, v_[cur_].p, kappa_[cur_].p,
-                                                     kappaV_[cur_].p, perm_[cur_].p, x_[nx].p, v_[nx].p,
-                                                     kappa_[nx].p, kappaV_[nx].p, perm_[nx].p);
+  k_gather_fluid<T><<<blocks(n_), 256, 0, stream_>>>(n_, order_.p, R_[cur_].p, kappa_[cur_].p, kappaV_[cur_].p,
+                                                     perm_[cur_].p, R_[nx].p, kappa_[nx].p, kappaV_[nx].p,
+                                                     perm_[nx].p);
   launched();
   pend(DFSPH_K_SORT, n_);
   cur_ = nx;
@@ -312,8 +319,8 @@ template <class T>
 void Engine<T>::sort_dynamic() {
   if (nd_ == 0) return;
   pbegin();
-  sort_points(xd_.p, nd_, keyD_.p, rankD_.p, cstartD_.p, orderD_.p);
-  k_gather_dynamic<T><<<blocks(nd_), 256, 0, stream_>>>(nd_, ns_, orderD_.p, xd_.p, vd_.p, bx_.p, bv_.p,
+  sort_points(xd_.p, 1, nd_, keyD_.p, rankD_.p, cstartD_.p, orderD_.p);
+  k_gather_dynamic<T><<<blocks(nd_), 256, 0, stream_>>>(nd_, ns_, orderD_.p, xd_.p, vd_.p, BR_.p,
                                                         dynSortedToBody_.p);
   launched();
   pend(DFSPH_K_SORT, nd_);
@@ -322,9 +329,9 @@ void Engine<T>::sort_dynamic() {
 template <class T>
 void Engine<T>::compute_psi() {
   if (ns_ + nd_ == 0) return;
-  k_boundary_psi<T><<<blocks(ns_ + nd_), 256, 0, stream_>>>(fc_, ns_, nd_, bx_.p, cstartS_.p,
+  k_boundary_psi<T><<<blocks(ns_ + nd_), 256, 0, stream_>>>(fc_, ns_, nd_, BR_.p, cstartS_.p,
                                                             nd_ ? cstartD_.p : nullptr, psi_.p);
-  k_set_psi<T><<<blocks(ns_ + nd_), 256, 0, stream_>>>(ns_, nd_, psi_.p, bx_.p, xd_.p, dynSortedToBody_.p);
+  k_set_psi<T><<<blocks(ns_ + nd_), 256, 0, stream_>>>(ns_, nd_, psi_.p, BR_.p, xd_.p, dynSortedToBody_.p);
   launched(2);
   check_launch();
 }
@@ -333,15 +340,14 @@ template <class T>
 void Engine<T>::upload_fluid_initial() {
   cur_ = 0;
   if (n_ == 0) return;
-  std::vector<V4<T>> xh(n_), vh(n_);
+  std::vector<Rec<T>> rh(n_);
   std::vector<int> ph(n_);
   for (int i = 0; i < n_; i++) {
-    xh[i] = V4<T>{(T)x_init_[3 * i], (T)x_init_[3 * i + 1], (T)x_init_[3 * i + 2], T(0)};
-    vh[i] = V4<T>{(T)v_init_[3 * i], (T)v_init_[3 * i + 1], (T)v_init_[3 * i + 2], T(0)};
+    rh[i].x = V4<T>{(T)x_init_[3 * i], (T)x_init_[3 * i + 1], (T)x_init_[3 * i + 2], T(0)};
+    rh[i].v = V4<T>{(T)v_init_[3 * i], (T)v_init_[3 * i + 1], (T)v_init_[3 * i + 2], T(0)};
     ph[i] = i;
   }
-  DF_CK(cudaMemcpyAsync(x_[0].p, xh.data(), n_ * sizeof(V4<T>), cudaMemcpyHostToDevice, stream_));
-  DF_CK(cudaMemcpyAsync(v_[0].p, vh.data(), n_ * sizeof(V4<T>), cudaMemcpyHostToDevice, stream_));
+  DF_CK(cudaMemcpyAsync(R_[0].p, rh.data(), n_ * sizeof(Rec<T>), cudaMemcpyHostToDevice, stream_));
   DF_CK(cudaMemcpyAsync(perm_[0].p, ph.data(), n_ * sizeof(int), cudaMemcpyHostToDevice, stream_));
   DF_CK(cudaMemsetAsync(kappa_[0].p, 0, n_ * sizeof(T), stream_));
   DF_CK(cudaMemsetAsync(kappaV_[0].p, 0, n_ * sizeof(T), stream_));
@@ -463,123 +469,94 @@ void Engine<T>::check_error_word() {
   }
 }
 
-// divergenceSolve (TimeStepDiffDFSPH.cpp:770-881)
 template <class T>
-void Engine<T>::divergence_solve() {
-  const int nbk = blocks(n_);
-  V4<T> *X = x_[cur_].p, *V = v_[cur_].p;
-  T *kV = kappaV_[cur_].p;
-  const int ndw = blocks(nd_ * 32, 128);
-  if (P_.use_divergence_warmstart) {
-    { pbegin(); k_density_pass<T, PASS_DIVERGENCE_WARM><<<nbk, 256, 0, stream_>>>(fc_, X, V, bx_.p, bv_.p, flist_.p, fcount_.p,
-                                                                     blist_.p, bcount_.p, rho_.p, alpha_.p,
-                                                                     rhoAdv_.p, kk_.p, kV, nullptr); pend(DFSPH_K_DENSITY_PASS, n_); }
-    if (nd_) { pbegin(); k_pairs<T, 1, true, false><<<ndw, 128, 0, stream_>>>(fc_, pcD_, nd_, xd_.p, vd_.p, x0d_.p, bodyd_.p, bs_.p,
-                                                                   bflist_.p, bfcount_.p, X, V, alpha_.p, rhoAdv_.p,
-                                                                   sumgrad_.p, kV, acc_.p); pend(DFSPH_K_PAIRS, nd_); }
-    { pbegin(); k_velocity_pass<T, 0><<<nbk, 256, 0, stream_>>>(fc_, X, V, bx_.p, flist_.p, fcount_.p, blist_.p, bcount_.p, kk_.p,
-                                                    nullptr); pend(DFSPH_K_VELOCITY_PASS, n_); }
-    launched(nd_ ? 3 : 2);
+void Engine<T>::launch_density(int mode, T *kappa_io, bool partials) {
+  const int nbk = blocks(n_ * LPP);
+  double *pp = partials ? partials_.p : nullptr;
+  pbegin();
+#define DF_DENS(M)                                                                                                \
+  k_density_pass<T, M><<<nbk, 256, 0, stream_>>>(fc_, R_[cur_].p, Q_.p, BR_.p, flist_.p, fcount_.p, blist_.p,           \
+                                                 bcount_.p, rho_.p, alpha_.p, rhoAdv_.p, kappa_io, pp)
+  switch (mode) {
+    case PASS_PRESSURE: DF_DENS(PASS_PRESSURE); break;
+    case PASS_DIVERGENCE: DF_DENS(PASS_DIVERGENCE); break;
+    case PASS_PRESSURE_WARM: DF_DENS(PASS_PRESSURE_WARM); break;
+    default: DF_DENS(PASS_DIVERGENCE_WARM); break;
   }
-  { pbegin(); k_density_pass<T, PASS_DIVERGENCE><<<nbk, 256, 0, stream_>>>(fc_, X, V, bx_.p, bv_.p, flist_.p, fcount_.p, blist_.p,
-                                                               bcount_.p, rho_.p, alpha_.p, rhoAdv_.p, kk_.p, nullptr,
-                                                               nullptr); pend(DFSPH_K_DENSITY_PASS, n_); }
+#undef DF_DENS
   launched();
-  int it = 0;
-  bool chk = false;
-  double avg = 0.0;
-  const T eta = (T(1) / fc_.dt) * (T)P_.max_error_v * T(0.01) * fc_.rho0;
-  const int maxIt = P_.max_iterations_v;
-  while ((!chk || it < 1) && it < maxIt) {
-    if (nd_) {
-      if (P_.enable_gradient)
-        { pbegin(); k_pairs<T, 1, false, true><<<ndw, 128, 0, stream_>>>(fc_, pcD_, nd_, xd_.p, vd_.p, x0d_.p, bodyd_.p, bs_.p,
-                                                             bflist_.p, bfcount_.p, X, V, alpha_.p, rhoAdv_.p,
-                                                             sumgrad_.p, kk_.p, acc_.p); pend(DFSPH_K_PAIRS, nd_); }
-      else
-        { pbegin(); k_pairs<T, 1, false, false><<<ndw, 128, 0, stream_>>>(fc_, pcD_, nd_, xd_.p, vd_.p, x0d_.p, bodyd_.p, bs_.p,
-                                                              bflist_.p, bfcount_.p, X, V, alpha_.p, rhoAdv_.p,
-                                                              sumgrad_.p, kk_.p, acc_.p); pend(DFSPH_K_PAIRS, nd_); }
-      launched();
-    }
-    if (P_.use_divergence_warmstart)
-      { pbegin(); k_velocity_pass<T, 1><<<nbk, 256, 0, stream_>>>(fc_, X, V, bx_.p, flist_.p, fcount_.p, blist_.p, bcount_.p,
-                                                      kk_.p, kV); pend(DFSPH_K_VELOCITY_PASS, n_); }
-    else
-      { pbegin(); k_velocity_pass<T, 0><<<nbk, 256, 0, stream_>>>(fc_, X, V, bx_.p, flist_.p, fcount_.p, blist_.p, bcount_.p,
-                                                      kk_.p, nullptr); pend(DFSPH_K_VELOCITY_PASS, n_); }
-    const bool need = (it + 1 >= 1) || (it + 1 >= maxIt);
-    { pbegin(); k_density_pass<T, PASS_DIVERGENCE><<<nbk, 256, 0, stream_>>>(fc_, X, V, bx_.p, bv_.p, flist_.p, fcount_.p,
-                                                                 blist_.p, bcount_.p, rho_.p, alpha_.p, rhoAdv_.p,
-                                                                 kk_.p, nullptr, need ? partials_.p : nullptr); pend(DFSPH_K_DENSITY_PASS, n_); }
-    launched(2);
-    if (need) {
-      k_final_sum<<<1, 32, 0, stream_>>>(nbk, partials_.p, 1.0 / (double)std::max(n_, 1), resid_.p, resid_host_dev_,
-                                         err_.p);
-      launched();
-      check_launch();
-      avg = read_residual();
-      chk = (T)avg <= eta;
-    }
-    it++;
-  }
-  last_iters_v_ = it;
-  last_err_v_ = avg;
+  pend(DFSPH_K_DENSITY_PASS, n_);
 }
 
-// pressureSolve (TimeStepDiffDFSPH.cpp:654-768)
 template <class T>
-void Engine<T>::pressure_solve() {
-  const int nbk = blocks(n_);
-  V4<T> *X = x_[cur_].p, *V = v_[cur_].p;
-  T *kP = kappa_[cur_].p;
-  const int ndw = blocks(nd_ * 32, 128);
-  if (P_.use_pressure_warmstart) {
-    { pbegin(); k_density_pass<T, PASS_PRESSURE_WARM><<<nbk, 256, 0, stream_>>>(fc_, X, V, bx_.p, bv_.p, flist_.p, fcount_.p,
-                                                                   blist_.p, bcount_.p, rho_.p, alpha_.p, rhoAdv_.p,
-                                                                   kk_.p, kP, nullptr); pend(DFSPH_K_DENSITY_PASS, n_); }
-    if (nd_) { pbegin(); k_pairs<T, 0, true, false><<<ndw, 128, 0, stream_>>>(fc_, pcP_, nd_, xd_.p, vd_.p, x0d_.p, bodyd_.p, bs_.p,
-                                                                   bflist_.p, bfcount_.p, X, V, alpha_.p, rhoAdv_.p,
-                                                                   sumgrad_.p, kP, acc_.p); pend(DFSPH_K_PAIRS, nd_); }
-    { pbegin(); k_velocity_pass<T, 0><<<nbk, 256, 0, stream_>>>(fc_, X, V, bx_.p, flist_.p, fcount_.p, blist_.p, bcount_.p, kk_.p,
-                                                    nullptr); pend(DFSPH_K_VELOCITY_PASS, n_); }
-    launched(nd_ ? 3 : 2);
-  }
-  { pbegin(); k_density_pass<T, PASS_PRESSURE><<<nbk, 256, 0, stream_>>>(fc_, X, V, bx_.p, bv_.p, flist_.p, fcount_.p, blist_.p,
-                                                             bcount_.p, rho_.p, alpha_.p, rhoAdv_.p, kk_.p, nullptr,
-                                                             nullptr); pend(DFSPH_K_DENSITY_PASS, n_); }
+void Engine<T>::launch_velocity(T *kappa_acc) {
+  const int nbk = blocks(n_ * LPP);
+  pbegin();
+  if (kappa_acc)
+    k_velocity_pass<T, 1><<<nbk, 256, 0, stream_>>>(fc_, Q_.p, R_[cur_].p, BR_.p, flist_.p, fcount_.p, blist_.p,
+                                                    bcount_.p, kappa_acc);
+  else
+    k_velocity_pass<T, 0><<<nbk, 256, 0, stream_>>>(fc_, Q_.p, R_[cur_].p, BR_.p, flist_.p, fcount_.p, blist_.p,
+                                                    bcount_.p, nullptr);
   launched();
+  pend(DFSPH_K_VELOCITY_PASS, n_);
+}
+
+template <class T>
+void Engine<T>::launch_pairs(bool pressure, bool warm, bool grad) {
+  if (nd_ == 0) return;
+  const int ndw = blocks(nd_ * 32, 128);
+  const PairConsts<T> &pc = pressure ? pcP_ : pcD_;
+  pbegin();
+#define DF_PAIRS(M, W, G)                                                                                          \
+  k_pairs<T, M, W, G><<<ndw, 128, 0, stream_>>>(fc_, pc, nd_, xd_.p, vd_.p, x0d_.p, bodyd_.p, bs_.p, bflist_.p,    \
+                                               bfcount_.p, Q_.p, R_[cur_].p, alpha_.p, rhoAdv_.p, sumgrad_.p, acc_.p)
+  if (pressure) {
+    if (warm) DF_PAIRS(0, true, false);
+    else if (grad) DF_PAIRS(0, false, true);
+    else DF_PAIRS(0, false, false);
+  } else {
+    if (warm) DF_PAIRS(1, true, false);
+    else if (grad) DF_PAIRS(1, false, true);
+    else DF_PAIRS(1, false, false);
+  }
+#undef DF_PAIRS
+  launched();
+  pend(DFSPH_K_PAIRS, nd_);
+}
+
+// pressureSolve (TimeStepDiffDFSPH.cpp:654-768) and divergenceSolve (:770-881):
+// warm start, then Jacobi sweeps of [pair Jacobians + boundary reaction forces,
+// velocity correction, density advection / change + residual] until the average
+// error is below eta (after at least min iterations) or max iterations are reached.
+template <class T>
+void Engine<T>::solve(bool pressure) {
+  const bool warm = pressure ? P_.use_pressure_warmstart : P_.use_divergence_warmstart;
+  T *kap = pressure ? kappa_[cur_].p : kappaV_[cur_].p;
+  const int wm = pressure ? PASS_PRESSURE_WARM : PASS_DIVERGENCE_WARM;
+  const int im = pressure ? PASS_PRESSURE : PASS_DIVERGENCE;
+  if (warm) {
+    launch_density(wm, kap, false);
+    launch_pairs(pressure, true, false);
+    launch_velocity(nullptr);
+  }
+  launch_density(im, nullptr, false);
   int it = 0;
   bool chk = false;
   double avg = 0.0;
-  const T eta = (T)P_.max_error * T(0.01) * fc_.rho0;
-  const int minIt = P_.min_iterations, maxIt = P_.max_iterations;
+  const T eta = pressure ? (T)P_.max_error * T(0.01) * fc_.rho0
+                         : (T(1) / fc_.dt) * (T)P_.max_error_v * T(0.01) * fc_.rho0;
+  const int minIt = pressure ? P_.min_iterations : 1;
+  const int maxIt = pressure ? P_.max_iterations : P_.max_iterations_v;
+  const int nbk = blocks(n_ * LPP);
   while ((!chk || it < minIt) && it < maxIt) {
-    if (nd_) {
-      if (P_.enable_gradient)
-        { pbegin(); k_pairs<T, 0, false, true><<<ndw, 128, 0, stream_>>>(fc_, pcP_, nd_, xd_.p, vd_.p, x0d_.p, bodyd_.p, bs_.p,
-                                                             bflist_.p, bfcount_.p, X, V, alpha_.p, rhoAdv_.p,
-                                                             sumgrad_.p, kk_.p, acc_.p); pend(DFSPH_K_PAIRS, nd_); }
-      else
-        { pbegin(); k_pairs<T, 0, false, false><<<ndw, 128, 0, stream_>>>(fc_, pcP_, nd_, xd_.p, vd_.p, x0d_.p, bodyd_.p, bs_.p,
-                                                              bflist_.p, bfcount_.p, X, V, alpha_.p, rhoAdv_.p,
-                                                              sumgrad_.p, kk_.p, acc_.p); pend(DFSPH_K_PAIRS, nd_); }
-      launched();
-    }
-    if (P_.use_pressure_warmstart)
-      { pbegin(); k_velocity_pass<T, 1><<<nbk, 256, 0, stream_>>>(fc_, X, V, bx_.p, flist_.p, fcount_.p, blist_.p, bcount_.p,
-                                                      kk_.p, kP); pend(DFSPH_K_VELOCITY_PASS, n_); }
-    else
-      { pbegin(); k_velocity_pass<T, 0><<<nbk, 256, 0, stream_>>>(fc_, X, V, bx_.p, flist_.p, fcount_.p, blist_.p, bcount_.p,
-                                                      kk_.p, nullptr); pend(DFSPH_K_VELOCITY_PASS, n_); }
+    launch_pairs(pressure, false, P_.enable_gradient != 0);
+    launch_velocity(warm ? kap : nullptr);
     const bool need = (it + 1 >= minIt) || (it + 1 >= maxIt);
-    { pbegin(); k_density_pass<T, PASS_PRESSURE><<<nbk, 256, 0, stream_>>>(fc_, X, V, bx_.p, bv_.p, flist_.p, fcount_.p, blist_.p,
-                                                               bcount_.p, rho_.p, alpha_.p, rhoAdv_.p, kk_.p, nullptr,
-                                                               need ? partials_.p : nullptr); pend(DFSPH_K_DENSITY_PASS, n_); }
-    launched(2);
+    launch_density(im, nullptr, need);
     if (need) {
-      k_final_sum<<<1, 32, 0, stream_>>>(nbk, partials_.p, 1.0 / (double)std::max(n_, 1), resid_.p, resid_host_dev_,
-                                         err_.p);
+      k_final_sum<<<1, 256, 0, stream_>>>(nbk, partials_.p, 1.0 / (double)std::max(n_, 1), resid_.p,
+                                          resid_host_dev_, err_.p);
       launched();
       check_launch();
       avg = read_residual();
@@ -587,8 +564,8 @@ void Engine<T>::pressure_solve() {
     }
     it++;
   }
-  last_iters_ = it;
-  last_err_ = avg;
+  if (pressure) { last_iters_ = it; last_err_ = avg; }
+  else { last_iters_v_ = it; last_err_v_ = avg; }
 }
 
 template <class T>
@@ -635,30 +612,36 @@ int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
     sort_fluid();
     sort_dynamic();
     if (n_ > 0) {
-      { pbegin(); k_lists_density_factor<T><<<blocks(n_), 256, 0, stream_>>>(fc_, x_[cur_].p, cstartF_.p, bx_.p, cstartS_.p,
-                                                                 nd_ ? cstartD_.p : nullptr, ns_, flist_.p, fcount_.p,
-                                                                 blist_.p, bcount_.p, rho_.p, alpha_.p, sumgrad_.p,
-                                                                 err_.p); pend(DFSPH_K_LISTS_DENSITY, n_); }
-      launched();
+      { pbegin(); k_lists_density_factor<T><<<blocks(n_), 256, 0, stream_>>>(fc_, R_[cur_].p, cstartF_.p,
+                                                                 BR_.p, cstartS_.p, nd_ ? cstartD_.p : nullptr, ns_,
+                                                                 flist_.p, fcount_.p, blist_.p, bcount_.p, rho_.p,
+                                                                 alpha_.p, sumgrad_.p, err_.p);
+        launched(); pend(DFSPH_K_LISTS_DENSITY, n_); }
       if (nd_) {
-        { pbegin(); k_bf_lists<T><<<blocks(nd_), 256, 0, stream_>>>(fc_, nd_, xd_.p, x_[cur_].p, cstartF_.p, kbf_, bflist_.p,
-                                                        bfcount_.p, err_.p); pend(DFSPH_K_BF_LISTS, nd_); }
+        pbegin();
+        k_bf_lists<T><<<blocks(nd_), 256, 0, stream_>>>(fc_, nd_, xd_.p, R_[cur_].p, cstartF_.p, kbf_, bflist_.p,
+                                                        bfcount_.p, err_.p);
         launched();
+        pend(DFSPH_K_BF_LISTS, nd_);
       }
       check_launch();
-      if (P_.enable_divergence_solver) divergence_solve();
+      if (P_.enable_divergence_solver) solve(false);
       else { last_iters_v_ = 0; last_err_v_ = 0.0; }
       const int nv = 1 - cur_;
-      { pbegin(); k_xsph_advect<T><<<blocks(n_), 256, 0, stream_>>>(fc_, x_[cur_].p, v_[cur_].p, v_[nv].p, flist_.p, fcount_.p,
-                                                        rho_.p, kappaV_[cur_].p,
-                                                        (P_.enable_divergence_solver && P_.use_divergence_warmstart) ? 1 : 0); pend(DFSPH_K_XSPH, n_); }
+      pbegin();
+      k_xsph_advect<T><<<blocks(n_ * LPP), 256, 0, stream_>>>(fc_, R_[cur_].p, R_[nv].p, flist_.p, fcount_.p,
+                                                        kappaV_[cur_].p,
+                                                        (P_.enable_divergence_solver && P_.use_divergence_warmstart) ? 1 : 0);
       launched();
-      // the advected velocity lives in the other buffer: swap the velocity pair only
-      std::swap(v_[cur_].p, v_[nv].p);
-      pressure_solve();
-      { pbegin(); k_integrate<T><<<blocks(n_), 256, 0, stream_>>>(fc_, x_[cur_].p, v_[cur_].p, kappa_[cur_].p,
-                                                      P_.use_pressure_warmstart ? 1 : 0); pend(DFSPH_K_INTEGRATE, n_); }
+      pend(DFSPH_K_XSPH, n_);
+      // the advected state lives in the other record buffer: swap the record pair only
+      std::swap(R_[cur_].p, R_[nv].p);
+      solve(true);
+      pbegin();
+      k_integrate<T><<<blocks(n_), 256, 0, stream_>>>(fc_, R_[cur_].p, kappa_[cur_].p,
+                                                      P_.use_pressure_warmstart ? 1 : 0);
       launched();
+      pend(DFSPH_K_INTEGRATE, n_);
     } else {
       last_iters_ = last_iters_v_ = 0;
     }
@@ -791,8 +774,13 @@ void Engine<T>::copy_field(int f, double *dst, int64_t n) {
     DF_CK(cudaMemcpy(perm.data(), perm_[cur_].p, n_ * sizeof(int), cudaMemcpyDeviceToHost));
     if (comps == 3) {
       std::vector<V4<T>> h(n_);
-      const V4<T> *src = f == DFSPH_FIELD_X ? x_[cur_].p : (f == DFSPH_FIELD_V ? v_[cur_].p : sumgrad_.p);
-      DF_CK(cudaMemcpy(h.data(), src, n_ * sizeof(V4<T>), cudaMemcpyDeviceToHost));
+      if (f == DFSPH_FIELD_SUM_GRAD_P) {
+        DF_CK(cudaMemcpy(h.data(), sumgrad_.p, n_ * sizeof(V4<T>), cudaMemcpyDeviceToHost));
+      } else {
+        std::vector<Rec<T>> rr(n_);
+        DF_CK(cudaMemcpy(rr.data(), R_[cur_].p, n_ * sizeof(Rec<T>), cudaMemcpyDeviceToHost));
+        for (int i = 0; i < n_; i++) h[i] = f == DFSPH_FIELD_X ? rr[i].x : rr[i].v;
+      }
       for (int i = 0; i < n_; i++) {
         double *o = dst + 3 * (size_t)perm[i];
         o[0] = h[i].x; o[1] = h[i].y; o[2] = h[i].z;
@@ -811,7 +799,11 @@ void Engine<T>::copy_field(int f, double *dst, int64_t n) {
   }
   std::vector<V4<T>> sx(ns_), sd(nd_);
   const bool wantv = f == DFSPH_FIELD_BOUNDARY_V;
-  if (ns_) DF_CK(cudaMemcpy(sx.data(), wantv ? bv_.p : bx_.p, ns_ * sizeof(V4<T>), cudaMemcpyDeviceToHost));
+  if (ns_) {
+    std::vector<Rec<T>> sr(ns_);
+    DF_CK(cudaMemcpy(sr.data(), BR_.p, ns_ * sizeof(Rec<T>), cudaMemcpyDeviceToHost));
+    for (int q = 0; q < ns_; q++) sx[q] = wantv ? sr[q].v : sr[q].x;
+  }
   if (nd_) DF_CK(cudaMemcpy(sd.data(), wantv ? vd_.p : xd_.p, nd_ * sizeof(V4<T>), cudaMemcpyDeviceToHost));
   auto put = [&](int orig, const V4<T> &p) {
     if (f == DFSPH_FIELD_BOUNDARY_PSI) dst[orig] = p.w;
@@ -832,12 +824,14 @@ void Engine<T>::set_field(int f, const double *src, int64_t n) {
   std::vector<int> perm(n_);
   DF_CK(cudaMemcpy(perm.data(), perm_[cur_].p, n_ * sizeof(int), cudaMemcpyDeviceToHost));
   if (comps == 3) {
-    std::vector<V4<T>> h(n_);
+    std::vector<Rec<T>> rr(n_);
+    DF_CK(cudaMemcpy(rr.data(), R_[cur_].p, n_ * sizeof(Rec<T>), cudaMemcpyDeviceToHost));
     for (int i = 0; i < n_; i++) {
       const double *s = src + 3 * (size_t)perm[i];
-      h[i] = V4<T>{(T)s[0], (T)s[1], (T)s[2], T(0)};
+      V4<T> &dst = f == DFSPH_FIELD_X ? rr[i].x : rr[i].v;
+      dst.x = (T)s[0]; dst.y = (T)s[1]; dst.z = (T)s[2];
     }
-    DF_CK(cudaMemcpy(f == DFSPH_FIELD_X ? x_[cur_].p : v_[cur_].p, h.data(), n_ * sizeof(V4<T>), cudaMemcpyHostToDevice));
+    DF_CK(cudaMemcpy(R_[cur_].p, rr.data(), n_ * sizeof(Rec<T>), cudaMemcpyHostToDevice));
   } else {
     std::vector<T> h(n_);
     for (int i = 0; i < n_; i++) h[i] = (T)src[perm[i]];
@@ -857,19 +851,19 @@ void Engine<T>::neighbors(int which, int64_t *start, int32_t *idx, int64_t *tota
   if (nd_) DF_CK(cudaMemcpy(d2b.data(), dynSortedToBody_.p, nd_ * sizeof(int), cudaMemcpyDeviceToHost));
   auto bmap = [&](int k) { return k < ns_ ? static_orig_[k] : dyn_orig_[d2b[k - ns_]]; };
   if (which == DFSPH_NB_FLUID_FLUID || which == DFSPH_NB_FLUID_BOUNDARY) {
-    const int K = which == DFSPH_NB_FLUID_FLUID ? fc_.kf : fc_.kb;
+    const bool ff = which == DFSPH_NB_FLUID_FLUID;
+    const int K = ff ? fc_.kf : fc_.kb;
     std::vector<int> cnt(std::max(n_, 1)), lst((size_t)std::max(n_, 1) * K);
     if (n_) {
-      DF_CK(cudaMemcpy(cnt.data(), which == DFSPH_NB_FLUID_FLUID ? fcount_.p : bcount_.p, n_ * sizeof(int), cudaMemcpyDeviceToHost));
-      DF_CK(cudaMemcpy(lst.data(), which == DFSPH_NB_FLUID_FLUID ? flist_.p : blist_.p, (size_t)n_ * K * sizeof(int),
-                       cudaMemcpyDeviceToHost));
+      DF_CK(cudaMemcpy(cnt.data(), ff ? fcount_.p : bcount_.p, n_ * sizeof(int), cudaMemcpyDeviceToHost));
+      DF_CK(cudaMemcpy(lst.data(), ff ? flist_.p : blist_.p, (size_t)n_ * K * sizeof(int), cudaMemcpyDeviceToHost));
     }
     rows.assign(n_, {});
     for (int i = 0; i < n_; i++) {
       auto &r = rows[perm[i]];
       for (int k = 0; k < cnt[i]; k++) {
         const int j = lst[(size_t)k * n_ + i];
-        r.push_back(which == DFSPH_NB_FLUID_FLUID ? perm[j] : bmap(j));
+        r.push_back(ff ? perm[j] : bmap(j));
       }
     }
   } else if (which == DFSPH_NB_BOUNDARY_FLUID) {

@@ -1,16 +1,23 @@
 // kernels_fluid.cuh — fluid-side kernels of the DiffDFSPH step, templated on the
 // fluid scalar T (float or double).
 //
-// Data layout (HBM, structure of arrays, particles kept in cell order and re-sorted
-// every step by a stable counting sort):
-//   x[i]  : V4<T> (x, y, z, -)        v[i] : V4<T> (vx, vy, vz, -)
-//   kk[i] : stiffness read by the next velocity-correction pass
-//   rho, alpha (DFSPH factor), kappa, kappaV, rhoAdv : T
-//   sumgrad[i] : V4<T> (sum_grad_p_k, -)
-//   fluid neighbours of i: flist[k * n + i], k < fcount[i]   (neighbour-major: coalesced)
+// Data layout (HBM; particles kept in cell order and re-sorted every step by a
+// stable counting sort):
+//   R[i]  : Rec<T> = { x, y, z, - | vx, vy, vz, m_i / rho_i }   (32 bytes in FP32: one
+//           256-bit load gives a neighbour's position and velocity)
+//   Q[i]  : V4<T> (x, y, z, k) during a solve: the stiffness each density pass produces
+//           for the next velocity-correction pass
+//   rho, alpha (DFSPH factor), kappa, kappaV, rhoAdv : T;  sumgrad[i] : V4<T>
+//   fluid neighbours of i: flist[k * n + i], k < fcount[i]   (neighbour-major)
 //   boundary neighbours of i: blist[k * n + i], k < bcount[i]
+// The neighbour passes run LPP lanes per particle (sub-lane s visits list entries
+// k = s, s + LPP, ...; the partial sums are combined with xor-shuffles in a fixed
+// order). LPP = 1 measured fastest on GB300: the passes are bound by L1 data
+// wavefronts (about one per distinct 32-byte record a warp gathers), which more
+// lanes per particle do not reduce.
 // Boundary samples: static ones sorted once; dynamic ones in body order (xd, vd, x0d)
-// plus a per-step cell-sorted copy appended after the static ones (bx, bv: x,y,z,psi).
+// plus a per-step cell-sorted copy after the static ones, both in BR[j] =
+// { x, y, z, psi | vx, vy, vz, - }.
 #pragma once
 #include "common.cuh"
 
@@ -25,14 +32,32 @@ struct FluidConsts {
   int kf, kb;  // list capacities
 };
 
+template <class T>
+struct alignas(8 * sizeof(T)) Rec {
+  V4<T> x, v;
+};
+
+// Whole-record load through the read-only path (the record is not written by the
+// kernel that calls this): one 256-bit request in FP32.
+template <class T> static __device__ __forceinline__ Rec<T> ld_rec(const Rec<T> *p) { return *p; }
+template <> __device__ __forceinline__ Rec<float> ld_rec<float>(const Rec<float> *p) {
+  Rec<float> r;
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(r.x.x), "=f"(r.x.y), "=f"(r.x.z), "=f"(r.x.w), "=f"(r.v.x), "=f"(r.v.y), "=f"(r.v.z), "=f"(r.v.w)
+      : "l"(p));
+  return r;
+}
+
 // ------------------------------------------------------------------ sorting
 
+// pts[i * stride] is the position of point i (stride 2 for Rec arrays, 1 for V4 arrays)
 template <class T>
-static __global__ void k_cell_keys(int n, const V4<T> *__restrict__ x, Grid<T> g, int *__restrict__ key,
-                            int *__restrict__ rank, int *__restrict__ count, int *__restrict__ err) {
+static __global__ void k_cell_keys(int n, const V4<T> *__restrict__ pts, int stride, Grid<T> g,
+                                   int *__restrict__ key, int *__restrict__ rank, int *__restrict__ count,
+                                   int *__restrict__ err) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const V4<T> p = x[i];
+  const V4<T> p = pts[(size_t)i * stride];
   if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) atomicOr(err, ERR_NONFINITE_POSITION);
   int cx, cy, cz;
   grid_cell(g, p.x, p.y, p.z, cx, cy, cz);
@@ -63,16 +88,14 @@ static __global__ void k_cell_insertion_sort(int ncell, const int *__restrict__ 
 }
 
 template <class T>
-static __global__ void k_gather_fluid(int n, const int *__restrict__ order, const V4<T> *__restrict__ x,
-                               const V4<T> *__restrict__ v, const T *__restrict__ kappa,
-                               const T *__restrict__ kappaV, const int *__restrict__ perm, V4<T> *__restrict__ x2,
-                               V4<T> *__restrict__ v2, T *__restrict__ kappa2, T *__restrict__ kappaV2,
-                               int *__restrict__ perm2) {
+static __global__ void k_gather_fluid(int n, const int *__restrict__ order, const Rec<T> *__restrict__ R,
+                                      const T *__restrict__ kappa, const T *__restrict__ kappaV,
+                                      const int *__restrict__ perm, Rec<T> *__restrict__ R2, T *__restrict__ kappa2,
+                                      T *__restrict__ kappaV2, int *__restrict__ perm2) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int o = order[i];
-  x2[i] = x[o];
-  v2[i] = v[o];
+  R2[i] = ld_rec(R + o);
   kappa2[i] = kappa[o];
   kappaV2[i] = kappaV[o];
   perm2[i] = perm[o];
@@ -81,13 +104,12 @@ static __global__ void k_gather_fluid(int n, const int *__restrict__ order, cons
 // dynamic boundary: body order -> cell order copy behind the static samples
 template <class T>
 static __global__ void k_gather_dynamic(int nd, int ns, const int *__restrict__ order, const V4<T> *__restrict__ xd,
-                                 const V4<T> *__restrict__ vd, V4<T> *__restrict__ bx, V4<T> *__restrict__ bv,
-                                 int *__restrict__ dyn_sorted_to_body) {
+                                        const V4<T> *__restrict__ vd, Rec<T> *__restrict__ BR,
+                                        int *__restrict__ dyn_sorted_to_body) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= nd) return;
   const int o = order[j];
-  bx[ns + j] = xd[o];
-  bv[ns + j] = vd[o];
+  BR[ns + j] = Rec<T>{xd[o], vd[o]};
   dyn_sorted_to_body[j] = o;
 }
 
@@ -112,15 +134,16 @@ static __device__ __forceinline__ void for_each_row(const Grid<T> &g, const int 
 
 // Neighbour lists (fluid and boundary), density (TimeStep.cpp:147-200) and the
 // DFSPH factor with sum_grad_p_k (TimeStepDiffDFSPH.cpp:883-962), fused in one pass.
+// Also stores the XSPH weight m_i / rho_i in v[i].w for the viscosity pass.
 template <class T>
 static __global__ void __launch_bounds__(256) k_lists_density_factor(
-    FluidConsts<T> c, const V4<T> *__restrict__ x, const int *__restrict__ cstartF, const V4<T> *__restrict__ bx,
-    const int *__restrict__ cstartS, const int *__restrict__ cstartD, int ns, int *__restrict__ flist,
-    int *__restrict__ fcount, int *__restrict__ blist, int *__restrict__ bcount, T *__restrict__ rho,
-    T *__restrict__ alpha, V4<T> *__restrict__ sumgrad, int *__restrict__ err) {
+    FluidConsts<T> c, Rec<T> *__restrict__ R, const int *__restrict__ cstartF,
+    const Rec<T> *__restrict__ BR, const int *__restrict__ cstartS, const int *__restrict__ cstartD, int ns,
+    int *__restrict__ flist, int *__restrict__ fcount, int *__restrict__ blist, int *__restrict__ bcount,
+    T *__restrict__ rho, T *__restrict__ alpha, V4<T> *__restrict__ sumgrad, int *__restrict__ err) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= c.n) return;
-  const V4<T> xi = x[i];
+  const V4<T> xi = R[i].x;
   int cx, cy, cz;
   grid_cell(c.grid, xi.x, xi.y, xi.z, cx, cy, cz);
   T dens = c.V * c.kc.w0;
@@ -128,20 +151,26 @@ static __global__ void __launch_bounds__(256) k_lists_density_factor(
   V3<T> gpi = {T(0), T(0), T(0)};
   int cnt = 0;
   for_each_row(c.grid, cstartF, cx, cy, cz, [&](int b, int e) {
-    for (int j = b; j < e; j++) {
-      if (j == i) continue;
-      const V4<T> xj = x[j];
-      const T dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
-      const T d2 = dist2_rn(dx, dy, dz);
-      if (d2 < c.h2) {
-        if (cnt < c.kf) flist[(size_t)cnt * c.n + i] = j;
-        cnt++;
-        const T rl = sqrt(d2);
-        dens += c.V * cubic_W(rl, c.kc);
-        const V3<T> gw = cubic_gradW(mk3(dx, dy, dz), rl, c.kc);
-        const V3<T> gpj = (-c.V) * gw;
-        sgk += dot(gpj, gpj);
-        gpi = gpi - gpj;
+    for (int j0 = b; j0 < e; j0 += 4) {
+      V4<T> xs[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+        if (j0 + u < e) xs[u] = R[j0 + u].x;
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int j = j0 + u;
+        if (j >= e || j == i) continue;
+        const T dx = xi.x - xs[u].x, dy = xi.y - xs[u].y, dz = xi.z - xs[u].z;
+        const T d2 = dist2_rn(dx, dy, dz);
+        if (d2 < c.h2) {
+          if (cnt < c.kf) flist[(size_t)cnt * c.n + i] = j;
+          cnt++;
+          dens += c.V * KEval<T>::W(d2, c.kc);
+          const T g = KEval<T>::G(d2, c.kc);
+          const V3<T> gpj = (-c.V) * V3<T>{g * dx, g * dy, g * dz};
+          sgk += dot(gpj, gpj);
+          gpi = gpi - gpj;
+        }
       }
     }
   });
@@ -150,16 +179,15 @@ static __global__ void __launch_bounds__(256) k_lists_density_factor(
   int bc = 0;
   auto visit_boundary = [&](int b, int e, int off) {
     for (int j = b; j < e; j++) {
-      const V4<T> xj = bx[off + j];
+      const V4<T> xj = BR[off + j].x;
       const T dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
       const T d2 = dist2_rn(dx, dy, dz);
       if (d2 < c.h2) {
         if (bc < c.kb) blist[(size_t)bc * c.n + i] = off + j;
         bc++;
-        const T rl = sqrt(d2);
-        dens += xj.w * cubic_W(rl, c.kc);
-        const V3<T> gw = cubic_gradW(mk3(dx, dy, dz), rl, c.kc);
-        const V3<T> gpj = (-xj.w) * gw;
+        dens += xj.w * KEval<T>::W(d2, c.kc);
+        const T g = KEval<T>::G(d2, c.kc);
+        const V3<T> gpj = (-xj.w) * V3<T>{g * dx, g * dy, g * dz};
         gpi = gpi - gpj;
       }
     }
@@ -168,7 +196,9 @@ static __global__ void __launch_bounds__(256) k_lists_density_factor(
   if (cstartD) for_each_row(c.grid, cstartD, cx, cy, cz, [&](int b, int e) { visit_boundary(b, e, ns); });
   if (bc > c.kb) { atomicOr(err, ERR_BOUNDARY_LIST_OVERFLOW); bc = c.kb; }
   bcount[i] = bc;
-  rho[i] = dens * c.rho0;
+  const T rh = dens * c.rho0;
+  rho[i] = rh;
+  R[i].v.w = c.m / rh;
   sumgrad[i] = V4<T>{-gpi.x, -gpi.y, -gpi.z, T(0)};
   sgk += dot(gpi, gpi);
   alpha[i] = (sgk > c.eps) ? -T(1) / sgk : T(0);
@@ -176,7 +206,7 @@ static __global__ void __launch_bounds__(256) k_lists_density_factor(
 
 // Fluid neighbours of each dynamic boundary sample (body order).
 template <class T>
-static __global__ void k_bf_lists(FluidConsts<T> c, int nd, const V4<T> *__restrict__ xd, const V4<T> *__restrict__ x,
+static __global__ void k_bf_lists(FluidConsts<T> c, int nd, const V4<T> *__restrict__ xd, const Rec<T> *__restrict__ R,
                            const int *__restrict__ cstartF, int kbf, int *__restrict__ bflist,
                            int *__restrict__ bfcount, int *__restrict__ err) {
   const int d = blockIdx.x * blockDim.x + threadIdx.x;
@@ -187,7 +217,7 @@ static __global__ void k_bf_lists(FluidConsts<T> c, int nd, const V4<T> *__restr
   int cnt = 0;
   for_each_row(c.grid, cstartF, cx, cy, cz, [&](int b, int e) {
     for (int i = b; i < e; i++) {
-      const V4<T> xi = x[i];
+      const V4<T> xi = R[i].x;
       const T dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
       if (dist2_rn(dx, dy, dz) < c.h2) {
         if (cnt < kbf) bflist[(size_t)cnt * nd + d] = i;
@@ -203,22 +233,22 @@ static __global__ void k_bf_lists(FluidConsts<T> c, int nd, const V4<T> *__restr
 // (BoundaryModel_Akinci2012.cpp:257-284 via Simulation::updateBoundaryVolume).
 // Samples p < ns are static (cell-sorted), p >= ns dynamic (sorted copy).
 template <class T>
-static __global__ void k_boundary_psi(FluidConsts<T> c, int ns, int nd, const V4<T> *__restrict__ bx,
+static __global__ void k_boundary_psi(FluidConsts<T> c, int ns, int nd, const Rec<T> *__restrict__ BR,
                                const int *__restrict__ cstartS, const int *__restrict__ cstartD,
                                T *__restrict__ psi_out) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= ns + nd) return;
-  const V4<T> xp = bx[p];
+  const V4<T> xp = BR[p].x;
   int cx, cy, cz;
   grid_cell(c.grid, xp.x, xp.y, xp.z, cx, cy, cz);
   T delta = c.kc.w0;
   auto visit = [&](int b, int e, int off) {
     for (int j = b; j < e; j++) {
       if (off + j == p) continue;
-      const V4<T> xj = bx[off + j];
+      const V4<T> xj = BR[off + j].x;
       const T dx = xp.x - xj.x, dy = xp.y - xj.y, dz = xp.z - xj.z;
       const T d2 = dist2_rn(dx, dy, dz);
-      if (d2 < c.h2) delta += cubic_W(sqrt(d2), c.kc);
+      if (d2 < c.h2) delta += KEval<T>::W(d2, c.kc);
     }
   };
   if (ns > 0) for_each_row(c.grid, cstartS, cx, cy, cz, [&](int b, int e) { visit(b, e, 0); });
@@ -227,11 +257,11 @@ static __global__ void k_boundary_psi(FluidConsts<T> c, int ns, int nd, const V4
 }
 
 template <class T>
-static __global__ void k_set_psi(int ns, int nd, const T *__restrict__ psi, V4<T> *__restrict__ bx, V4<T> *__restrict__ xd,
-                          const int *__restrict__ dyn_sorted_to_body) {
+static __global__ void k_set_psi(int ns, int nd, const T *__restrict__ psi, Rec<T> *__restrict__ BR,
+                                 V4<T> *__restrict__ xd, const int *__restrict__ dyn_sorted_to_body) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= ns + nd) return;
-  bx[p].w = psi[p];
+  BR[p].x.w = psi[p];
   if (p >= ns) xd[dyn_sorted_to_body[p - ns]].w = psi[p];
 }
 
@@ -259,37 +289,69 @@ enum PassMode : int {
   PASS_DIVERGENCE_WARM = 3,  // rho_dot, kappaV = rho_dot > 0 ? .5 max(kappaV, -.5)/h : 0      (:1721-1732)
 };
 
+constexpr int LPP = 1;  // lanes per particle in the neighbour passes
+
+// Visits the entries k = s, s + LPP, ... < cnt of the neighbour-major list of particle i
+// for sub-lane s, U at a time: U index loads, then U gathers (load(j)), then U bodies.
+template <int U, class D, class LoadF, class BodyF>
+static __device__ __forceinline__ void for_neighbors_sub(int cnt, const int *__restrict__ list, int n, int i, int s,
+                                                         LoadF &&load, BodyF &&body) {
+  for (int k0 = s; k0 < cnt; k0 += U * LPP) {
+    int js[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) js[u] = (k0 + u * LPP < cnt) ? __ldcs(list + (size_t)(k0 + u * LPP) * n + i) : -1;
+    D d[U];
+#pragma unroll
+    for (int u = 0; u < U; u++)
+      if (js[u] >= 0) d[u] = load(js[u]);
+#pragma unroll
+    for (int u = 0; u < U; u++)
+      if (js[u] >= 0) body(d[u]);
+  }
+}
+
+// Sum over the LPP sub-lanes of a particle (all lanes of the warp take part).
+template <class T> static __device__ __forceinline__ T sub_sum(T v) {
+#pragma unroll
+  for (int o = 1; o < LPP; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
 // Density advection / density change of every particle, the stiffness for the next
 // velocity correction, and the block partials of the solver residual.
+// Reads R (positions, velocities); writes Q[i] = (x_i, k_i): the next velocity pass
+// gathers position and stiffness of a neighbour with one 16-byte load.
 template <class T, int MODE>
 static __global__ void __launch_bounds__(256) k_density_pass(
-    FluidConsts<T> c, const V4<T> *__restrict__ x, const V4<T> *__restrict__ v, const V4<T> *__restrict__ bx,
-    const V4<T> *__restrict__ bv, const int *__restrict__ flist, const int *__restrict__ fcount,
-    const int *__restrict__ blist, const int *__restrict__ bcount, const T *__restrict__ rho,
-    const T *__restrict__ alpha, T *__restrict__ rhoAdv, T *__restrict__ kk, T *__restrict__ kappa_io,
-    double *__restrict__ partials) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    FluidConsts<T> c, const Rec<T> *__restrict__ R, V4<T> *__restrict__ Q, const Rec<T> *__restrict__ BR,
+    const int *__restrict__ flist, const int *__restrict__ fcount, const int *__restrict__ blist,
+    const int *__restrict__ bcount, const T *__restrict__ rho, const T *__restrict__ alpha, T *__restrict__ rhoAdv,
+    T *__restrict__ kappa_io, double *__restrict__ partials) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = t / LPP, s = t % LPP;
+  const bool live = i < c.n;
   double e = 0.0;
-  if (i < c.n) {
-    const V4<T> xi = x[i], vi4 = v[i];
-    const V3<T> vi = xyz(vi4);
-    T delta = T(0);
-    const int nf = fcount[i];
-    for (int k = 0; k < nf; k++) {
-      const int j = flist[(size_t)k * c.n + i];
-      const V4<T> xj = x[j], vj = v[j];
-      const V3<T> r = {xi.x - xj.x, xi.y - xj.y, xi.z - xj.z};
-      const T rl = sqrt(dot(r, r));
-      delta += c.V * dot(vi - xyz(vj), cubic_gradW(r, rl, c.kc));
-    }
-    const int nb = bcount[i];
-    for (int k = 0; k < nb; k++) {
-      const int j = blist[(size_t)k * c.n + i];
-      const V4<T> xj = bx[j], vj = bv[j];
-      const V3<T> r = {xi.x - xj.x, xi.y - xj.y, xi.z - xj.z};
-      const T rl = sqrt(dot(r, r));
-      delta += xj.w * dot(vi - xyz(vj), cubic_gradW(r, rl, c.kc));
-    }
+  T delta = T(0);
+  int nf = 0, nb = 0;
+  Rec<T> ri;
+  if (live) {
+    ri = ld_rec(R + i);
+    const V4<T> xi = ri.x, vi4 = ri.v;
+    nf = fcount[i];
+    for_neighbors_sub<4, Rec<T>>(nf, flist, c.n, i, s, [&](int j) { return ld_rec(R + j); }, [&](const Rec<T> &d) {
+      const T rx = xi.x - d.x.x, ry = xi.y - d.x.y, rz = xi.z - d.x.z;
+      const T g = KEval<T>::G(rx * rx + ry * ry + rz * rz, c.kc);
+      delta += c.V * (g * ((vi4.x - d.v.x) * rx + (vi4.y - d.v.y) * ry + (vi4.z - d.v.z) * rz));
+    });
+    nb = bcount[i];
+    for_neighbors_sub<4, Rec<T>>(nb, blist, c.n, i, s, [&](int j) { return ld_rec(BR + j); }, [&](const Rec<T> &d) {
+      const T rx = xi.x - d.x.x, ry = xi.y - d.x.y, rz = xi.z - d.x.z;
+      const T g = KEval<T>::G(rx * rx + ry * ry + rz * rz, c.kc);
+      delta += d.x.w * (g * ((vi4.x - d.v.x) * rx + (vi4.y - d.v.y) * ry + (vi4.z - d.v.z) * rz));
+    });
+  }
+  delta = sub_sum(delta);
+  if (live && s == 0) {
     T ra;
     if (MODE == PASS_PRESSURE || MODE == PASS_PRESSURE_WARM) {
       ra = rho[i] / c.rho0 + c.dt * delta;
@@ -299,124 +361,137 @@ static __global__ void __launch_bounds__(256) k_density_pass(
       if (nf + nb < 20) ra = T(0);
     }
     rhoAdv[i] = ra;
+    T kq;
     if (MODE == PASS_PRESSURE) {
-      kk[i] = (ra - T(1)) * alpha[i] * c.invH2;
+      kq = (ra - T(1)) * alpha[i] * c.invH2;
       e = (double)(c.rho0 * ra - c.rho0);
     } else if (MODE == PASS_DIVERGENCE) {
-      kk[i] = ra * alpha[i] * c.invH;
+      kq = ra * alpha[i] * c.invH;
       e = (double)(c.rho0 * ra);
     } else if (MODE == PASS_PRESSURE_WARM) {
       const T kp = kappa_io[i];
-      const T kn = (ra > T(1)) ? T(0.5) * (kp > T(-0.00025) ? kp : T(-0.00025)) * c.invH2 : T(0);
-      kappa_io[i] = kn;
-      kk[i] = kn;
+      kq = (ra > T(1)) ? T(0.5) * (kp > T(-0.00025) ? kp : T(-0.00025)) * c.invH2 : T(0);
+      kappa_io[i] = kq;
     } else {
       const T kp = kappa_io[i];
-      const T kn = (ra > T(0)) ? T(0.5) * (kp > T(-0.5) ? kp : T(-0.5)) * c.invH : T(0);
-      kappa_io[i] = kn;
-      kk[i] = kn;
+      kq = (ra > T(0)) ? T(0.5) * (kp > T(-0.5) ? kp : T(-0.5)) * c.invH : T(0);
+      kappa_io[i] = kq;
     }
+    Q[i] = V4<T>{ri.x.x, ri.x.y, ri.x.z, kq};
   }
   if (partials) block_partial_sum(e, partials);
 }
 
-// Velocity correction with stiffness kk (warm start or Jacobi sweep):
+// Velocity correction with the stiffness k held in Q[.].w (warm start or Jacobi sweep):
 // v_i -= dt sum_f (k_i + k_j)(-V grad W) [if |k_i + k_j| > eps];
 // v_i += -dt k_i (-psi grad W) over boundary neighbours [if |k_i| > eps].
-// ACC = 1 adds k_i to kappa_acc (the solver's running stiffness).
+// ACC = 1 adds k_i to kappa_acc (the solver's running stiffness). v[i].w is kept.
 template <class T, int ACC>
 static __global__ void __launch_bounds__(256) k_velocity_pass(
-    FluidConsts<T> c, const V4<T> *__restrict__ x, V4<T> *__restrict__ v, const V4<T> *__restrict__ bx,
+    FluidConsts<T> c, const V4<T> *__restrict__ Q, Rec<T> *__restrict__ R, const Rec<T> *__restrict__ BR,
     const int *__restrict__ flist, const int *__restrict__ fcount, const int *__restrict__ blist,
-    const int *__restrict__ bcount, const T *__restrict__ kk, T *__restrict__ kappa_acc) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= c.n) return;
-  const T ki = kk[i];
-  if (ACC) kappa_acc[i] += ki;
-  const V4<T> xi = x[i];
-  V4<T> vi = v[i];
-  const int nf = fcount[i];
-  for (int k = 0; k < nf; k++) {
-    const int j = flist[(size_t)k * c.n + i];
-    const T kSum = ki + kk[j];
-    if (fabs(kSum) > c.eps) {
-      const V4<T> xj = x[j];
-      const V3<T> r = {xi.x - xj.x, xi.y - xj.y, xi.z - xj.z};
-      const T rl = sqrt(dot(r, r));
-      const V3<T> gpj = (-c.V) * cubic_gradW(r, rl, c.kc);
-      const T s = c.dt * kSum;
-      vi.x -= s * gpj.x; vi.y -= s * gpj.y; vi.z -= s * gpj.z;
+    const int *__restrict__ bcount, T *__restrict__ kappa_acc) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = t / LPP, s = t % LPP;
+  const bool live = i < c.n;
+  T dvx = T(0), dvy = T(0), dvz = T(0);
+  T ki = T(0);
+  if (live) {
+    const V4<T> qi = Q[i];
+    ki = qi.w;
+    const T sV = c.dt * c.V;
+    for_neighbors_sub<8, V4<T>>(fcount[i], flist, c.n, i, s, [&](int j) { return Q[j]; }, [&](const V4<T> &qj) {
+      const T kSum = ki + qj.w;
+      if (fabs(kSum) > c.eps) {
+        const T rx = qi.x - qj.x, ry = qi.y - qj.y, rz = qi.z - qj.z;
+        const T f = sV * kSum * KEval<T>::G(rx * rx + ry * ry + rz * rz, c.kc);
+        dvx += f * rx; dvy += f * ry; dvz += f * rz;
+      }
+    });
+    if (fabs(ki) > c.eps) {
+      const T sk = c.dt * ki;
+      for_neighbors_sub<8, V4<T>>(bcount[i], blist, c.n, i, s, [&](int j) { return BR[j].x; }, [&](const V4<T> &xj) {
+        const T rx = qi.x - xj.x, ry = qi.y - xj.y, rz = qi.z - xj.z;
+        const T f = sk * xj.w * KEval<T>::G(rx * rx + ry * ry + rz * rz, c.kc);
+        dvx += f * rx; dvy += f * ry; dvz += f * rz;
+      });
     }
   }
-  if (fabs(ki) > c.eps) {
-    const int nb = bcount[i];
-    const T s = -c.dt * T(1) * ki;
-    for (int k = 0; k < nb; k++) {
-      const int j = blist[(size_t)k * c.n + i];
-      const V4<T> xj = bx[j];
-      const V3<T> r = {xi.x - xj.x, xi.y - xj.y, xi.z - xj.z};
-      const T rl = sqrt(dot(r, r));
-      const V3<T> gpj = (-xj.w) * cubic_gradW(r, rl, c.kc);
-      vi.x += s * gpj.x; vi.y += s * gpj.y; vi.z += s * gpj.z;
-    }
+  dvx = sub_sum(dvx); dvy = sub_sum(dvy); dvz = sub_sum(dvz);
+  if (live && s == 0) {
+    if (ACC) kappa_acc[i] += ki;
+    V4<T> vi = R[i].v;
+    vi.x += dvx; vi.y += dvy; vi.z += dvz;
+    R[i].v = vi;
   }
-  v[i] = vi;
 }
 
 // clearAccelerations + XSPH viscosity + v += dt a (TimeStep.cpp:66-81,
 // Viscosity_XSPH.cpp:35-110, TimeStepDiffDFSPH.cpp:588-605); also kappaV *= dt
 // (end of the divergence solve, :870-880) when scale_kappaV is set.
+// v[j].w holds m_j / rho_j.
 template <class T>
-static __global__ void __launch_bounds__(256) k_xsph_advect(FluidConsts<T> c, const V4<T> *__restrict__ x,
-                                                     const V4<T> *__restrict__ v, V4<T> *__restrict__ v_out,
-                                                     const int *__restrict__ flist, const int *__restrict__ fcount,
-                                                     const T *__restrict__ rho, T *__restrict__ kappaV,
-                                                     int scale_kappaV) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= c.n) return;
-  const V4<T> xi = x[i], vi = v[i];
-  V3<T> a = {c.gx, c.gy, c.gz};
-  const int nf = fcount[i];
-  const T cvis = c.invH * c.visc;
-  for (int k = 0; k < nf; k++) {
-    const int j = flist[(size_t)k * c.n + i];
-    const V4<T> xj = x[j], vj = v[j];
-    const V3<T> r = {xi.x - xj.x, xi.y - xj.y, xi.z - xj.z};
-    const T w = cubic_W(sqrt(dot(r, r)), c.kc);
-    const T s = cvis * (c.m / rho[j]);
-    a.x -= s * (vi.x - vj.x) * w;
-    a.y -= s * (vi.y - vj.y) * w;
-    a.z -= s * (vi.z - vj.z) * w;
+static __global__ void __launch_bounds__(256) k_xsph_advect(FluidConsts<T> c, const Rec<T> *__restrict__ R,
+                                                            Rec<T> *__restrict__ R_out, const int *__restrict__ flist,
+                                                            const int *__restrict__ fcount, T *__restrict__ kappaV,
+                                                            int scale_kappaV) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = t / LPP, s = t % LPP;
+  const bool live = i < c.n;
+  T ax = T(0), ay = T(0), az = T(0);
+  Rec<T> ri;
+  if (live) {
+    ri = ld_rec(R + i);
+    const V4<T> xi = ri.x, vi = ri.v;
+    const T cvis = c.invH * c.visc;
+    for_neighbors_sub<4, Rec<T>>(fcount[i], flist, c.n, i, s, [&](int j) { return ld_rec(R + j); },
+                                 [&](const Rec<T> &d) {
+      const T rx = xi.x - d.x.x, ry = xi.y - d.x.y, rz = xi.z - d.x.z;
+      const T w = KEval<T>::W(rx * rx + ry * ry + rz * rz, c.kc);
+      const T f = cvis * d.v.w;
+      ax -= f * (vi.x - d.v.x) * w;
+      ay -= f * (vi.y - d.v.y) * w;
+      az -= f * (vi.z - d.v.z) * w;
+    });
   }
-  v_out[i] = V4<T>{vi.x + c.dt * a.x, vi.y + c.dt * a.y, vi.z + c.dt * a.z, T(0)};
-  if (scale_kappaV) kappaV[i] *= c.dt;
+  ax = sub_sum(ax); ay = sub_sum(ay); az = sub_sum(az);
+  if (live && s == 0) {
+    const V4<T> vi = ri.v;
+    ax += c.gx; ay += c.gy; az += c.gz;
+    R_out[i] = Rec<T>{ri.x, V4<T>{vi.x + c.dt * ax, vi.y + c.dt * ay, vi.z + c.dt * az, vi.w}};
+    if (scale_kappaV) kappaV[i] *= c.dt;
+  }
 }
 
 // x += dt v (TimeStepDiffDFSPH.cpp:613-635); kappa *= dt^2 (:752-767) when requested.
 template <class T>
-static __global__ void k_integrate(FluidConsts<T> c, V4<T> *__restrict__ x, const V4<T> *__restrict__ v,
-                            T *__restrict__ kappa, int scale_kappa) {
+static __global__ void k_integrate(FluidConsts<T> c, Rec<T> *__restrict__ R, T *__restrict__ kappa, int scale_kappa) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= c.n) return;
-  V4<T> p = x[i];
-  const V4<T> u = v[i];
-  p.x += c.dt * u.x; p.y += c.dt * u.y; p.z += c.dt * u.z;
-  x[i] = p;
+  Rec<T> r = R[i];
+  r.x.x += c.dt * r.v.x; r.x.y += c.dt * r.v.y; r.x.z += c.dt * r.v.z;
+  R[i].x = r.x;
   if (scale_kappa) kappa[i] *= c.dt * c.dt;
 }
 
-// Final residual sum (one warp, fixed order); also publishes the device error word
-// next to it in mapped host memory, so one stream synchronisation reads both.
-static __global__ void k_final_sum(int nparts, const double *__restrict__ partials, double scale,
-                                   double *__restrict__ out, double *__restrict__ out_host,
-                                   const int *__restrict__ err) {
+// Final residual sum (one block of 256 threads, fixed order); also publishes the
+// device error word next to it in mapped host memory, so one stream synchronisation
+// reads both.
+static __global__ void __launch_bounds__(256) k_final_sum(int nparts, const double *__restrict__ partials,
+                                                          double scale, double *__restrict__ out,
+                                                          double *__restrict__ out_host, const int *__restrict__ err) {
+  __shared__ double ws[8];
   double s = 0.0;
-  for (int k = threadIdx.x; k < nparts; k += 32) s += partials[k];
+  for (int k = threadIdx.x; k < nparts; k += blockDim.x) s += partials[k];
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
   if (threadIdx.x == 0) {
-    *out = s * scale;
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += ws[w];
+    *out = t * scale;
     if (out_host) {
-      out_host[0] = s * scale;
+      out_host[0] = t * scale;
       out_host[1] = (double)(*err);
     }
   }

@@ -114,7 +114,8 @@ struct PairConsts {
   int optimize_rotation;
 };
 
-// One warp per dynamic boundary sample j, lanes over its fluid neighbours i.
+// One warp per dynamic boundary sample j, lanes over its fluid neighbours i; x[i].w
+// carries the stiffness k_i of the current pass.
 // Force: the Akinci reaction f_ij = -m_i (-dt k_i (-psi_j grad W_ij)) / dt that the
 // fluid-side velocity correction applies (TimeStepDiffDFSPH.cpp:1038-1053, 1139-1196,
 // 1767-1784, 1862-1901), only where |k_i| > eps, k_i the pass's stiffness.
@@ -128,9 +129,9 @@ static __global__ void __launch_bounds__(128) k_pairs(FluidConsts<T> c, PairCons
                                                const V4<T> *__restrict__ x0d, const int *__restrict__ bodyd,
                                                const BodyState *__restrict__ bs, const int *__restrict__ bflist,
                                                const int *__restrict__ bfcount, const V4<T> *__restrict__ x,
-                                               const V4<T> *__restrict__ v, const T *__restrict__ alpha,
+                                               const Rec<T> *__restrict__ R, const T *__restrict__ alpha,
                                                const T *__restrict__ rhoAdv, const V4<T> *__restrict__ sumgrad,
-                                               const T *__restrict__ kforce, double *__restrict__ acc) {
+                                               double *__restrict__ acc) {
   const int d = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (d >= nd) return;
@@ -164,13 +165,13 @@ static __global__ void __launch_bounds__(128) k_pairs(FluidConsts<T> c, PairCons
 
   for (int k = lane; k < cnt; k += 32) {
     const int i = bflist[(size_t)k * nd + d];
-    const V4<T> xi4 = x[i];
+    const V4<T> xi4 = x[i];  // position and the pass's stiffness k_i
     const V3<T> r = {xi4.x - xj.x, xi4.y - xj.y, xi4.z - xj.z};
     const T rl = sqrt(dot(r, r));
     const V3<T> g = cubic_gradW(r, rl, c.kc);
     const V3<T> gpj = (-psi) * g;
     {
-      const T kF = kforce[i];
+      const T kF = xi4.w;
       if (fabs(kF) > c.eps) {
         const T s = -c.dt * T(1) * kF;
         facc[0] += (-c.m * (s * gpj.x)) * c.invH;
@@ -186,7 +187,7 @@ static __global__ void __launch_bounds__(128) k_pairs(FluidConsts<T> c, PairCons
     const V3<T> fT = {(-c.m * (sT * gpj.x)) * c.invH, (-c.m * (sT * gpj.y)) * c.invH, (-c.m * (sT * gpj.z)) * c.invH};
     const Sym3<T> Hs = cubic_gradGradW(r, rl, c.kc);
     const V3<T> sg = xyz(sumgrad[i]);
-    const V3<T> dv = xyz(v[i]) - vj;
+    const V3<T> dv = xyz(R[i].v) - vj;
     const bool act = (MODE == 0) ? (ra > T(1)) : (ra > T(0));
     V3<T> gbx = {T(0), T(0), T(0)}, gbv = {T(0), T(0), T(0)}, gbvi = {T(0), T(0), T(0)};
     if (act) {
