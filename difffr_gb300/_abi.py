@@ -220,6 +220,7 @@ def load_library(path: str | None = None):
         "dfsph_profile_read": ([vp, c_int32, POINTER(c_int64), POINTER(c_double), POINTER(c_int64)], c_int32),
         "dfsph_kernel_class_name": ([c_int32], c_char_p),
         "dfsph_set_device": ([c_int32], c_int32),
+        "dfsph_density_error_noalloc": ([c_void_p, c_int32, c_int64, c_double, c_int32, c_void_p, c_void_p], c_int32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -237,6 +238,7 @@ EXPORTED_SYMBOLS = (
     "dfsph_copy_field", "dfsph_set_field", "dfsph_num_particles", "dfsph_get_neighbors", "dfsph_get_time",
     "dfsph_synchronize", "dfsph_launch_count", "dfsph_record_event", "dfsph_event_elapsed",
     "dfsph_profile_enable", "dfsph_profile_read", "dfsph_kernel_class_name", "dfsph_set_device",
+    "dfsph_density_error_noalloc",
 )
 KERNEL_CLASSES = ("sort", "lists_density_factor", "bf_lists", "density_pass", "velocity_pass",
                   "xsph_advect", "integrate", "pairs", "rigid")

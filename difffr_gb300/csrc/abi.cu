@@ -47,6 +47,10 @@ int valid(dfsph_ctx *c) {
 }
 }  // namespace
 
+namespace dfsph {
+void set_last_error(const std::string &msg) { g_last_error = msg; }
+}  // namespace dfsph
+
 extern "C" {
 
 int dfsph_abi_version(void) { return DFSPH_ABI_VERSION; }

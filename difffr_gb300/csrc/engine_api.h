@@ -55,6 +55,8 @@ class EngineBase {
 };
 
 EngineBase *make_engine_fp32(const dfsph_scene *sc);
+// Sets the calling thread's message returned by dfsph_last_error (defined in abi.cu).
+void set_last_error(const std::string &msg);
 EngineBase *make_engine_fp64(const dfsph_scene *sc);
 
 }  // namespace dfsph

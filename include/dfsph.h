@@ -283,6 +283,19 @@ int dfsph_profile_read(dfsph_ctx *ctx, int32_t kernel_class, int64_t *launches, 
                        int64_t *units);
 const char *dfsph_kernel_class_name(int32_t kernel_class);
 
+/* Allocation-free average density error, for callers that cannot allocate GPU memory
+   where they need it (an embedding that gives its whole device budget to its own pool,
+   or a real-time loop that forbids allocations after start-up). No counterpart in the
+   reference. Computes mean(rho0 * rho_adv - rho0) (pressure_mode != 0) or
+   mean(rho0 * rho_adv) (pressure_mode == 0) over n device values (float or double per
+   fluid_precision) into *out (device pointer, one double), with the same fixed-order
+   FP64 reduction the solver uses, on `stream` (a cudaStream_t; NULL = default stream).
+   Its only scratch is a static device array in the library: n is limited to 4,194,304;
+   calls on one device share that array, so calls that overlap on the GPU race; the first
+   call on each device resolves the array's address (make it before any stream capture). */
+int dfsph_density_error_noalloc(const void *rho_adv, int32_t fluid_precision, int64_t n, double density0,
+                                int32_t pressure_mode, double *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
