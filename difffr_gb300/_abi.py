@@ -221,6 +221,13 @@ def load_library(path: str | None = None):
         "dfsph_kernel_class_name": ([c_int32], c_char_p),
         "dfsph_set_device": ([c_int32], c_int32),
         "dfsph_density_error_noalloc": ([c_void_p, c_int32, c_int64, c_double, c_int32, c_void_p, c_void_p], c_int32),
+        "dfsph_set_time": ([vp, c_double, c_int64], c_int32),
+        "dfsph_set_rigid_state": ([vp, c_int32] + [POINTER(c_double)] * 4, c_int32),
+        "dfsph_set_gradient_enabled": ([vp, c_int32], c_int32),
+        "dfsph_checkpoint_save": ([vp, POINTER(c_int32)], c_int32),
+        "dfsph_checkpoint_restore": ([vp, c_int32], c_int32),
+        "dfsph_checkpoint_free": ([vp, c_int32], c_int32),
+        "dfsph_adjoint_sweep": ([vp, POINTER(c_double), POINTER(c_double)], c_int32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -238,7 +245,8 @@ EXPORTED_SYMBOLS = (
     "dfsph_copy_field", "dfsph_set_field", "dfsph_num_particles", "dfsph_get_neighbors", "dfsph_get_time",
     "dfsph_synchronize", "dfsph_launch_count", "dfsph_record_event", "dfsph_event_elapsed",
     "dfsph_profile_enable", "dfsph_profile_read", "dfsph_kernel_class_name", "dfsph_set_device",
-    "dfsph_density_error_noalloc",
+    "dfsph_density_error_noalloc", "dfsph_set_time", "dfsph_set_rigid_state", "dfsph_set_gradient_enabled",
+    "dfsph_checkpoint_save", "dfsph_checkpoint_restore", "dfsph_checkpoint_free", "dfsph_adjoint_sweep",
 )
 KERNEL_CLASSES = ("sort", "lists_density_factor", "bf_lists", "density_pass", "velocity_pass",
                   "xsph_advect", "integrate", "pairs", "rigid")

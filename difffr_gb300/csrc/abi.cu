@@ -310,4 +310,38 @@ const char *dfsph_kernel_class_name(int32_t k) {
   return (k >= 0 && k < DFSPH_K_COUNT) ? names[k] : "";
 }
 
+int dfsph_set_time(dfsph_ctx *ctx, double t, int64_t step_count) {
+  return guard([&] { valid(ctx); ctx->engine->set_time(t, step_count); return DFSPH_OK; });
+}
+
+int dfsph_set_rigid_state(dfsph_ctx *ctx, int32_t body, const double x[3], const double q[4], const double v[3],
+                          const double omega[3]) {
+  return guard([&] { valid(ctx); ctx->engine->set_rigid_state(body, x, q, v, omega); return DFSPH_OK; });
+}
+
+int dfsph_set_gradient_enabled(dfsph_ctx *ctx, int32_t on) {
+  return guard([&] { valid(ctx); ctx->engine->set_gradient_enabled(on != 0); return DFSPH_OK; });
+}
+
+int dfsph_checkpoint_save(dfsph_ctx *ctx, int32_t *slot) {
+  return guard([&] {
+    valid(ctx);
+    if (!slot) throw DfsphException(DFSPH_ERR_INVALID_ARG, "NULL output");
+    *slot = ctx->engine->checkpoint_save();
+    return DFSPH_OK;
+  });
+}
+
+int dfsph_checkpoint_restore(dfsph_ctx *ctx, int32_t slot) {
+  return guard([&] { valid(ctx); ctx->engine->checkpoint_restore(slot); return DFSPH_OK; });
+}
+
+int dfsph_checkpoint_free(dfsph_ctx *ctx, int32_t slot) {
+  return guard([&] { valid(ctx); ctx->engine->checkpoint_free(slot); return DFSPH_OK; });
+}
+
+int dfsph_adjoint_sweep(dfsph_ctx *ctx, const double *lam_in, double *lam_out) {
+  return guard([&] { valid(ctx); ctx->engine->adjoint_sweep(lam_in, lam_out); return DFSPH_OK; });
+}
+
 }  // extern "C"

@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -141,6 +142,13 @@ class Engine : public EngineBase {
   double event_elapsed(int a, int b) override;
   void profile_enable(bool on) override;
   void profile_read(int k, int64_t *launches, double *ms, int64_t *units) override;
+  void set_time(double t, int64_t sc) override { t_ = t; step_count_ = sc; finished_ = t_ >= P_.target_time + P_.uniform_accelerate_rb_time; }
+  void set_rigid_state(int b, const double *x, const double *q, const double *v, const double *w) override;
+  void set_gradient_enabled(bool on) override;
+  int checkpoint_save() override;
+  void checkpoint_restore(int slot) override;
+  void checkpoint_free(int slot) override;
+  void adjoint_sweep(const double *lam_in, double *lam_out) override;
 
  private:
   // configuration
@@ -186,6 +194,19 @@ class Engine : public EngineBase {
   double *resid_host_dev_ = nullptr;
   DBuf<int> err_;
   Scanner scan_;
+  // device-resident snapshots
+  struct Snap {
+    DBuf<Rec<T>> R;
+    DBuf<T> kap, kapV;
+    DBuf<int> perm;
+    DBuf<BodyState> bs;
+    DBuf<V4<T>> xd, vd;
+    double t = 0;
+    int64_t sc = 0;
+    bool finished = false;
+    std::vector<int> anim;
+  };
+  std::vector<std::unique_ptr<Snap>> snaps_;
   // adjoint tape
   DBuf<double> tape_;
   int64_t tape_len_ = 0, tape_cap_ = 0;

@@ -52,6 +52,13 @@ class EngineBase {
   virtual double event_elapsed(int a, int b) = 0;
   virtual void profile_enable(bool on) = 0;
   virtual void profile_read(int k, int64_t *launches, double *ms, int64_t *units) = 0;
+  virtual void set_time(double t, int64_t sc) = 0;
+  virtual void set_rigid_state(int b, const double *x, const double *q, const double *v, const double *w) = 0;
+  virtual void set_gradient_enabled(bool on) = 0;
+  virtual int checkpoint_save() = 0;
+  virtual void checkpoint_restore(int slot) = 0;
+  virtual void checkpoint_free(int slot) = 0;
+  virtual void adjoint_sweep(const double *lam_in, double *lam_out) = 0;
 };
 
 EngineBase *make_engine_fp32(const dfsph_scene *sc);

@@ -506,20 +506,14 @@ template <class T>
 void Engine<T>::launch_pairs(bool pressure, bool warm, bool grad) {
   if (nd_ == 0) return;
   const int ndw = blocks(nd_ * 32, 128);
-  const PairConsts<T> &pc = pressure ? pcP_ : pcD_;
+  PairConsts<T> pc = pressure ? pcP_ : pcD_;
+  pc.grad = (grad && !warm) ? 1 : 0;
   pbegin();
-#define DF_PAIRS(M, W, G)                                                                                          \
-  k_pairs<T, M, W, G><<<ndw, 128, 0, stream_>>>(fc_, pc, nd_, xd_.p, vd_.p, x0d_.p, bodyd_.p, bs_.p, bflist_.p,    \
-                                               bfcount_.p, Q_.p, R_[cur_].p, alpha_.p, rhoAdv_.p, sumgrad_.p, acc_.p)
-  if (pressure) {
-    if (warm) DF_PAIRS(0, true, false);
-    else if (grad) DF_PAIRS(0, false, true);
-    else DF_PAIRS(0, false, false);
-  } else {
-    if (warm) DF_PAIRS(1, true, false);
-    else if (grad) DF_PAIRS(1, false, true);
-    else DF_PAIRS(1, false, false);
-  }
+#define DF_PAIRS(M)                                                                                                \
+  k_pairs<T, M><<<ndw, 128, 0, stream_>>>(fc_, pc, nd_, xd_.p, vd_.p, x0d_.p, bodyd_.p, bs_.p, bflist_.p, bfcount_.p, \
+                                          Q_.p, R_[cur_].p, alpha_.p, rhoAdv_.p, sumgrad_.p, acc_.p)
+  if (pressure) DF_PAIRS(0);
+  else DF_PAIRS(1);
 #undef DF_PAIRS
   launched();
   pend(DFSPH_K_PAIRS, nd_);
@@ -938,5 +932,103 @@ void Engine<T>::profile_read(int k, int64_t *launches, double *ms, int64_t *unit
   if (launches) *launches = prof_launches_[k];
   if (ms) *ms = prof_ms_[k];
   if (units) *units = prof_units_[k];
+}
+}  // namespace dfsph
+
+namespace dfsph {
+template <class T>
+void Engine<T>::set_rigid_state(int b, const double *x, const double *q, const double *v, const double *w) {
+  if (b < 0 || b >= nb_) throw DfsphException(DFSPH_ERR_INVALID_ARG, "body index");
+  if (!x || !q || !v || !w) throw DfsphException(DFSPH_ERR_INVALID_ARG, "NULL vector");
+  const double qn = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+  if (!(qn > 0)) throw DfsphException(DFSPH_ERR_INVALID_ARG, "zero quaternion");
+  std::vector<BodyState> bsv;
+  body_state_download(bsv);
+  BodyState &B = bsv[b];
+  for (int k = 0; k < 3; k++) { B.x[k] = x[k]; B.v[k] = v[k]; B.w[k] = w[k]; }
+  for (int k = 0; k < 4; k++) B.q[k] = q[k] / qn;
+  world_inertia(B);
+  body_state_upload(bsv);
+  if (nd_ > 0) {
+    k_boundary_update<T><<<blocks(nd_), 256, 0, stream_>>>(bs_.p, nd_, x0d_.p, bodyd_.p, xd_.p, vd_.p, 1);
+    launched();
+    DF_CK(cudaStreamSynchronize(stream_));
+  }
+}
+
+template <class T>
+void Engine<T>::set_gradient_enabled(bool on) {
+  P_.enable_gradient = on ? 1 : 0;
+  rc_.enable_gradient = P_.enable_gradient;
+  if (on && nd_ > 0 && tape_cap_ == 0) {
+    tape_cap_ = 256;
+    tape_.alloc((size_t)tape_cap_ * nb_ * NSTATE * NSTATE);
+  }
+}
+
+template <class T>
+int Engine<T>::checkpoint_save() {
+  DF_CK(cudaStreamSynchronize(stream_));
+  std::unique_ptr<Snap> s(new Snap());
+  const size_t N = std::max(n_, 1), ND = std::max(nd_, 1), NBd = std::max(nb_, 1);
+  s->R.alloc(N); s->kap.alloc(N); s->kapV.alloc(N); s->perm.alloc(N);
+  s->bs.alloc(NBd); s->xd.alloc(ND); s->vd.alloc(ND);
+  DF_CK(cudaMemcpyAsync(s->R.p, R_[cur_].p, N * sizeof(Rec<T>), cudaMemcpyDeviceToDevice, stream_));
+  DF_CK(cudaMemcpyAsync(s->kap.p, kappa_[cur_].p, N * sizeof(T), cudaMemcpyDeviceToDevice, stream_));
+  DF_CK(cudaMemcpyAsync(s->kapV.p, kappaV_[cur_].p, N * sizeof(T), cudaMemcpyDeviceToDevice, stream_));
+  DF_CK(cudaMemcpyAsync(s->perm.p, perm_[cur_].p, N * sizeof(int), cudaMemcpyDeviceToDevice, stream_));
+  DF_CK(cudaMemcpyAsync(s->bs.p, bs_.p, NBd * sizeof(BodyState), cudaMemcpyDeviceToDevice, stream_));
+  DF_CK(cudaMemcpyAsync(s->xd.p, xd_.p, ND * sizeof(V4<T>), cudaMemcpyDeviceToDevice, stream_));
+  DF_CK(cudaMemcpyAsync(s->vd.p, vd_.p, ND * sizeof(V4<T>), cudaMemcpyDeviceToDevice, stream_));
+  DF_CK(cudaStreamSynchronize(stream_));
+  s->t = t_; s->sc = step_count_; s->finished = finished_; s->anim = anim_;
+  for (size_t k = 0; k < snaps_.size(); k++)
+    if (!snaps_[k]) { snaps_[k] = std::move(s); return (int)k; }
+  snaps_.push_back(std::move(s));
+  return (int)snaps_.size() - 1;
+}
+
+template <class T>
+void Engine<T>::checkpoint_restore(int slot) {
+  if (slot < 0 || slot >= (int)snaps_.size() || !snaps_[slot]) throw DfsphException(DFSPH_ERR_INVALID_ARG, "checkpoint slot");
+  Snap &s = *snaps_[slot];
+  const size_t N = std::max(n_, 1), ND = std::max(nd_, 1), NBd = std::max(nb_, 1);
+  DF_CK(cudaStreamSynchronize(stream_));
+  DF_CK(cudaMemcpyAsync(R_[cur_].p, s.R.p, N * sizeof(Rec<T>), cudaMemcpyDeviceToDevice, stream_));
+  DF_CK(cudaMemcpyAsync(kappa_[cur_].p, s.kap.p, N * sizeof(T), cudaMemcpyDeviceToDevice, stream_));
+  DF_CK(cudaMemcpyAsync(kappaV_[cur_].p, s.kapV.p, N * sizeof(T), cudaMemcpyDeviceToDevice, stream_));
+  DF_CK(cudaMemcpyAsync(perm_[cur_].p, s.perm.p, N * sizeof(int), cudaMemcpyDeviceToDevice, stream_));
+  DF_CK(cudaMemcpyAsync(bs_.p, s.bs.p, NBd * sizeof(BodyState), cudaMemcpyDeviceToDevice, stream_));
+  DF_CK(cudaMemcpyAsync(xd_.p, s.xd.p, ND * sizeof(V4<T>), cudaMemcpyDeviceToDevice, stream_));
+  DF_CK(cudaMemcpyAsync(vd_.p, s.vd.p, ND * sizeof(V4<T>), cudaMemcpyDeviceToDevice, stream_));
+  if (nd_ > 0) DF_CK(cudaMemsetAsync(acc_.p, 0, (size_t)nd_ * ACC_STRIDE * sizeof(double), stream_));
+  DF_CK(cudaStreamSynchronize(stream_));
+  t_ = s.t; step_count_ = s.sc; finished_ = s.finished; anim_ = s.anim;
+}
+
+template <class T>
+void Engine<T>::checkpoint_free(int slot) {
+  if (slot < 0 || slot >= (int)snaps_.size() || !snaps_[slot]) throw DfsphException(DFSPH_ERR_INVALID_ARG, "checkpoint slot");
+  DF_CK(cudaStreamSynchronize(stream_));
+  snaps_[slot].reset();
+}
+
+template <class T>
+void Engine<T>::adjoint_sweep(const double *lam_in, double *lam_out) {
+  if (!lam_in || !lam_out) throw DfsphException(DFSPH_ERR_INVALID_ARG, "NULL buffer");
+  const size_t m = (size_t)NSTATE * std::max(nb_, 1);
+  if (tape_len_ == 0 || nb_ == 0) {
+    for (size_t k = 0; k < (size_t)NSTATE * nb_; k++) lam_out[k] = lam_in[k];
+    return;
+  }
+  DBuf<double> li, lo;
+  li.alloc(m);
+  lo.alloc(m);
+  DF_CK(cudaMemcpyAsync(li.p, lam_in, (size_t)NSTATE * nb_ * sizeof(double), cudaMemcpyHostToDevice, stream_));
+  k_backward<<<nb_, 32, 0, stream_>>>(tape_.p, (int)tape_len_, nb_, li.p, lo.p);
+  launched();
+  check_launch();
+  DF_CK(cudaMemcpyAsync(lam_out, lo.p, (size_t)NSTATE * nb_ * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+  DF_CK(cudaStreamSynchronize(stream_));
 }
 }  // namespace dfsph

@@ -112,6 +112,7 @@ struct PairConsts {
   T cReal;    // 1/dt^2 (pressure) or 1/dt (divergence)
   T cTrunc;   // the same, truncated to unsigned as at TimeStepDiffDFSPH.cpp:1266 (or not)
   int optimize_rotation;
+  int grad;   // accumulate the pair Jacobians in this launch
 };
 
 // One warp per dynamic boundary sample j, lanes over its fluid neighbours i; x[i].w
@@ -123,7 +124,11 @@ struct PairConsts {
 // helper derivatives (:1485-1694); the nested neighbour sum of :1632-1694 equals
 // -h sum_grad_p_k (pressure) or -sum_grad_p_k (divergence) exactly, because particle
 // positions do not change between the factor pass and the solver sweeps.
-template <class T, int MODE, bool WARM, bool GRAD>
+//
+// The Jacobian switch is a launch constant, not a template parameter: one compiled body
+// serves both, so the force sums (and hence the forward trajectory) are bit-identical
+// whether or not gradients are recorded.
+template <class T, int MODE>
 static __global__ void __launch_bounds__(128) k_pairs(FluidConsts<T> c, PairConsts<T> pc, int nd,
                                                const V4<T> *__restrict__ xd, const V4<T> *__restrict__ vd,
                                                const V4<T> *__restrict__ x0d, const int *__restrict__ bodyd,
@@ -138,7 +143,7 @@ static __global__ void __launch_bounds__(128) k_pairs(FluidConsts<T> c, PairCons
   const int b = bodyd[d];
   const BodyState &B = bs[b];
   if (!B.dyn) return;
-  const bool grad = GRAD && !B.anim;
+  const bool grad = pc.grad && !B.anim;
   const V4<T> xj4 = xd[d];
   const V3<T> xj = xyz(xj4);
   const T psi = xj4.w;

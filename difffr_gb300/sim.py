@@ -188,3 +188,36 @@ class DiffDFSPH:
             check(self.lib, self.lib.dfsph_profile_read(self.h, k, byref(l), byref(ms), byref(u)))
             out[name] = {"launches": l.value, "ms": ms.value, "units": u.value}
         return out
+
+    # -------------------------------------------------------------- state control
+    def set_time(self, t, step_count=0):
+        check(self.lib, self.lib.dfsph_set_time(self.h, float(t), int(step_count)))
+
+    def set_rigid_state(self, b, x, q, v, w):
+        a = [np.ascontiguousarray(z, dtype=np.float64) for z in (x, q, v, w)]
+        check(self.lib, self.lib.dfsph_set_rigid_state(self.h, int(b), *[dptr(z) for z in a]))
+
+    def set_gradient_enabled(self, on=True):
+        check(self.lib, self.lib.dfsph_set_gradient_enabled(self.h, 1 if on else 0))
+
+    def checkpoint_save(self):
+        slot = c_int32()
+        check(self.lib, self.lib.dfsph_checkpoint_save(self.h, byref(slot)))
+        return slot.value
+
+    def checkpoint_restore(self, slot):
+        check(self.lib, self.lib.dfsph_checkpoint_restore(self.h, int(slot)))
+
+    def checkpoint_free(self, slot):
+        check(self.lib, self.lib.dfsph_checkpoint_free(self.h, int(slot)))
+
+    def adjoint_sweep(self, lam):
+        """Full 13-component adjoints (n_bodies, 13) pulled back over the recorded steps."""
+        g = np.ascontiguousarray(lam, dtype=np.float64).reshape(self.n_bodies, 13)
+        out = np.zeros_like(g)
+        check(self.lib, self.lib.dfsph_adjoint_sweep(self.h, dptr(g), dptr(out)))
+        return out
+
+    def rigid_state_vector(self, b):
+        x, q, v, w = self.rigid_state(b)
+        return np.concatenate([x, q, v, w])

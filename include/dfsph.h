@@ -249,6 +249,33 @@ int dfsph_get_neighbors(dfsph_ctx *ctx, int32_t which, int64_t *start, int32_t *
 
 /* Simulated time (TimeManager::getTime) and steps since reset (get_step_count). */
 int dfsph_get_time(dfsph_ctx *ctx, double *t, int64_t *step_count);
+/* Sets the simulated time and step counter (TimeManager::setTime; used when a saved
+   state is restored, SimulatorBase::loadState SimulatorBase.cpp:2046-2203). */
+int dfsph_set_time(dfsph_ctx *ctx, double t, int64_t step_count);
+
+/* Overwrites a body's pose and velocities (Dynamic3dRigidBody::setPosition / setRotation /
+   setVelocity / setAngularVelocity, Dynamic3dRigidBody.h:67-96) and refreshes its boundary
+   samples (SimulatorBase::updateBoundaryParticles). q is (w, x, y, z) and is normalised. */
+int dfsph_set_rigid_state(dfsph_ctx *ctx, int32_t body, const double x[3], const double q[4],
+                          const double v[3], const double omega[3]);
+
+/* Switches the per-sweep pair-Jacobian accumulation and the per-step chain/tape on or off
+   (the reference always accumulates in its BACKWARD build). */
+int dfsph_set_gradient_enabled(dfsph_ctx *ctx, int32_t on);
+
+/* Device-resident snapshots of the full simulation state (fluid records, kappa, kappaV,
+   particle order, rigid states, dynamic samples, time) for checkpointed recomputation
+   (the reference keeps no in-memory checkpoints; it writes state files,
+   SimulatorBase::saveState SimulatorBase.cpp:1899-2005). A snapshot lives in HBM until
+   dfsph_checkpoint_free. */
+int dfsph_checkpoint_save(dfsph_ctx *ctx, int32_t *slot);
+int dfsph_checkpoint_restore(dfsph_ctx *ctx, int32_t slot);
+int dfsph_checkpoint_free(dfsph_ctx *ctx, int32_t slot);
+
+/* Reverse sweep of the recorded step matrices on full 13-component adjoints: lam_out =
+   A_1^T ... A_N^T lam_in, per body (x, q, v, omega). Lets a caller chain the adjoint across
+   recomputed segments; dfsph_backward is this sweep followed by taking the (v, omega) part. */
+int dfsph_adjoint_sweep(dfsph_ctx *ctx, const double *lam_in, double *lam_out);
 
 /* Synchronises the context's stream (for timing from the caller). */
 int dfsph_synchronize(dfsph_ctx *ctx);

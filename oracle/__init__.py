@@ -139,6 +139,15 @@ class Oracle:
         assert self.L.orc_get_rigid_grad(self.h, b, _p(o)) == 0
         return o
 
+    def rigid_grad_blocks(self, b):
+        g = self.rigid_grad(b)
+        return {
+            "x_v0": g[0:9].reshape(3, 3), "x_w0": g[9:18].reshape(3, 3),
+            "q_v0": g[18:30].reshape(4, 3), "q_w0": g[30:42].reshape(4, 3),
+            "v_v0": g[42:51].reshape(3, 3), "v_w0": g[51:60].reshape(3, 3),
+            "w_v0": g[60:69].reshape(3, 3), "w_w0": g[69:78].reshape(3, 3),
+        }
+
     def net_jacobians(self, b):
         o = np.zeros(78)
         assert self.L.orc_get_net_jacobians(self.h, b, _p(o)) == 0

@@ -1,0 +1,149 @@
+"""Scene generators, the scene-JSON reader, and oracle-level checks (CPU only)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from difffr_gb300 import _abi
+from difffr_gb300 import scene as scn
+from difffr_gb300.scene_json import load_scene
+
+
+def test_benchmark_scene_sizes():
+    sc = scn.config1()
+    assert sc.n_fluid == 1_000_000
+    assert 140_000 < sc.n_boundary - sc.n_dynamic_boundary() < 150_000
+    assert sc.n_dynamic_boundary() == 314
+    assert sc.params.time_step == 0.0005 and sc.params.particle_radius == 0.005
+    sc0 = scn.config0()
+    assert sc0.n_fluid == 8000 and sc0.n_dynamic_boundary() == 50
+    sc2 = scn.config2()
+    assert sc2.n_fluid == 250_000 and 2000 < sc2.n_dynamic_boundary() < 2500
+
+
+def test_lattice_jitter_bounds():
+    rng = np.random.default_rng(0)
+    r = 0.01
+    p = scn.fluid_lattice((4, 5, 6), 2 * r, (0, 0, 0), r, rng)
+    base = scn.fluid_lattice((4, 5, 6), 2 * r, (0, 0, 0), r, rng, jitter=False)
+    assert p.shape == (120, 3)
+    assert np.all(np.abs(p - base) <= 0.01 * r)
+
+
+def test_scene_json_fluid_block_and_bodies(tmp_path):
+    data = {
+        "Configuration": {"particleRadius": 0.025, "timeStepSize": 0.002, "maxError": 0.05, "gradientMode": 0,
+                          "targetTime": 0.5, "gravitation": [0, -9.8, 0]},
+        "FluidBlocks": [{"start": [0, 0, 0], "end": [0.5, 0.5, 0.5]}],
+        "RigidBodies": [
+            {"geometryFile": "../models/UnitBox.obj", "scale": [1, 1, 1], "translation": [0.5, 0.5, 0.5],
+             "isDynamic": False, "isWall": True},
+            {"geometryFile": "sphere.obj", "scale": [0.1, 0.1, 0.1], "translation": [0.25, 0.8, 0.25],
+             "isDynamic": True, "density": 500, "initVelocity": [1, 0, 0], "targetX": [0.3, 0.2, 0.1],
+             "rotationAxis": [0, 0, 1], "rotationAngle": 90},
+        ],
+    }
+    f = tmp_path / "s.json"
+    f.write_text(json.dumps(data))
+    sc = load_scene(str(f))
+    # createFluidBlocks: round(0.5 / 0.05) - 1 = 9 points per axis, starting at min + 2r
+    assert sc.n_fluid == 9 ** 3
+    assert np.allclose(sc.fluid_x.min(0), 0.05)
+    assert sc.params.gradient_mode == 0 and sc.params.max_error == 0.05 and sc.params.time_step == 0.002
+    assert sc.params.gravity == (0.0, -9.8, 0.0)
+    s = sc.bodies[1]
+    assert s.is_dynamic and s.init_velocity == (1, 0, 0)
+    assert np.allclose(np.linalg.norm(s.samples, axis=1), 0.1)
+    assert np.allclose(s.rotation, (np.cos(np.pi / 4), 0, 0, np.sin(np.pi / 4)))
+
+
+def test_synthetic_scene_reference_in_json():
+    sc = load_scene({"synthetic": "small_contact", "overrides": {"n": (6, 6, 6)}})
+    assert sc.n_fluid > 0 and len(sc.bodies) == 2
+
+
+def _oracle_pair(oracle_lib, sc, steps):
+    a = oracle_lib.Oracle(sc)
+    for _ in range(steps):
+        a.step(1)
+    return a
+
+
+def test_oracle_step_force_jacobian_against_finite_differences(oracle_lib):
+    """The per-step dF/dv_n of the reference's formulation against central differences of
+    the net fluid force, the check of experiments/others/python/finite-difference.py:78-126.
+    The formulation drops the fluid's coupled response to the boundary velocity, so only the
+    direction is expected to agree (cosine of the flattened 3x3 blocks)."""
+    sc = scn.small_contact_scene(precision=_abi.DFSPH_FP64)
+    ref = _oracle_pair(oracle_lib, sc, 3)
+    x, q, v, w = ref.rigid_state(1)
+    eps = 1e-4
+    J = np.zeros((3, 3))
+    for c in range(3):
+        p, m = _oracle_pair(oracle_lib, sc, 3), _oracle_pair(oracle_lib, sc, 3)
+        vp, vm = v.copy(), v.copy()
+        vp[c] += eps
+        vm[c] -= eps
+        p.set_rigid_velocity(1, vp, w)
+        m.set_rigid_velocity(1, vm, w)
+        p.step(1)
+        m.step(1)
+        J[:, c] = (p.rigid_force(1)[0] - m.rigid_force(1)[0]) / (2 * eps)
+    ref.step(1)
+    Fv = ref.net_jacobians(1)[0:9].reshape(3, 3)
+    cos = float(np.sum(Fv * J) / (np.linalg.norm(Fv) * np.linalg.norm(J)))
+    assert cos > 0.9, (cos, Fv, J)
+
+
+def test_oracle_free_flight_chain_matches_finite_differences(oracle_lib):
+    """Without fluid contact the chain rule is exact rigid-body dynamics: its dx_T/dv0 and
+    dx_T/domega0 must match central differences of full trajectories."""
+    sc = scn.tank_sphere(n=(4, 4, 4), r=0.025, drop_gap=0.6, sphere_v=(0.3, 0.1, -0.2),
+                         sphere_w=(0.5, 1.0, -0.3), precision=_abi.DFSPH_FP64, steps=20,
+                         gradient_mode=_abi.GRAD_COMPLETE)
+    steps = 20
+    base = _oracle_pair(oracle_lib, sc, steps)
+    G = base.rigid_grad(1)
+    Gx_v, Gx_w = G[0:9].reshape(3, 3), G[9:18].reshape(3, 3)
+    eps = 1e-6
+    v0 = np.array(sc.bodies[1].init_velocity)
+    w0 = np.array(sc.bodies[1].init_angular_velocity)
+    fd_v, fd_w = np.zeros((3, 3)), np.zeros((3, 3))
+    for c in range(3):
+        xs = []
+        for sgn in (1, -1):
+            o = oracle_lib.Oracle(sc)
+            dv = np.zeros(3)
+            dv[c] = sgn * eps
+            o.set_rigid_init(1, v0 + dv, w0)
+            for _ in range(steps):
+                o.step(1)
+            xs.append(o.rigid_state(1)[0])
+        fd_v[:, c] = (xs[0] - xs[1]) / (2 * eps)
+        xs = []
+        for sgn in (1, -1):
+            o = oracle_lib.Oracle(sc)
+            dw = np.zeros(3)
+            dw[c] = sgn * eps
+            o.set_rigid_init(1, v0, w0 + dw)
+            for _ in range(steps):
+                o.step(1)
+            xs.append(o.rigid_state(1)[0])
+        fd_w[:, c] = (xs[0] - xs[1]) / (2 * eps)
+    assert np.allclose(Gx_v, fd_v, rtol=1e-4, atol=1e-7), (Gx_v, fd_v)
+    assert np.allclose(Gx_w, fd_w, rtol=1e-4, atol=1e-7), (Gx_w, fd_w)
+
+
+def test_oracle_hydrostatic_column_settles(oracle_lib):
+    """A fluid block at rest in a closed box: densities stay near rest, velocities small."""
+    sc = scn.tank_sphere(n=(8, 8, 8), r=0.025, drop_gap=0.5, precision=_abi.DFSPH_FP64, steps=30)
+    o = oracle_lib.Oracle(sc)
+    for _ in range(30):
+        o.step(1)
+    rho = o.field(_abi.FIELD_DENSITY)
+    v = o.field(_abi.FIELD_V)
+    assert rho.max() < 1.05 * 1000.0
+    assert np.abs(v).max() < 0.5
+    q = o.rigid_state(1)[1]
+    assert abs(np.linalg.norm(q) - 1.0) < 1e-12
