@@ -216,7 +216,8 @@ def run_ours(args):
     sim.step(args.steps)
     prof = sim.profile()
     sim.profile_enable(False)
-    dom = max(prof, key=lambda k: prof[k]["ms"])
+    from difffr_gb300._abi import KERNEL_CLASSES
+    dom = max(KERNEL_CLASSES, key=lambda k: prof[k]["ms"])
     d = prof[dom]
     avg_launch_s = d["ms"] / max(d["launches"], 1) / 1000.0
     units_per_launch = d["units"] / max(d["launches"], 1)
@@ -247,7 +248,8 @@ def run_ours(args):
     # trajectory: set the initial rigid velocity, reset (initial fluid state uploaded from
     # host memory), K steps each followed by a rigid-state read-back, then the adjoint.
     n = sim.n_fluid
-    elt = sizeof_real = 4
+    n_boundary = sim.n_boundary
+    elt = 4
     t0 = time.perf_counter()
     for b in range(nb):
         v0, w0 = sim.rigid_init(b)
@@ -266,6 +268,13 @@ def run_ours(args):
     d2h = nb * body_state_bytes + (nb * 13 * 8) / args.steps
     e2e_value = world * args.steps / e2e_s
 
+    # ---- learned warm start vs the reference warm start (collapse phase of a held-out seed)
+    ws = None
+    if rank == 0 and args.config == 1 and args.ws_steps > 0:
+        sim.close()
+        sim = None
+        ws = warm_start_ab(args)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -280,7 +289,7 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded lattice + sampled boundaries)",
-            "config": {"workload": args.config_name, "n_fluid": n, "n_boundary": sim.n_boundary,
+            "config": {"workload": args.config_name, "n_fluid": n, "n_boundary": n_boundary,
                        "dt": sc.params.time_step, "gradient_mode": "incomplete", "l2": "inputs larger than L2",
                        "parallelism": f"replicas{world}" if world > 1 else "single GPU"},
             "fwd_only_steps_per_s": world * args.steps / (fwd_ms / 1000.0),
@@ -294,10 +303,35 @@ def run_ours(args):
             "kernel_ms_per_step": {k: v["ms"] / args.steps for k, v in prof.items()},
             "clocks": clk,
             "cpu_baseline": cpu,
+            "warm_start": ws,
         }
         print(json.dumps(line), flush=True)
-    sim.close()
+    if sim is not None:
+        sim.close()
     return 0
+
+
+def warm_start_ab(args):
+    """Pressure solve from the reference warm start vs from the learned one, both to the
+    0.01 % density tolerance, on seed 1 from the state after `ws_start` plain steps (the
+    collapse phase, where the solve needs more than its minimum sweeps). The model is the
+    committed one trained on seed 0 (difffr_gb300/train_warmstart.py), or trained here."""
+    from difffr_gb300 import train_warmstart as tw
+    from difffr_gb300.warmstart import WarmStartModel
+    t0 = time.perf_counter()
+    if os.path.exists(tw.DEFAULT_MODEL) and not args.train_warm_start:
+        model = WarmStartModel(seed=0)
+        model.load(tw.DEFAULT_MODEL)
+        source = "committed weights " + os.path.basename(tw.DEFAULT_MODEL)
+    else:
+        model, info = tw.train_model(start=args.ws_start)
+        source = f"trained here on seed 0 ({info['samples']} samples, {info['train_s']:.2f} s)"
+    r = tw.evaluate(model, 1, args.ws_start, args.ws_steps)
+    model.close()
+    r.update({"workload": f"dam_break_sphere_1M seed 1, steps {args.ws_start}-{args.ws_start + args.ws_steps - 1}",
+              "model": source, "tolerance": "0.01 % average density error (both runs)",
+              "wall_s": time.perf_counter() - t0})
+    return r
 
 
 def main():
@@ -309,6 +343,9 @@ def main():
     ap.add_argument("--config", type=int, default=1)
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ws-start", type=int, default=300)
+    ap.add_argument("--ws-steps", type=int, default=200)
+    ap.add_argument("--train-warm-start", action="store_true")
     args = ap.parse_args()
     args.config_name = {0: "tank_sphere_8k (20^3 lattice, r 0.025)",
                         1: "dam_break_sphere_1M (100^3 lattice, r 0.005, 2.4x1.2x1.2 box, R 0.05 sphere)",

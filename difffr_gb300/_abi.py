@@ -7,7 +7,7 @@ from __future__ import annotations
 
 import ctypes
 import os
-from ctypes import POINTER, c_char_p, c_double, c_int32, c_int64, c_void_p
+from ctypes import POINTER, c_char_p, c_double, c_float, c_int32, c_int64, c_uint64, c_void_p
 
 import numpy as np
 
@@ -228,6 +228,17 @@ def load_library(path: str | None = None):
         "dfsph_checkpoint_restore": ([vp, c_int32], c_int32),
         "dfsph_checkpoint_free": ([vp, c_int32], c_int32),
         "dfsph_adjoint_sweep": ([vp, POINTER(c_double), POINTER(c_double)], c_int32),
+        "dfsph_mlp_create": ([c_int32, c_uint64, POINTER(vp)], c_int32),
+        "dfsph_mlp_destroy": ([vp], c_int32),
+        "dfsph_mlp_get_params": ([vp, POINTER(c_float), POINTER(c_float)], c_int32),
+        "dfsph_mlp_set_params": ([vp, POINTER(c_float), POINTER(c_float)], c_int32),
+        "dfsph_mlp_fit_normalization": ([vp, vp, vp, c_int64], c_int32),
+        "dfsph_mlp_train_step": ([vp, vp, vp, c_int64, vp, c_int64, c_float, POINTER(c_double)], c_int32),
+        "dfsph_mlp_gradient": ([vp, vp, vp, c_int64, POINTER(c_double), POINTER(c_double)], c_int32),
+        "dfsph_mlp_predict": ([vp, vp, vp, c_int64], c_int32),
+        "dfsph_set_warmstart_model": ([vp, vp], c_int32),
+        "dfsph_ml_record": ([vp, c_int32], c_int32),
+        "dfsph_ml_capture": ([vp, vp, vp, c_int64, POINTER(c_int64)], c_int32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -247,9 +258,14 @@ EXPORTED_SYMBOLS = (
     "dfsph_profile_enable", "dfsph_profile_read", "dfsph_kernel_class_name", "dfsph_set_device",
     "dfsph_density_error_noalloc", "dfsph_set_time", "dfsph_set_rigid_state", "dfsph_set_gradient_enabled",
     "dfsph_checkpoint_save", "dfsph_checkpoint_restore", "dfsph_checkpoint_free", "dfsph_adjoint_sweep",
+    "dfsph_mlp_create", "dfsph_mlp_destroy", "dfsph_mlp_get_params", "dfsph_mlp_set_params",
+    "dfsph_mlp_fit_normalization", "dfsph_mlp_train_step", "dfsph_mlp_gradient", "dfsph_mlp_predict",
+    "dfsph_set_warmstart_model", "dfsph_ml_record", "dfsph_ml_capture",
 )
 KERNEL_CLASSES = ("sort", "lists_density_factor", "bf_lists", "density_pass", "velocity_pass",
-                  "xsph_advect", "integrate", "pairs", "rigid")
+                  "xsph_advect", "integrate", "pairs", "rigid", "mlp")
+PHASES = ("divergence_solve", "pressure_solve")   # profile slots after the kernel classes
+MLP_NPARAMS = 4545
 
 
 def check(lib, rc, allow=()):

@@ -9,10 +9,13 @@
 
 using dfsph::DfsphException;
 using dfsph::EngineBase;
+using dfsph::MlpView;
+using dfsph::mlp_view;
 
 struct dfsph_ctx {
   EngineBase *engine;
   int device;
+  dfsph_mlp *mlp = nullptr;  // learned warm-start model in use (not owned)
 };
 
 namespace {
@@ -132,6 +135,10 @@ int dfsph_reset(dfsph_ctx *ctx) {
 int dfsph_step(dfsph_ctx *ctx, int32_t nsteps, dfsph_step_stats *stats) {
   return guard([&] {
     valid(ctx);
+    if (ctx->mlp) {
+      const MlpView v = mlp_view(ctx->mlp);  // the model's current weights and normalisation
+      ctx->engine->set_warmstart_model(&v);
+    }
     const int rc = ctx->engine->step(nsteps, stats);
     if (rc == DFSPH_ERR_NOT_CONVERGED) g_last_error = "a solve reached its iteration cap";
     return rc;
@@ -305,9 +312,10 @@ int dfsph_profile_read(dfsph_ctx *ctx, int32_t kernel_class, int64_t *launches, 
 }
 
 const char *dfsph_kernel_class_name(int32_t k) {
-  static const char *names[DFSPH_K_COUNT] = {"sort", "lists_density_factor", "bf_lists", "density_pass",
-                                             "velocity_pass", "xsph_advect", "integrate", "pairs", "rigid"};
-  return (k >= 0 && k < DFSPH_K_COUNT) ? names[k] : "";
+  static const char *names[DFSPH_PROFILE_COUNT] = {
+      "sort",        "lists_density_factor", "bf_lists", "density_pass", "velocity_pass",    "xsph_advect",
+      "integrate",   "pairs",                "rigid",    "mlp",          "divergence_solve", "pressure_solve"};
+  return (k >= 0 && k < DFSPH_PROFILE_COUNT) ? names[k] : "";
 }
 
 int dfsph_set_time(dfsph_ctx *ctx, double t, int64_t step_count) {
@@ -342,6 +350,42 @@ int dfsph_checkpoint_free(dfsph_ctx *ctx, int32_t slot) {
 
 int dfsph_adjoint_sweep(dfsph_ctx *ctx, const double *lam_in, double *lam_out) {
   return guard([&] { valid(ctx); ctx->engine->adjoint_sweep(lam_in, lam_out); return DFSPH_OK; });
+}
+
+int dfsph_set_warmstart_model(dfsph_ctx *ctx, dfsph_mlp *m) {
+  return guard([&] {
+    valid(ctx);
+    if (m) {
+      const MlpView v = mlp_view(m);
+      ctx->engine->set_warmstart_model(&v);
+    } else {
+      ctx->engine->set_warmstart_model(nullptr);
+    }
+    ctx->mlp = m;
+    return DFSPH_OK;
+  });
+}
+
+int dfsph_ml_record(dfsph_ctx *ctx, int32_t on) {
+  return guard([&] { valid(ctx); ctx->engine->ml_record(on != 0); return DFSPH_OK; });
+}
+
+int dfsph_ml_capture(dfsph_ctx *ctx, float *x, float *y, int64_t capacity, int64_t *count) {
+  return guard([&] {
+    valid(ctx);
+    if (!x || !y || !count) throw DfsphException(DFSPH_ERR_INVALID_ARG, "NULL argument");
+    if (capacity < 0) throw DfsphException(DFSPH_ERR_INVALID_ARG, "capacity < 0");
+    cudaPointerAttributes a;
+    for (const void *p : {(const void *)x, (const void *)y}) {
+      if (cudaPointerGetAttributes(&a, p) != cudaSuccess ||
+          (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged)) {
+        cudaGetLastError();
+        throw DfsphException(DFSPH_ERR_INVALID_ARG, "x and y must be device pointers");
+      }
+    }
+    *count = ctx->engine->ml_capture(x, y, capacity);
+    return DFSPH_OK;
+  });
 }
 
 }  // extern "C"

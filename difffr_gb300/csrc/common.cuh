@@ -15,6 +15,7 @@ enum : int {
   ERR_BOUNDARY_LIST_OVERFLOW = 1 << 1,
   ERR_BF_LIST_OVERFLOW = 1 << 2,
   ERR_NONFINITE_POSITION = 1 << 3,
+  ERR_MLP_TIMEOUT = 1 << 4,
 };
 
 template <class T>

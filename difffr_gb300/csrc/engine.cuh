@@ -17,6 +17,7 @@
 #include "common.cuh"
 #include "kernels_fluid.cuh"
 #include "kernels_rigid.cuh"
+#include "kernels_mlp.cuh"
 
 namespace dfsph {
 
@@ -111,6 +112,50 @@ struct Scanner {
   }
 };
 
+// ----------------------------------------------------------------- learned warm start glue
+// Inference IO inside the pressure warm start: features from F, prediction only where
+// rho_adv > 1 (feature x > 0, the same gate as the reference warm start); the result is
+// the stiffness of the warm-start velocity correction (Q.w) and the start of the
+// solver's stiffness accumulator.
+template <class T>
+struct MlpWarmIO {
+  const float4 *F;
+  V4<T> *Q;
+  T *kappa;
+  __device__ bool load(int i, float f[4]) const {
+    const float4 v = F[i];
+    f[0] = v.x; f[1] = v.y; f[2] = v.z; f[3] = v.w;
+    return v.x > 0.f;
+  }
+  __device__ void store(int i, float y) const {
+    Q[i].w = (T)y;
+    kappa[i] = (T)y;
+  }
+};
+
+// the step's accumulated pressure stiffness (pass units) before the end-of-step scaling
+template <class T>
+static __global__ void k_ml_target(int n, const T *__restrict__ kappa, float *__restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (float)kappa[i];
+}
+static __global__ void k_ml_flags(int n, const float4 *__restrict__ F, int *__restrict__ flag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) flag[i] = F[i].x > 0.f ? 1 : 0;
+}
+static __global__ void k_ml_scatter(int n, const float4 *__restrict__ F, const float *__restrict__ kfin,
+                                    const int *__restrict__ pos, int64_t cap, float *__restrict__ x,
+                                    float *__restrict__ y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 f = F[i];
+  if (!(f.x > 0.f)) return;
+  const int64_t k = pos[i];
+  if (k >= cap) return;
+  reinterpret_cast<float4 *>(x)[k] = f;
+  y[k] = kfin[i];
+}
+
 // ----------------------------------------------------------------- engine
 template <class T>
 class Engine : public EngineBase {
@@ -149,6 +194,9 @@ class Engine : public EngineBase {
   void checkpoint_restore(int slot) override;
   void checkpoint_free(int slot) override;
   void adjoint_sweep(const double *lam_in, double *lam_out) override;
+  void set_warmstart_model(const MlpView *v) override;
+  void ml_record(bool on) override;
+  int64_t ml_capture(float *x, float *y, int64_t cap) override;
 
  private:
   // configuration
@@ -207,6 +255,15 @@ class Engine : public EngineBase {
     std::vector<int> anim;
   };
   std::vector<std::unique_ptr<Snap>> snaps_;
+  // learned warm start: features at the pressure warm start, the step's final stiffness,
+  // capture flags, and the model view
+  bool ml_record_ = false, ml_on_ = false;
+  MlpView mlv_;
+  DBuf<float4> F_;
+  DBuf<float> kfin_;
+  DBuf<int> mlflag_;
+  Scanner mlscan_;
+  int num_sms_ = 152;
   // adjoint tape
   DBuf<double> tape_;
   int64_t tape_len_ = 0, tape_cap_ = 0;
@@ -226,9 +283,9 @@ class Engine : public EngineBase {
   std::vector<ProfRec> pending_;
   std::vector<cudaEvent_t> pool_;
   cudaEvent_t open_ev_ = nullptr;
-  int64_t prof_launches_[DFSPH_K_COUNT] = {};
-  double prof_ms_[DFSPH_K_COUNT] = {};
-  int64_t prof_units_[DFSPH_K_COUNT] = {};
+  int64_t prof_launches_[DFSPH_PROFILE_COUNT] = {};
+  double prof_ms_[DFSPH_PROFILE_COUNT] = {};
+  int64_t prof_units_[DFSPH_PROFILE_COUNT] = {};
   cudaEvent_t take_event() {
     if (pool_.empty()) { cudaEvent_t e; DF_CK(cudaEventCreate(&e)); return e; }
     cudaEvent_t e = pool_.back(); pool_.pop_back(); return e;
@@ -246,6 +303,19 @@ class Engine : public EngineBase {
     open_ev_ = nullptr;
   }
   void resolve_profile();
+  // phase timers (a whole solve); independent of the per-launch pair above
+  cudaEvent_t phase_begin() {
+    if (!prof_on_) return nullptr;
+    cudaEvent_t e = take_event();
+    DF_CK(cudaEventRecord(e, stream_));
+    return e;
+  }
+  void phase_end(int k, cudaEvent_t a, int64_t units) {
+    if (!prof_on_ || !a) return;
+    cudaEvent_t b = take_event();
+    DF_CK(cudaEventRecord(b, stream_));
+    pending_.push_back({k, a, b, units});
+  }
 
   int blocks(int n, int t = 256) const { return (n + t - 1) / t; }
   void launched(int k = 1) { launches_ += k; }
@@ -257,7 +327,10 @@ class Engine : public EngineBase {
   void compute_psi();
   void begin_step();
   void solve(bool pressure);
-  void launch_density(int mode, T *kappa_io, bool partials);
+  void solve_impl(bool pressure);
+  void launch_density(int mode, T *kappa_io, bool partials, float4 *feat = nullptr);
+  void launch_mlp_warmstart(T *kap);
+  void ml_buffers();
   void launch_velocity(T *kappa_acc);
   void launch_pairs(bool pressure, bool warm, bool grad);
   void rigid_end();

@@ -8,6 +8,7 @@
 #include <string>
 
 #include "../../include/dfsph.h"
+#include "mlp_view.h"
 
 namespace dfsph {
 
@@ -59,6 +60,9 @@ class EngineBase {
   virtual void checkpoint_restore(int slot) = 0;
   virtual void checkpoint_free(int slot) = 0;
   virtual void adjoint_sweep(const double *lam_in, double *lam_out) = 0;
+  virtual void set_warmstart_model(const MlpView *v) = 0;
+  virtual void ml_record(bool on) = 0;
+  virtual int64_t ml_capture(float *x, float *y, int64_t cap) = 0;
 };
 
 EngineBase *make_engine_fp32(const dfsph_scene *sc);

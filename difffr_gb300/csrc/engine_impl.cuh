@@ -197,6 +197,11 @@ Engine<T>::Engine(const dfsph_scene *sc) {
   ncell_ = fc_.grid.nx * fc_.grid.ny * fc_.grid.nz;
 
   DF_CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  {
+    int dev = 0;
+    DF_CK(cudaGetDevice(&dev));
+    DF_CK(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, dev));
+  }
   scan_.prepare((size_t)ncell_ + 1);
 
   // ---- fluid buffers
@@ -465,18 +470,19 @@ void Engine<T>::check_error_word() {
     if (e & ERR_BOUNDARY_LIST_OVERFLOW) m += " boundary neighbour list overflow (raise max_boundary_neighbors);";
     if (e & ERR_BF_LIST_OVERFLOW) m += " dynamic-boundary fluid list overflow;";
     if (e & ERR_NONFINITE_POSITION) m += " non-finite particle position;";
+    if (e & ERR_MLP_TIMEOUT) m += " tensor-core wait timed out in the warm-start model;";
     throw DfsphException(DFSPH_ERR_DEVICE, m);
   }
 }
 
 template <class T>
-void Engine<T>::launch_density(int mode, T *kappa_io, bool partials) {
+void Engine<T>::launch_density(int mode, T *kappa_io, bool partials, float4 *feat) {
   const int nbk = blocks(n_ * LPP);
   double *pp = partials ? partials_.p : nullptr;
   pbegin();
 #define DF_DENS(M)                                                                                                \
   k_density_pass<T, M><<<nbk, 256, 0, stream_>>>(fc_, R_[cur_].p, Q_.p, BR_.p, flist_.p, fcount_.p, blist_.p,           \
-                                                 bcount_.p, rho_.p, alpha_.p, rhoAdv_.p, kappa_io, pp)
+                                                 bcount_.p, rho_.p, alpha_.p, rhoAdv_.p, kappa_io, pp, feat)
   switch (mode) {
     case PASS_PRESSURE: DF_DENS(PASS_PRESSURE); break;
     case PASS_DIVERGENCE: DF_DENS(PASS_DIVERGENCE); break;
@@ -525,12 +531,21 @@ void Engine<T>::launch_pairs(bool pressure, bool warm, bool grad) {
 // error is below eta (after at least min iterations) or max iterations are reached.
 template <class T>
 void Engine<T>::solve(bool pressure) {
+  cudaEvent_t ph = phase_begin();
+  solve_impl(pressure);
+  phase_end(pressure ? DFSPH_PHASE_PRESSURE_SOLVE : DFSPH_PHASE_DIVERGENCE_SOLVE, ph, n_);
+}
+
+template <class T>
+void Engine<T>::solve_impl(bool pressure) {
   const bool warm = pressure ? P_.use_pressure_warmstart : P_.use_divergence_warmstart;
   T *kap = pressure ? kappa_[cur_].p : kappaV_[cur_].p;
   const int wm = pressure ? PASS_PRESSURE_WARM : PASS_DIVERGENCE_WARM;
   const int im = pressure ? PASS_PRESSURE : PASS_DIVERGENCE;
   if (warm) {
-    launch_density(wm, kap, false);
+    const bool ml = pressure && (ml_record_ || ml_on_);
+    launch_density(wm, kap, false, ml ? F_.p : nullptr);
+    if (pressure && ml_on_) launch_mlp_warmstart(kap);
     launch_pairs(pressure, true, false);
     launch_velocity(nullptr);
   }
@@ -631,6 +646,10 @@ int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
       // the advected state lives in the other record buffer: swap the record pair only
       std::swap(R_[cur_].p, R_[nv].p);
       solve(true);
+      if (ml_record_ && P_.use_pressure_warmstart) {
+        k_ml_target<T><<<blocks(n_), 256, 0, stream_>>>(n_, kappa_[cur_].p, kfin_.p);
+        launched();
+      }
       pbegin();
       k_integrate<T><<<blocks(n_), 256, 0, stream_>>>(fc_, R_[cur_].p, kappa_[cur_].p,
                                                       P_.use_pressure_warmstart ? 1 : 0);
@@ -922,12 +941,12 @@ void Engine<T>::resolve_profile() {
 template <class T>
 void Engine<T>::profile_enable(bool on) {
   resolve_profile();
-  for (int k = 0; k < DFSPH_K_COUNT; k++) { prof_launches_[k] = 0; prof_ms_[k] = 0; prof_units_[k] = 0; }
+  for (int k = 0; k < DFSPH_PROFILE_COUNT; k++) { prof_launches_[k] = 0; prof_ms_[k] = 0; prof_units_[k] = 0; }
   prof_on_ = on;
 }
 template <class T>
 void Engine<T>::profile_read(int k, int64_t *launches, double *ms, int64_t *units) {
-  if (k < 0 || k >= DFSPH_K_COUNT) throw DfsphException(DFSPH_ERR_INVALID_ARG, "kernel class");
+  if (k < 0 || k >= DFSPH_PROFILE_COUNT) throw DfsphException(DFSPH_ERR_INVALID_ARG, "kernel class or phase");
   resolve_profile();
   if (launches) *launches = prof_launches_[k];
   if (ms) *ms = prof_ms_[k];
@@ -1030,5 +1049,70 @@ void Engine<T>::adjoint_sweep(const double *lam_in, double *lam_out) {
   check_launch();
   DF_CK(cudaMemcpyAsync(lam_out, lo.p, (size_t)NSTATE * nb_ * sizeof(double), cudaMemcpyDeviceToHost, stream_));
   DF_CK(cudaStreamSynchronize(stream_));
+}
+// ----------------------------------------------------------------- learned warm start
+template <class T>
+void Engine<T>::ml_buffers() {
+  if (F_.n >= (size_t)std::max(n_, 1)) return;
+  const size_t N = std::max(n_, 1);
+  F_.alloc(N);
+  kfin_.alloc(N);
+  mlflag_.alloc(N);
+  mlscan_.prepare(N);
+  DF_CK(cudaMemsetAsync(F_.p, 0, N * sizeof(float4), stream_));
+  DF_CK(cudaMemsetAsync(kfin_.p, 0, N * sizeof(float), stream_));
+}
+
+template <class T>
+void Engine<T>::set_warmstart_model(const MlpView *v) {
+  if (!v) { ml_on_ = false; return; }
+  int dev = 0;
+  DF_CK(cudaGetDevice(&dev));
+  if (v->device != dev) throw DfsphException(DFSPH_ERR_INVALID_ARG, "model and context live on different devices");
+  if (!P_.use_pressure_warmstart)
+    throw DfsphException(DFSPH_ERR_STATE, "the learned warm start needs use_pressure_warmstart");
+  ml_buffers();
+  mlv_ = *v;
+  ml_on_ = true;
+}
+
+template <class T>
+void Engine<T>::ml_record(bool on) {
+  if (on && !P_.use_pressure_warmstart)
+    throw DfsphException(DFSPH_ERR_STATE, "recording warm-start samples needs use_pressure_warmstart");
+  if (on) ml_buffers();
+  ml_record_ = on;
+}
+
+// inference inside the pressure warm start: kappa_warm = MLP(features) where rho_adv > 1
+template <class T>
+void Engine<T>::launch_mlp_warmstart(T *kap) {
+  if (n_ == 0) return;
+  pbegin();
+  const int ntiles = (n_ + MLP_TILE - 1) / MLP_TILE;
+  const int grid = std::min(ntiles, num_sms_ * 7);
+  k_mlp_infer<MlpWarmIO<T>><<<grid, MLP_THREADS, MLP_INFER_SMEM, stream_>>>(mlv_, MlpWarmIO<T>{F_.p, Q_.p, kap}, n_,
+                                                                           err_.p, ERR_MLP_TIMEOUT);
+  launched();
+  pend(DFSPH_K_MLP, n_);
+}
+
+template <class T>
+int64_t Engine<T>::ml_capture(float *x, float *y, int64_t cap) {
+  if (!ml_record_ || F_.n == 0) throw DfsphException(DFSPH_ERR_STATE, "recording is off");
+  if (n_ == 0) return 0;
+  k_ml_flags<<<blocks(n_), 256, 0, stream_>>>(n_, F_.p, mlflag_.p);
+  launched();
+  int last_flag = 0, last_scan = 0;
+  DF_CK(cudaMemcpyAsync(&last_flag, mlflag_.p + n_ - 1, sizeof(int), cudaMemcpyDeviceToHost, stream_));
+  int64_t ls = 0;
+  mlscan_.run(mlflag_.p, n_, stream_, ls);
+  launches_ += ls;
+  DF_CK(cudaMemcpyAsync(&last_scan, mlflag_.p + n_ - 1, sizeof(int), cudaMemcpyDeviceToHost, stream_));
+  k_ml_scatter<<<blocks(n_), 256, 0, stream_>>>(n_, F_.p, kfin_.p, mlflag_.p, cap, x, y);
+  launched();
+  check_launch();
+  DF_CK(cudaStreamSynchronize(stream_));
+  return std::min<int64_t>((int64_t)last_scan + last_flag, cap);
 }
 }  // namespace dfsph

@@ -326,7 +326,7 @@ static __global__ void __launch_bounds__(256) k_density_pass(
     FluidConsts<T> c, const Rec<T> *__restrict__ R, V4<T> *__restrict__ Q, const Rec<T> *__restrict__ BR,
     const int *__restrict__ flist, const int *__restrict__ fcount, const int *__restrict__ blist,
     const int *__restrict__ bcount, const T *__restrict__ rho, const T *__restrict__ alpha, T *__restrict__ rhoAdv,
-    T *__restrict__ kappa_io, double *__restrict__ partials) {
+    T *__restrict__ kappa_io, double *__restrict__ partials, float4 *__restrict__ feat) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = t / LPP, s = t % LPP;
   const bool live = i < c.n;
@@ -372,6 +372,11 @@ static __global__ void __launch_bounds__(256) k_density_pass(
       const T kp = kappa_io[i];
       kq = (ra > T(1)) ? T(0.5) * (kp > T(-0.00025) ? kp : T(-0.00025)) * c.invH2 : T(0);
       kappa_io[i] = kq;
+      // learned warm start: its features (density error, neighbour count, previous
+      // stiffness in pass units, speed)
+      if (feat)
+        feat[i] = make_float4((float)(ra - T(1)), (float)(nf + nb), (float)(kp * c.invH2),
+                              (float)sqrt(ri.v.x * ri.v.x + ri.v.y * ri.v.y + ri.v.z * ri.v.z));
     } else {
       const T kp = kappa_io[i];
       kq = (ra > T(0)) ? T(0.5) * (kp > T(-0.5) ? kp : T(-0.5)) * c.invH : T(0);

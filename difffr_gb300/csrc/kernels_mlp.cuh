@@ -1,0 +1,543 @@
+// kernels_mlp.cuh — the learned warm start for the DFSPH pressure stiffness: a per-particle
+// MLP 4 -> 64 -> 64 -> 1 with GELU activations, BF16 weights and FP32 accumulation.
+//
+// The 64 x 64 hidden layer (the only dense contraction of the project) runs on the
+// tensor cores: tcgen05.mma with BF16 operands staged in shared memory and FP32
+// accumulators in TMEM, for the forward product and, in training, for the input
+// gradient and for all weight gradients (bias gradients come out of the same products
+// through a constant-1 column). The 4-wide input layer and the 64-wide output layer are
+// per-thread FP32 arithmetic on BF16-rounded weights.
+//
+// Features (per particle, at the pressure warm start): the density error rho_adv - 1,
+// the neighbour count, the previous step's stiffness kappa (in Jacobi-pass units) and
+// |v|. The target is the stiffness the plain solve accumulated in that step. Features
+// and target are normalised with per-column mean and standard deviation.
+//
+// No reference counterpart: the reference warm start is
+// TimeStepDiffDFSPH::warmstartPressureSolve (TimeStepDiffDFSPH.cpp:964-1059),
+// kappa <- 0.5 max(kappa, -0.00025) / h^2, which is what the learned start replaces.
+#pragma once
+#include <cuda_bf16.h>
+
+#include <cstdint>
+
+#include "mlp_view.h"
+#include "tc.cuh"
+
+namespace dfsph {
+
+constexpr int MLP_TILE = 128;                            // particles per MMA tile (M = 128)
+constexpr int MLP_THREADS = 128;
+constexpr uint32_t MLP_WAIT_LIMIT = 1u << 21;            // mbarrier polls (x 64 ns sleep) before giving up
+
+static __device__ __forceinline__ float gelu_d(float x, float &d) {
+  // tanh form: 0.5 x (1 + tanh(c (x + a x^3)))
+  const float c = 0.7978845608028654f, a = 0.044715f;
+  const float x2 = x * x;
+  const float u = c * (x + a * x2 * x);
+  const float t = tanhf(u);
+  d = 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * c * (1.0f + 3.0f * a * x2);
+  return 0.5f * x * (1.0f + t);
+}
+static __device__ __forceinline__ float gelu_f(float x) {
+  float d;
+  return gelu_d(x, d);
+}
+
+static __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+  const uint32_t l = __bfloat16_as_ushort(__float2bfloat16_rn(lo));
+  const uint32_t h = __bfloat16_as_ushort(__float2bfloat16_rn(hi));
+  return l | (h << 16);
+}
+// store 8 consecutive columns (c0 multiple of 8) of row `row` of a core-matrix tile
+static __device__ __forceinline__ void st_row8(uint8_t *tile, int row, int c0, int cols, const float *v) {
+  uint4 q;
+  q.x = pack_bf16x2(v[0], v[1]);
+  q.y = pack_bf16x2(v[2], v[3]);
+  q.z = pack_bf16x2(v[4], v[5]);
+  q.w = pack_bf16x2(v[6], v[7]);
+  *reinterpret_cast<uint4 *>(tile + tc::cm_offset(row, c0, cols)) = q;
+}
+
+static __device__ __forceinline__ uint8_t *align1024(uint8_t *p) {
+  return reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
+}
+
+// Small weights in shared memory: W1 (256), b1 (64), b2 (64), w3 (64), b3 (1).
+constexpr int MLP_SW_W1 = 0, MLP_SW_B1 = 256, MLP_SW_B2 = 320, MLP_SW_W3 = 384, MLP_SW_B3 = 448, MLP_SW_N = 452;
+
+static __device__ __forceinline__ void mlp_stage_small(const float *wuse, float *sw) {
+  for (int k = threadIdx.x; k < MLP_SW_N; k += blockDim.x) {
+    float v = 0.f;
+    if (k < MLP_SW_B2) v = wuse[k];                                  // W1, b1
+    else if (k < MLP_SW_W3) v = wuse[MLP_OFF_B2 + (k - MLP_SW_B2)];  // b2
+    else if (k < MLP_SW_B3) v = wuse[MLP_OFF_W3 + (k - MLP_SW_W3)];  // w3
+    else if (k == MLP_SW_B3) v = wuse[MLP_OFF_B3];
+    sw[k] = v;
+  }
+}
+
+// hidden layer 1 for one particle: h1 (64, to the tile row as BF16) and optionally
+// gelu'(z1) into g1d
+template <bool DERIV>
+static __device__ __forceinline__ void mlp_layer1(const float *sw, const float f[4], uint8_t *tile, int row, int cols,
+                                                  float *g1d) {
+#pragma unroll
+  for (int c = 0; c < MLP_H; c += 8) {
+    float h[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      const int j = c + u;
+      const float *w = sw + MLP_SW_W1 + 4 * j;
+      const float z = sw[MLP_SW_B1 + j] + w[0] * f[0] + w[1] * f[1] + w[2] * f[2] + w[3] * f[3];
+      if (DERIV) {
+        float d;
+        h[u] = gelu_d(z, d);
+        g1d[j] = d;
+      } else {
+        h[u] = gelu_f(z);
+      }
+    }
+    st_row8(tile, row, c, cols, h);
+  }
+}
+
+// ------------------------------------------------------------------ inference
+// Persistent over tiles of 128 particles: one thread per particle row. Shared memory:
+// W2 image 8 KB, the H1 tile 16 KB, small weights, one mbarrier; TMEM: 64 columns.
+// IO supplies `bool load(int i, float f[4])` (false: no prediction wanted for i) and
+// `void store(int i, float y)`.
+constexpr int MLP_INFER_SMEM = 32 * 1024;  // also caps residency at 7 CTAs per SM (7 x 64 TMEM columns)
+
+template <class IO>
+static __global__ void __launch_bounds__(MLP_THREADS) k_mlp_infer(MlpView mv, IO io, int n, int *err, int errbit) {
+  extern __shared__ uint8_t mlp_smem_raw[];
+  uint8_t *base = align1024(mlp_smem_raw);
+  uint8_t *sW2 = base;                   // 8192 B
+  uint8_t *sH1 = base + 8192;            // 16384 B: 128 rows x 64 cols
+  float *sw = reinterpret_cast<float *>(base + 8192 + 16384);
+  uint64_t *bar = reinterpret_cast<uint64_t *>(sw + MLP_SW_N);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5;
+
+  for (int k = tid; k < 8192 / 16; k += MLP_THREADS)
+    reinterpret_cast<uint4 *>(sW2)[k] = reinterpret_cast<const uint4 *>(mv.w2img)[k];
+  mlp_stage_small(mv.wuse, sw);
+  if (tid == 0) {
+    tc::mbar_init(bar, 1);
+    tc::fence_mbar_init();
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(tslot, 64);
+    tc::tmem_relinquish();
+  }
+  tc::fence_async_smem();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  const uint32_t idesc = tc::idesc_bf16(128, 64, 0, 0);
+  const uint32_t aBase = tc::smem_u32(sH1), bBase = tc::smem_u32(sW2);
+  float xm[4], xi[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) { xm[k] = mv.norm[k]; xi[k] = 1.0f / mv.norm[4 + k]; }
+  const float ym = mv.norm[8], ys = mv.norm[9];
+  const int ntiles = (n + MLP_TILE - 1) / MLP_TILE;
+  uint32_t phase = 0;
+  bool pending = false;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int i = tile * MLP_TILE + tid;
+    float f[4] = {0.f, 0.f, 0.f, 0.f};
+    bool want = false;
+    if (i < n) want = io.load(i, f);
+#pragma unroll
+    for (int k = 0; k < 4; k++) f[k] = (f[k] - xm[k]) * xi[k];
+    mlp_layer1<false>(sw, f, sH1, tid, 64, nullptr);
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+#pragma unroll
+      for (int s = 0; s < 4; s++)
+        tc::mma_bf16(tmem, tc::sdesc(aBase + 256u * s, 128, 1024), tc::sdesc(bBase + 256u * s, 128, 1024), idesc,
+                     s > 0 ? 1u : 0u);
+      tc::mma_commit(bar);
+    }
+    pending = true;
+    bool ok = tc::mbar_wait(bar, phase, MLP_WAIT_LIMIT);
+    ok = __syncthreads_and(ok) != 0;
+    if (!ok) break;
+    pending = false;
+    phase ^= 1u;
+    tc::fence_after_sync();
+    float out = sw[MLP_SW_B3];
+#pragma unroll
+    for (int c = 0; c < 64; c += 16) {
+      float z[16];
+      tc::tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c, z);
+      tc::tmem_wait_ld();
+#pragma unroll
+      for (int u = 0; u < 16; u++) out += sw[MLP_SW_W3 + c + u] * gelu_f(z[u] + sw[MLP_SW_B2 + c + u]);
+    }
+    if (want) io.store(i, out * ys + ym);
+    tc::fence_before_sync();
+  }
+  if (pending) {
+    // an MMA may still be in flight: record the failure, give it a bounded wait, then free TMEM
+    if (tid == 0) atomicOr(err, errbit);
+    tc::mbar_wait(bar, phase, MLP_WAIT_LIMIT);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (warp == 0) tc::tmem_dealloc(tmem, 64);
+}
+
+// Plain device arrays: x[n][4] -> y[n].
+struct MlpArrayIO {
+  const float *x;
+  float *y;
+  __device__ bool load(int i, float f[4]) const {
+    const float4 v = reinterpret_cast<const float4 *>(x)[i];
+    f[0] = v.x; f[1] = v.y; f[2] = v.z; f[3] = v.w;
+    return true;
+  }
+  __device__ void store(int i, float v) const { y[i] = v; }
+};
+
+// ------------------------------------------------------------------ training
+// One CTA per SM, persistent over the batch's tiles. Per tile (thread p = particle row):
+//   forward:   z1 = W1 f + b1, h1 = gelu(z1)           (per thread, FP32)
+//              Z2 = H1 W2^T                             (MMA1, M=128 N=64 K=64)
+//              h2 = gelu(z2 + b2), y = w3 . h2 + b3     (per thread)
+//   backward:  e = y - target, dz2 = e w3 gelu'(z2)
+//              DH1 = DZ2 W2                             (MMA2, M=128 N=64 K=64)
+//              GW2 += DZ2^T [H1 | 1]                    (MMA3, M=128 N=80 K=128: dW2 and db2)
+//              GW3 += [H2 | 1]^T e                      (MMA5, M=128 N=16 K=128: dw3 and db3)
+//              dz1 = dh1 gelu'(z1)
+//              GW1 += DZ1^T [F | 1]                     (MMA4, M=128 N=16 K=128: dW1 and db1)
+// The weight-gradient products read the per-particle tiles as MN-major operands, so every
+// thread writes only its own row. Rows 64..127 of the M dimension are zero padding
+// (M = 128 keeps row r of D in TMEM lane r). At the end the CTA writes its gradient
+// partial sums (unscaled) and its loss partial; k_mlp_adam reduces them in fixed order.
+namespace mlptrain {
+constexpr int SW2 = 0;                      // W2 image, 64 x 64
+constexpr int SH1 = SW2 + 8192;             // 128 x 80  (col 64 = 1)
+constexpr int SDZ2 = SH1 + 128 * 80 * 2;    // 128 x 128 (cols 64.. = 0)
+constexpr int SH2 = SDZ2 + 128 * 128 * 2;   // 128 x 128 (col 64 = 1)
+constexpr int SDZ1 = SH2 + 128 * 128 * 2;   // 128 x 128 (cols 64.. = 0)
+constexpr int SFX = SDZ1 + 128 * 128 * 2;   // 128 x 16  (cols 0..3 features, col 4 = 1)
+constexpr int SDO = SFX + 128 * 16 * 2;     // 128 x 16  (col 0 = error)
+constexpr int SSW = SDO + 128 * 16 * 2;     // small weights
+constexpr int SBAR = SSW + MLP_SW_N * 4;    // mbarrier
+constexpr int SEND = SBAR + 16;
+// The dynamic allocation is padded far beyond SEND so that every operand read of every
+// MMA stays inside it even if the descriptor's two byte offsets were read the other way
+// round (largest such read: a 128-column tile read with 2048-B M/N stride from SDZ1).
+constexpr int SMEM = 225 * 1024;
+static_assert(SDZ1 + 15 * 2048 + 7 * 4096 + 128 * 2 + 128 < SMEM - 1024, "operand reads stay in the allocation");
+static_assert(SEND < SMEM - 1024, "layout fits");
+// TMEM columns
+constexpr uint32_t TZ2 = 0, TDH1 = 64, TGW2 = 128, TGW1 = 208, TGW3 = 224, TCOLS = 256;
+}  // namespace mlptrain
+
+static __global__ void __launch_bounds__(MLP_THREADS, 1)
+    k_mlp_train(MlpView mv, const float *__restrict__ x, const float *__restrict__ y, const int *__restrict__ idx, int n,
+                int nsrc, float *__restrict__ gpart, double *__restrict__ lpart, int *err) {
+  using namespace mlptrain;
+  extern __shared__ uint8_t mlp_smem_raw[];
+  uint8_t *base = align1024(mlp_smem_raw);
+  float *sw = reinterpret_cast<float *>(base + SSW);
+  uint64_t *bar = reinterpret_cast<uint64_t *>(base + SBAR);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(base + SBAR + 8);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  // constant parts of the tiles: zeros, and the constant-1 columns
+  for (int k = tid; k < (SSW - SH1) / 16; k += MLP_THREADS) reinterpret_cast<uint4 *>(base + SH1)[k] = make_uint4(0, 0, 0, 0);
+  for (int k = tid; k < 8192 / 16; k += MLP_THREADS)
+    reinterpret_cast<uint4 *>(base + SW2)[k] = reinterpret_cast<const uint4 *>(mv.w2img)[k];
+  mlp_stage_small(mv.wuse, sw);
+  __syncthreads();
+  {
+    const uint16_t one = __bfloat16_as_ushort(__float2bfloat16_rn(1.0f));
+    *reinterpret_cast<uint16_t *>(base + SH1 + tc::cm_offset(tid, 64, 80)) = one;
+    *reinterpret_cast<uint16_t *>(base + SH2 + tc::cm_offset(tid, 64, 128)) = one;
+    *reinterpret_cast<uint16_t *>(base + SFX + tc::cm_offset(tid, 4, 16)) = one;
+  }
+  if (tid == 0) {
+    tc::mbar_init(bar, 1);
+    tc::fence_mbar_init();
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(tslot, TCOLS);
+    tc::tmem_relinquish();
+  }
+  tc::fence_async_smem();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  const uint32_t lane_off = (uint32_t)(32 * warp) << 16;
+  const uint32_t sb = tc::smem_u32(base);
+  float xm[4], xi[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) { xm[k] = mv.norm[k]; xi[k] = 1.0f / mv.norm[4 + k]; }
+  const float ym = mv.norm[8], yi = 1.0f / mv.norm[9];
+
+  const int ntiles = (n + MLP_TILE - 1) / MLP_TILE;
+  uint32_t phase = 0;
+  bool pending = false, failed = false;
+  int it = 0;
+  double loss = 0.0;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+    const int r = tile * MLP_TILE + tid;
+    bool valid = r < n;
+    float f[4] = {0.f, 0.f, 0.f, 0.f}, yn = 0.f;
+    int s = r;
+    if (valid && idx) {
+      s = idx[r];
+      if (s < 0 || s >= nsrc) {  // an index outside the sample arrays: flag it, skip the sample
+        atomicOr(err, 2);
+        valid = false;
+      }
+    }
+    if (valid) {
+      const float4 v = reinterpret_cast<const float4 *>(x)[s];
+      f[0] = (v.x - xm[0]) * xi[0]; f[1] = (v.y - xm[1]) * xi[1];
+      f[2] = (v.z - xm[2]) * xi[2]; f[3] = (v.w - xm[3]) * xi[3];
+      yn = (y[s] - ym) * yi;
+    }
+    float g1d[MLP_H];
+    mlp_layer1<true>(sw, f, base + SH1, tid, 80, g1d);
+    {
+      const float fr[8] = {f[0], f[1], f[2], f[3], 1.0f, 0.f, 0.f, 0.f};
+      st_row8(base + SFX, tid, 0, 16, fr);
+    }
+    // ---- MMA1: Z2 = H1 W2^T
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      const uint32_t id1 = tc::idesc_bf16(128, 64, 0, 0);
+#pragma unroll
+      for (int s = 0; s < 4; s++)
+        tc::mma_bf16(tmem + TZ2, tc::sdesc(sb + SH1 + 256u * s, 128, 1280), tc::sdesc(sb + SW2 + 256u * s, 128, 1024),
+                     id1, s > 0 ? 1u : 0u);
+      tc::mma_commit(bar);
+    }
+    pending = true;
+    if (!__syncthreads_and(tc::mbar_wait(bar, phase, MLP_WAIT_LIMIT))) { failed = true; break; }
+    pending = false;
+    phase ^= 1u;
+    tc::fence_after_sync();
+    // ---- output layer, error, dz2
+    float z2[MLP_H];
+#pragma unroll
+    for (int c = 0; c < MLP_H; c += 16) {
+      float t[16];
+      tc::tmem_ld16(tmem + lane_off + TZ2 + (uint32_t)c, t);
+      tc::tmem_wait_ld();
+#pragma unroll
+      for (int u = 0; u < 16; u++) z2[c + u] = t[u];
+    }
+    float out = sw[MLP_SW_B3];
+#pragma unroll
+    for (int c = 0; c < MLP_H; c += 8) {
+      float h[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        float d;
+        h[u] = gelu_d(z2[c + u] + sw[MLP_SW_B2 + c + u], d);
+        out += sw[MLP_SW_W3 + c + u] * h[u];
+        z2[c + u] = d;  // keep gelu'(z2)
+      }
+      st_row8(base + SH2, tid, c, 128, h);
+    }
+    const float e = valid ? out - yn : 0.f;
+    loss += (double)e * (double)e;
+    {
+      const float er[8] = {e, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      st_row8(base + SDO, tid, 0, 16, er);
+    }
+#pragma unroll
+    for (int c = 0; c < MLP_H; c += 8) {
+      float d[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) d[u] = e * sw[MLP_SW_W3 + c + u] * z2[c + u];
+      st_row8(base + SDZ2, tid, c, 128, d);
+    }
+    // ---- MMA2 (DH1 = DZ2 W2), MMA3 (GW2 += DZ2^T [H1|1]), MMA5 (GW3 += [H2|1]^T e)
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      const uint32_t id2 = tc::idesc_bf16(128, 64, 0, 1);
+#pragma unroll
+      for (int s = 0; s < 4; s++)
+        tc::mma_bf16(tmem + TDH1, tc::sdesc(sb + SDZ2 + 256u * s, 128, 2048),
+                     tc::sdesc(sb + SW2 + 2048u * s, 1024, 128), id2, s > 0 ? 1u : 0u);
+      const uint32_t id3 = tc::idesc_bf16(128, 80, 1, 1);
+      const uint32_t id5 = tc::idesc_bf16(128, 16, 1, 1);
+#pragma unroll
+      for (int s = 0; s < 8; s++) {
+        const uint32_t acc = (it > 0 || s > 0) ? 1u : 0u;
+        tc::mma_bf16(tmem + TGW2, tc::sdesc(sb + SDZ2 + 4096u * s, 2048, 128),
+                     tc::sdesc(sb + SH1 + 2560u * s, 1280, 128), id3, acc);
+        tc::mma_bf16(tmem + TGW3, tc::sdesc(sb + SH2 + 4096u * s, 2048, 128),
+                     tc::sdesc(sb + SDO + 512u * s, 256, 128), id5, acc);
+      }
+      tc::mma_commit(bar);
+    }
+    pending = true;
+    if (!__syncthreads_and(tc::mbar_wait(bar, phase, MLP_WAIT_LIMIT))) { failed = true; break; }
+    pending = false;
+    phase ^= 1u;
+    tc::fence_after_sync();
+    // ---- dz1 = dh1 gelu'(z1)
+#pragma unroll
+    for (int c = 0; c < MLP_H; c += 16) {
+      float t[16];
+      tc::tmem_ld16(tmem + lane_off + TDH1 + (uint32_t)c, t);
+      tc::tmem_wait_ld();
+      float a[8], b[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        a[u] = valid ? t[u] * g1d[c + u] : 0.f;
+        b[u] = valid ? t[8 + u] * g1d[c + 8 + u] : 0.f;
+      }
+      st_row8(base + SDZ1, tid, c, 128, a);
+      st_row8(base + SDZ1, tid, c + 8, 128, b);
+    }
+    // ---- MMA4: GW1 += DZ1^T [F|1]
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      const uint32_t id4 = tc::idesc_bf16(128, 16, 1, 1);
+#pragma unroll
+      for (int s = 0; s < 8; s++)
+        tc::mma_bf16(tmem + TGW1, tc::sdesc(sb + SDZ1 + 4096u * s, 2048, 128),
+                     tc::sdesc(sb + SFX + 512u * s, 256, 128), id4, (it > 0 || s > 0) ? 1u : 0u);
+      tc::mma_commit(bar);
+    }
+    pending = true;
+    if (!__syncthreads_and(tc::mbar_wait(bar, phase, MLP_WAIT_LIMIT))) { failed = true; break; }
+    pending = false;
+    phase ^= 1u;
+    tc::fence_after_sync();
+  }
+  if (failed) {
+    if (tid == 0) atomicOr(err, 1);
+    if (pending) tc::mbar_wait(bar, phase, MLP_WAIT_LIMIT);
+  }
+  // ---- gradient partials of this CTA
+  float *gp = gpart + (size_t)blockIdx.x * MLP_NPARAMS;
+  if (it == 0 || failed) {
+    for (int k = tid; k < MLP_NPARAMS; k += MLP_THREADS) gp[k] = 0.f;
+  } else if (warp < 3) {
+    const int row = 32 * warp + lane;
+    if (warp < 2) {
+      for (int c = 0; c < 80; c += 16) {
+        float t[16];
+        tc::tmem_ld16(tmem + lane_off + TGW2 + (uint32_t)c, t);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int u = 0; u < 16; u++) {
+          const int col = c + u;
+          if (col < 64) gp[MLP_OFF_W2 + row * 64 + col] = t[u];
+          else if (col == 64) gp[MLP_OFF_B2 + row] = t[u];
+        }
+      }
+      float t[16];
+      tc::tmem_ld16(tmem + lane_off + TGW1, t);
+      tc::tmem_wait_ld();
+#pragma unroll
+      for (int k = 0; k < 4; k++) gp[MLP_OFF_W1 + row * 4 + k] = t[k];
+      gp[MLP_OFF_B1 + row] = t[4];
+    }
+    float t[16];
+    tc::tmem_ld16(tmem + lane_off + TGW3, t);
+    tc::tmem_wait_ld();
+    if (row < 64) gp[MLP_OFF_W3 + row] = t[0];
+    else if (row == 64) gp[MLP_OFF_B3] = t[0];
+  }
+  // ---- loss partial (fixed order)
+  __shared__ double lred[MLP_THREADS / 32];
+  for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
+  if (lane == 0) lred[warp] = loss;
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (tid == 0) {
+    double s = 0.0;
+    for (int w = 0; w < MLP_THREADS / 32; w++) s += lred[w];
+    lpart[blockIdx.x] = s;
+  }
+  if (warp == 0) tc::tmem_dealloc(tmem, TCOLS);
+}
+
+// Sums the CTA partials in fixed order, scales (2/n: gradient of the mean squared error),
+// writes the gradient, and (lr > 0) takes one Adam step on the FP32 master weights; then
+// refreshes the weights the kernels use (BF16-rounded W1, W2, w3) and the W2 image.
+static __global__ void k_mlp_adam(int nparts, const float *__restrict__ gpart, float scale, float *__restrict__ grad,
+                                  float *__restrict__ master, float *__restrict__ m1, float *__restrict__ m2,
+                                  float *__restrict__ wuse, uint16_t *__restrict__ w2img, float lr, float b1c,
+                                  float b2c) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= MLP_NPARAMS) return;
+  float g = 0.f;
+  for (int c = 0; c < nparts; c++) g += gpart[(size_t)c * MLP_NPARAMS + p];
+  g *= scale;
+  if (grad) grad[p] = g;
+  float w = master[p];
+  if (lr > 0.f) {
+    const float beta1 = 0.9f, beta2 = 0.999f, eps = 1e-8f;
+    const float a = beta1 * m1[p] + (1.f - beta1) * g;
+    const float b = beta2 * m2[p] + (1.f - beta2) * g * g;
+    m1[p] = a;
+    m2[p] = b;
+    w -= lr * (a / b1c) / (sqrtf(b / b2c) + eps);
+    master[p] = w;
+  }
+  const bool is_w = (p < MLP_OFF_B1) || (p >= MLP_OFF_W2 && p < MLP_OFF_B2) || (p >= MLP_OFF_W3 && p < MLP_OFF_B3);
+  const __nv_bfloat16 wb = __float2bfloat16_rn(w);
+  wuse[p] = is_w ? __bfloat162float(wb) : w;
+  if (p >= MLP_OFF_W2 && p < MLP_OFF_B2) {
+    const int o = (p - MLP_OFF_W2) / 64, i = (p - MLP_OFF_W2) % 64;
+    w2img[tc::cm_offset(o, i, 64) / 2] = __bfloat16_as_ushort(wb);
+  }
+}
+
+// Feature/target statistics: per block partial sums (double) of x, x^2 (4 columns) and y, y^2.
+static __global__ void k_mlp_stats(const float *__restrict__ x, const float *__restrict__ y, int n,
+                                   double *__restrict__ part) {
+  double s[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float4 v = reinterpret_cast<const float4 *>(x)[i];
+    const double a[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int k = 0; k < 4; k++) { s[k] += a[k]; s[4 + k] += a[k] * a[k]; }
+    s[8] += (double)y[i];
+    s[9] += (double)y[i] * (double)y[i];
+  }
+  __shared__ double red[8][10];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 10; k++) {
+    double t = s[k];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) red[w][k] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x < 10) {
+    double t = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++) t += red[q][threadIdx.x];
+    part[blockIdx.x * 10 + threadIdx.x] = t;
+  }
+}
+
+}  // namespace dfsph

@@ -1,0 +1,133 @@
+// tc.cuh — Blackwell (sm_100 family, here sm_103a) tensor-core primitives in inline PTX:
+// TMEM allocation, tcgen05.mma (kind::f16, BF16 operands, FP32 accumulator), commit to an
+// mbarrier, bounded mbarrier waits, TMEM loads, and the proxy / tcgen05 fences.
+//
+// Operand layout. Every operand tile lives in shared memory without swizzling, as
+// "core matrices" of 8 rows x 16 bytes (8 bf16) stored contiguously (128 B each). A tile
+// of R rows and C bf16 columns (row-major by rows) puts core matrix (R/8 index rg, C/8
+// index cc) at byte offset (rg * (C/8) + cc) * 128; inside it, row r%8 sits at
+// (r%8) * 16 and column c%8 at (c%8) * 2. Such a tile is read by the MMA either
+//   - K-major (rows = M or N, columns = K): K-adjacent core matrices 128 B apart (LBO),
+//     M/N-adjacent ones (C/8)*128 B apart (SBO); or
+//   - MN-major (rows = K, columns = M or N): M/N-adjacent core matrices 128 B apart
+//     (SBO), K-adjacent ones (C/8)*128 B apart (LBO).
+// One MMA instruction consumes K = 16 (two core matrices along K).
+#pragma once
+#include <cstdint>
+
+namespace dfsph {
+namespace tc {
+
+static __device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Byte offset of element (row, col) in a core-matrix tile with `cols` columns (bf16).
+static __host__ __device__ __forceinline__ uint32_t cm_offset(int row, int col, int cols) {
+  return (uint32_t)(((row >> 3) * (cols >> 3) + (col >> 3)) * 128 + (row & 7) * 16 + (col & 7) * 2);
+}
+
+// Shared-memory matrix descriptor (tcgen05 format): start address, leading and stride
+// byte offsets (all >> 4), descriptor version 1 at bits 46-48, no swizzle, base offset 0.
+static __device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// Instruction descriptor for kind::f16 with BF16 A and B, FP32 D.
+// a_mn / b_mn: operand is MN-major (1) or K-major (0).
+static __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N, int a_mn, int b_mn) {
+  return (1u << 4)                     // D format: F32
+         | (1u << 7)                   // A format: BF16
+         | (1u << 10)                  // B format: BF16
+         | ((uint32_t)a_mn << 15)      // A major
+         | ((uint32_t)b_mn << 16)      // B major
+         | ((uint32_t)(N >> 3) << 17)  // N / 8
+         | ((uint32_t)(M >> 4) << 24); // M / 16
+}
+
+// ---- TMEM allocation (one full warp executes these)
+static __device__ __forceinline__ void tmem_alloc(uint32_t *smem_dst, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(smem_dst)),
+               "r"(ncols)
+               : "memory");
+}
+static __device__ __forceinline__ void tmem_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+static __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+// ---- MMA (issued by one thread) and its completion signal
+static __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                                uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+static __device__ __forceinline__ void mma_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+// ---- fences
+static __device__ __forceinline__ void fence_before_sync() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+static __device__ __forceinline__ void fence_after_sync() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+// generic-proxy shared-memory writes made visible to the async proxy (the MMA's operand reads)
+static __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// ---- mbarrier
+static __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+static __device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+static __device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Waits for the phase with the given parity to complete; gives up after `limit` polls
+// (with a short sleep between polls) and returns false.
+static __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t limit) {
+  for (uint32_t k = 0; k < limit; ++k) {
+    if (mbar_test(bar, parity)) return true;
+    __nanosleep(64);
+  }
+  return false;
+}
+
+// ---- TMEM -> registers: 32 lanes x 32 bit, 16 consecutive columns per thread
+static __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int k = 0; k < 16; k++) v[k] = __uint_as_float(r[k]);
+}
+static __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+}  // namespace tc
+}  // namespace dfsph

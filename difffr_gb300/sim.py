@@ -183,7 +183,7 @@ class DiffDFSPH:
     def profile(self):
         """Per kernel class: launches, device ms, work units since profile_enable()."""
         out = {}
-        for k, name in enumerate(_abi.KERNEL_CLASSES):
+        for k, name in enumerate(_abi.KERNEL_CLASSES + _abi.PHASES):
             l, ms, u = c_int64(), c_double(), c_int64()
             check(self.lib, self.lib.dfsph_profile_read(self.h, k, byref(l), byref(ms), byref(u)))
             out[name] = {"launches": l.value, "ms": ms.value, "units": u.value}
@@ -221,3 +221,26 @@ class DiffDFSPH:
     def rigid_state_vector(self, b):
         x, q, v, w = self.rigid_state(b)
         return np.concatenate([x, q, v, w])
+
+    # -------------------------------------------------------------- learned warm start
+    def set_warmstart_model(self, model):
+        """Use a ``WarmStartModel`` for the pressure warm start (None: the reference formula)."""
+        check(self.lib, self.lib.dfsph_set_warmstart_model(self.h, model.h if model is not None else None))
+        self._ws_model = model  # keep the model alive while the context uses it
+
+    def ml_record(self, on=True):
+        check(self.lib, self.lib.dfsph_ml_record(self.h, 1 if on else 0))
+
+    def ml_capture(self, x, y):
+        """Copies the last step's training samples (features, target stiffness) into the
+        device tensors x (float32 [cap, 4]) and y (float32 [cap]); returns the count."""
+        import torch
+        if not (x.is_cuda and y.is_cuda and x.dtype == torch.float32 and y.dtype == torch.float32
+                and x.is_contiguous() and y.is_contiguous() and x.dim() == 2 and x.shape[1] == 4):
+            raise ValueError("x: contiguous CUDA float32 [cap, 4]; y: contiguous CUDA float32 [cap]")
+        torch.cuda.current_stream(x.device).synchronize()  # the library's stream is not ordered against PyTorch's
+        cap = min(int(x.shape[0]), int(y.shape[0]))
+        cnt = c_int64()
+        check(self.lib, self.lib.dfsph_ml_capture(self.h, c_void_p(x.data_ptr()), c_void_p(y.data_ptr()), cap,
+                                                  byref(cnt)))
+        return cnt.value

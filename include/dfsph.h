@@ -304,11 +304,62 @@ int dfsph_event_elapsed(dfsph_ctx *ctx, int32_t slot_a, int32_t slot_b, double *
 #define DFSPH_K_INTEGRATE      6
 #define DFSPH_K_PAIRS          7
 #define DFSPH_K_RIGID          8
-#define DFSPH_K_COUNT          9
+#define DFSPH_K_MLP            9   /* learned warm-start inference */
+#define DFSPH_K_COUNT          10
+/* Phases (read with dfsph_profile_read like kernel classes): whole solves, from their
+   first launch to their last, including the host's residual checks in between. */
+#define DFSPH_PHASE_DIVERGENCE_SOLVE 10
+#define DFSPH_PHASE_PRESSURE_SOLVE   11
+#define DFSPH_PROFILE_COUNT          12
 int dfsph_profile_enable(dfsph_ctx *ctx, int32_t on);
 int dfsph_profile_read(dfsph_ctx *ctx, int32_t kernel_class, int64_t *launches, double *total_ms,
                        int64_t *units);
 const char *dfsph_kernel_class_name(int32_t kernel_class);
+
+/* ---- Learned warm start for the pressure stiffness.
+   No reference counterpart: it replaces the stiffness formula of
+   TimeStepDiffDFSPH::warmstartPressureSolve (TimeStepDiffDFSPH.cpp:964-1059),
+   kappa <- 0.5 max(kappa, -0.00025) / h^2 (where rho_adv > 1), with a per-particle MLP
+   4 -> 64 -> 64 -> 1 (GELU, BF16 weights, FP32 accumulation; the hidden layer on the
+   tensor cores). The Jacobi solve then runs to the same tolerance from that start.
+   Features (float[4] per sample): rho_adv - 1 at the warm start, neighbour count,
+   previous step's stiffness in pass units, |v|; target: the stiffness the solve
+   accumulated in that step (pass units). Data pointers of the dfsph_mlp_* calls are
+   DEVICE pointers (x: float[n][4], y: float[n], idx: int32[n]); the calls are synchronous
+   with the host but not ordered against other streams: the caller finishes writing its
+   buffers (synchronises its stream) before the call.
+   Parameter vector (DFSPH_MLP_NPARAMS floats): W1[64][4], b1[64], W2[64][64] (row =
+   output), b2[64], w3[64], b3. Normalisation (10 floats): feature means[4], feature
+   standard deviations[4], target mean, target standard deviation. */
+#define DFSPH_MLP_NPARAMS 4545
+typedef struct dfsph_mlp dfsph_mlp;
+int dfsph_mlp_create(int32_t device, uint64_t seed, dfsph_mlp **out);
+int dfsph_mlp_destroy(dfsph_mlp *m);
+int dfsph_mlp_get_params(dfsph_mlp *m, float *params, float *norm);
+/* Either pointer may be NULL (left unchanged); new parameters reset the Adam state. */
+int dfsph_mlp_set_params(dfsph_mlp *m, const float *params, const float *norm);
+/* Sets the normalisation from the mean and standard deviation of n samples. */
+int dfsph_mlp_fit_normalization(dfsph_mlp *m, const float *x, const float *y, int64_t n);
+/* One Adam step (beta 0.9/0.999) on the mean squared error (normalised units) over the
+   samples idx[0..n) of the n_samples rows of x and y (idx NULL: rows 0..n); *loss = that
+   error before the step. An index outside [0, n_samples) is an error (the sample is not
+   read). */
+int dfsph_mlp_train_step(dfsph_mlp *m, const float *x, const float *y, int64_t n_samples, const int32_t *idx,
+                         int64_t n, float lr, double *loss);
+/* Gradient of that loss over samples 0..n (DFSPH_MLP_NPARAMS doubles, host) without
+   updating the parameters. */
+int dfsph_mlp_gradient(dfsph_mlp *m, const float *x, const float *y, int64_t n, double *grad, double *loss);
+/* Predicted targets (denormalised) for n samples. */
+int dfsph_mlp_predict(dfsph_mlp *m, const float *x, float *y, int64_t n);
+/* Use model m for the pressure warm start of ctx (NULL: the reference formula). The
+   context keeps the pointer: detach before destroying the model. Needs
+   use_pressure_warmstart. */
+int dfsph_set_warmstart_model(dfsph_ctx *ctx, dfsph_mlp *m);
+/* Recording of training samples: while on, each step keeps its warm-start features and
+   final stiffness; dfsph_ml_capture copies the last step's samples with rho_adv > 1
+   (at most `capacity`) to device buffers and returns how many it wrote. */
+int dfsph_ml_record(dfsph_ctx *ctx, int32_t on);
+int dfsph_ml_capture(dfsph_ctx *ctx, float *x, float *y, int64_t capacity, int64_t *count);
 
 /* Allocation-free average density error, for callers that cannot allocate GPU memory
    where they need it (an embedding that gives its whole device budget to its own pool,

@@ -12,6 +12,7 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(_HERE, "dfsph_oracle.cpp")
+SRCS = [SRC, os.path.join(_HERE, "mlp_oracle.cpp")]
 LIB = os.path.join(_HERE, "_build", "liboracle_dfsph.so")
 
 MODE_F32 = 0       # <float, float>   the reference's default float build
@@ -22,10 +23,10 @@ MODE_F64 = 2       # <double, double> the reference's USE_DOUBLE build
 def build(force=False):
     """Compiles the oracle with g++ (OpenMP, no FMA contraction so x86 and Arm agree)."""
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(s) for s in SRCS):
         return LIB
     cmd = ["g++", "-O3", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
-           "-o", LIB, SRC]
+           "-o", LIB, *SRCS]
     subprocess.check_call(cmd)
     return LIB
 
@@ -65,6 +66,8 @@ def lib():
         fp = POINTER(c_float)
         L.orc_kernel_eval_f.argtypes = [c_float, c_int, fp, fp, fp, fp]
         L.orc_quat_eval.argtypes = [c_int, dp, dp, dp, dp, dp, dp]
+        L.orc_mlp_eval.argtypes = [fp, fp, fp, fp, c_int64, fp, dp]
+        L.orc_mlp_eval.restype = c_double
         _lib = L
     return _lib
 
@@ -208,3 +211,20 @@ def quat_eval(q, p):
     a, b, c, d = np.zeros((n, 3, 4)), np.zeros((n, 3, 4)), np.zeros((n, 4, 4)), np.zeros((n, 4, 3))
     lib().orc_quat_eval(n, _p(q), _p(p), _p(a), _p(b), _p(c), _p(d))
     return a, b, c, d
+
+
+def mlp_eval(params, norm, x, y=None, with_grad=True):
+    """The warm-start MLP on the CPU: (prediction, gradient of the mean squared error or
+    None, loss). params: 4545 floats; norm: 10 floats; x: (n, 4); y: (n,) or None."""
+    fp = POINTER(c_float)
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    norm = np.ascontiguousarray(norm, dtype=np.float32)
+    x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 4)
+    n = x.shape[0]
+    pred = np.zeros(n, dtype=np.float32)
+    yy = None if y is None else np.ascontiguousarray(y, dtype=np.float32)
+    grad = np.zeros(4545) if (with_grad and y is not None) else None
+    loss = lib().orc_mlp_eval(params.ctypes.data_as(fp), norm.ctypes.data_as(fp), x.ctypes.data_as(fp),
+                              None if yy is None else yy.ctypes.data_as(fp), n, pred.ctypes.data_as(fp),
+                              None if grad is None else _p(grad))
+    return pred, grad, loss
