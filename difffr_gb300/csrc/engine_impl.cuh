@@ -621,7 +621,7 @@ int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
     sort_fluid();
     sort_dynamic();
     if (n_ > 0) {
-      { pbegin(); k_lists_density_factor<T><<<blocks(n_), 256, 0, stream_>>>(fc_, R_[cur_].p, cstartF_.p,
+      { pbegin(); k_lists_density_factor<T><<<blocks(n_, LIST_THREADS), LIST_THREADS, 0, stream_>>>(fc_, R_[cur_].p, cstartF_.p,
                                                                  BR_.p, cstartS_.p, nd_ ? cstartD_.p : nullptr, ns_,
                                                                  flist_.p, fcount_.p, blist_.p, bcount_.p, rho_.p,
                                                                  alpha_.p, sumgrad_.p, err_.p);
@@ -1090,7 +1090,7 @@ void Engine<T>::launch_mlp_warmstart(T *kap) {
   if (n_ == 0) return;
   pbegin();
   const int ntiles = (n_ + MLP_TILE - 1) / MLP_TILE;
-  const int grid = std::min(ntiles, num_sms_ * 7);
+  const int grid = std::min(ntiles, num_sms_ * 8);
   k_mlp_infer<MlpWarmIO<T>><<<grid, MLP_THREADS, MLP_INFER_SMEM, stream_>>>(mlv_, MlpWarmIO<T>{F_.p, Q_.p, kap}, n_,
                                                                            err_.p, ERR_MLP_TIMEOUT);
   launched();

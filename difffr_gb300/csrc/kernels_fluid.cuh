@@ -135,8 +135,9 @@ static __device__ __forceinline__ void for_each_row(const Grid<T> &g, const int 
 // Neighbour lists (fluid and boundary), density (TimeStep.cpp:147-200) and the
 // DFSPH factor with sum_grad_p_k (TimeStepDiffDFSPH.cpp:883-962), fused in one pass.
 // Also stores the XSPH weight m_i / rho_i in v[i].w for the viscosity pass.
+constexpr int LIST_THREADS = 256;
 template <class T>
-static __global__ void __launch_bounds__(256) k_lists_density_factor(
+static __global__ void __launch_bounds__(LIST_THREADS) k_lists_density_factor(
     FluidConsts<T> c, Rec<T> *__restrict__ R, const int *__restrict__ cstartF,
     const Rec<T> *__restrict__ BR, const int *__restrict__ cstartS, const int *__restrict__ cstartD, int ns,
     int *__restrict__ flist, int *__restrict__ fcount, int *__restrict__ blist, int *__restrict__ bcount,
@@ -292,23 +293,49 @@ enum PassMode : int {
 constexpr int LPP = 1;  // lanes per particle in the neighbour passes
 
 // Visits the entries k = s, s + LPP, ... < cnt of the neighbour-major list of particle i
-// for sub-lane s, U at a time: U index loads, then U gathers (load(j)), then U bodies.
+// for sub-lane s, U at a time, as a software pipeline: the U list indices of the next
+// batch are requested before the U gathers (load(j)) of the current batch are consumed,
+// so the list's DRAM latency overlaps the gathers. Bodies run in ascending k.
 template <int U, class D, class LoadF, class BodyF>
 static __device__ __forceinline__ void for_neighbors_sub(int cnt, const int *__restrict__ list, int n, int i, int s,
                                                          LoadF &&load, BodyF &&body) {
-  for (int k0 = s; k0 < cnt; k0 += U * LPP) {
-    int js[U];
+  int js[U];
 #pragma unroll
-    for (int u = 0; u < U; u++) js[u] = (k0 + u * LPP < cnt) ? __ldcs(list + (size_t)(k0 + u * LPP) * n + i) : -1;
+  for (int u = 0; u < U; u++) js[u] = (s + u * LPP < cnt) ? __ldcs(list + (size_t)(s + u * LPP) * n + i) : 0;
+  for (int k0 = s; k0 < cnt; k0 += U * LPP) {
     D d[U];
 #pragma unroll
     for (int u = 0; u < U; u++)
-      if (js[u] >= 0) d[u] = load(js[u]);
+      if (k0 + u * LPP < cnt) d[u] = load(js[u]);
+    const int k1 = k0 + U * LPP;
+#pragma unroll
+    for (int u = 0; u < U; u++) js[u] = (k1 + u * LPP < cnt) ? __ldcs(list + (size_t)(k1 + u * LPP) * n + i) : 0;
 #pragma unroll
     for (int u = 0; u < U; u++)
-      if (js[u] >= 0) body(d[u]);
+      if (k0 + u * LPP < cnt) body(d[u]);
   }
 }
+
+// Batch sizes of the neighbour passes and their minimum resident blocks per SM
+// (register budget); build-time tuning constants.
+#ifndef DFSPH_DENSITY_BATCH
+#define DFSPH_DENSITY_BATCH 2
+#endif
+#ifndef DFSPH_VELOCITY_BATCH
+#define DFSPH_VELOCITY_BATCH 4
+#endif
+#ifndef DFSPH_XSPH_BATCH
+#define DFSPH_XSPH_BATCH 4
+#endif
+#ifndef DFSPH_DENSITY_MIN_BLOCKS
+#define DFSPH_DENSITY_MIN_BLOCKS 6
+#endif
+#ifndef DFSPH_VELOCITY_MIN_BLOCKS
+#define DFSPH_VELOCITY_MIN_BLOCKS 4
+#endif
+#ifndef DFSPH_XSPH_MIN_BLOCKS
+#define DFSPH_XSPH_MIN_BLOCKS 4
+#endif
 
 // Sum over the LPP sub-lanes of a particle (all lanes of the warp take part).
 template <class T> static __device__ __forceinline__ T sub_sum(T v) {
@@ -322,7 +349,7 @@ template <class T> static __device__ __forceinline__ T sub_sum(T v) {
 // Reads R (positions, velocities); writes Q[i] = (x_i, k_i): the next velocity pass
 // gathers position and stiffness of a neighbour with one 16-byte load.
 template <class T, int MODE>
-static __global__ void __launch_bounds__(256) k_density_pass(
+static __global__ void __launch_bounds__(256, DFSPH_DENSITY_MIN_BLOCKS) k_density_pass(
     FluidConsts<T> c, const Rec<T> *__restrict__ R, V4<T> *__restrict__ Q, const Rec<T> *__restrict__ BR,
     const int *__restrict__ flist, const int *__restrict__ fcount, const int *__restrict__ blist,
     const int *__restrict__ bcount, const T *__restrict__ rho, const T *__restrict__ alpha, T *__restrict__ rhoAdv,
@@ -338,13 +365,13 @@ static __global__ void __launch_bounds__(256) k_density_pass(
     ri = ld_rec(R + i);
     const V4<T> xi = ri.x, vi4 = ri.v;
     nf = fcount[i];
-    for_neighbors_sub<4, Rec<T>>(nf, flist, c.n, i, s, [&](int j) { return ld_rec(R + j); }, [&](const Rec<T> &d) {
+    for_neighbors_sub<DFSPH_DENSITY_BATCH, Rec<T>>(nf, flist, c.n, i, s, [&](int j) { return ld_rec(R + j); }, [&](const Rec<T> &d) {
       const T rx = xi.x - d.x.x, ry = xi.y - d.x.y, rz = xi.z - d.x.z;
       const T g = KEval<T>::G(rx * rx + ry * ry + rz * rz, c.kc);
       delta += c.V * (g * ((vi4.x - d.v.x) * rx + (vi4.y - d.v.y) * ry + (vi4.z - d.v.z) * rz));
     });
     nb = bcount[i];
-    for_neighbors_sub<4, Rec<T>>(nb, blist, c.n, i, s, [&](int j) { return ld_rec(BR + j); }, [&](const Rec<T> &d) {
+    for_neighbors_sub<DFSPH_DENSITY_BATCH, Rec<T>>(nb, blist, c.n, i, s, [&](int j) { return ld_rec(BR + j); }, [&](const Rec<T> &d) {
       const T rx = xi.x - d.x.x, ry = xi.y - d.x.y, rz = xi.z - d.x.z;
       const T g = KEval<T>::G(rx * rx + ry * ry + rz * rz, c.kc);
       delta += d.x.w * (g * ((vi4.x - d.v.x) * rx + (vi4.y - d.v.y) * ry + (vi4.z - d.v.z) * rz));
@@ -392,7 +419,7 @@ static __global__ void __launch_bounds__(256) k_density_pass(
 // v_i += -dt k_i (-psi grad W) over boundary neighbours [if |k_i| > eps].
 // ACC = 1 adds k_i to kappa_acc (the solver's running stiffness). v[i].w is kept.
 template <class T, int ACC>
-static __global__ void __launch_bounds__(256) k_velocity_pass(
+static __global__ void __launch_bounds__(256, DFSPH_VELOCITY_MIN_BLOCKS) k_velocity_pass(
     FluidConsts<T> c, const V4<T> *__restrict__ Q, Rec<T> *__restrict__ R, const Rec<T> *__restrict__ BR,
     const int *__restrict__ flist, const int *__restrict__ fcount, const int *__restrict__ blist,
     const int *__restrict__ bcount, T *__restrict__ kappa_acc) {
@@ -405,7 +432,7 @@ static __global__ void __launch_bounds__(256) k_velocity_pass(
     const V4<T> qi = Q[i];
     ki = qi.w;
     const T sV = c.dt * c.V;
-    for_neighbors_sub<8, V4<T>>(fcount[i], flist, c.n, i, s, [&](int j) { return Q[j]; }, [&](const V4<T> &qj) {
+    for_neighbors_sub<DFSPH_VELOCITY_BATCH, V4<T>>(fcount[i], flist, c.n, i, s, [&](int j) { return Q[j]; }, [&](const V4<T> &qj) {
       const T kSum = ki + qj.w;
       if (fabs(kSum) > c.eps) {
         const T rx = qi.x - qj.x, ry = qi.y - qj.y, rz = qi.z - qj.z;
@@ -415,7 +442,7 @@ static __global__ void __launch_bounds__(256) k_velocity_pass(
     });
     if (fabs(ki) > c.eps) {
       const T sk = c.dt * ki;
-      for_neighbors_sub<8, V4<T>>(bcount[i], blist, c.n, i, s, [&](int j) { return BR[j].x; }, [&](const V4<T> &xj) {
+      for_neighbors_sub<DFSPH_VELOCITY_BATCH, V4<T>>(bcount[i], blist, c.n, i, s, [&](int j) { return BR[j].x; }, [&](const V4<T> &xj) {
         const T rx = qi.x - xj.x, ry = qi.y - xj.y, rz = qi.z - xj.z;
         const T f = sk * xj.w * KEval<T>::G(rx * rx + ry * ry + rz * rz, c.kc);
         dvx += f * rx; dvy += f * ry; dvz += f * rz;
@@ -436,7 +463,7 @@ static __global__ void __launch_bounds__(256) k_velocity_pass(
 // (end of the divergence solve, :870-880) when scale_kappaV is set.
 // v[j].w holds m_j / rho_j.
 template <class T>
-static __global__ void __launch_bounds__(256) k_xsph_advect(FluidConsts<T> c, const Rec<T> *__restrict__ R,
+static __global__ void __launch_bounds__(256, DFSPH_XSPH_MIN_BLOCKS) k_xsph_advect(FluidConsts<T> c, const Rec<T> *__restrict__ R,
                                                             Rec<T> *__restrict__ R_out, const int *__restrict__ flist,
                                                             const int *__restrict__ fcount, T *__restrict__ kappaV,
                                                             int scale_kappaV) {
@@ -449,7 +476,7 @@ static __global__ void __launch_bounds__(256) k_xsph_advect(FluidConsts<T> c, co
     ri = ld_rec(R + i);
     const V4<T> xi = ri.x, vi = ri.v;
     const T cvis = c.invH * c.visc;
-    for_neighbors_sub<4, Rec<T>>(fcount[i], flist, c.n, i, s, [&](int j) { return ld_rec(R + j); },
+    for_neighbors_sub<DFSPH_XSPH_BATCH, Rec<T>>(fcount[i], flist, c.n, i, s, [&](int j) { return ld_rec(R + j); },
                                  [&](const Rec<T> &d) {
       const T rx = xi.x - d.x.x, ry = xi.y - d.x.y, rz = xi.z - d.x.z;
       const T w = KEval<T>::W(rx * rx + ry * ry + rz * rz, c.kc);

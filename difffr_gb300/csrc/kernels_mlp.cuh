@@ -30,12 +30,20 @@ constexpr int MLP_TILE = 128;                            // particles per MMA ti
 constexpr int MLP_THREADS = 128;
 constexpr uint32_t MLP_WAIT_LIMIT = 1u << 21;            // mbarrier polls (x 64 ns sleep) before giving up
 
+// hardware tanh (one MUFU instruction; relative error about 2^-11, below the BF16
+// rounding every activation goes through before the tensor-core products)
+static __device__ __forceinline__ float tanh_approx(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 static __device__ __forceinline__ float gelu_d(float x, float &d) {
   // tanh form: 0.5 x (1 + tanh(c (x + a x^3)))
   const float c = 0.7978845608028654f, a = 0.044715f;
   const float x2 = x * x;
   const float u = c * (x + a * x2 * x);
-  const float t = tanhf(u);
+  const float t = tanh_approx(u);
   d = 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * c * (1.0f + 3.0f * a * x2);
   return 0.5f * x * (1.0f + t);
 }
@@ -107,7 +115,12 @@ static __device__ __forceinline__ void mlp_layer1(const float *sw, const float f
 // W2 image 8 KB, the H1 tile 16 KB, small weights, one mbarrier; TMEM: 64 columns.
 // IO supplies `bool load(int i, float f[4])` (false: no prediction wanted for i) and
 // `void store(int i, float y)`.
-constexpr int MLP_INFER_SMEM = 32 * 1024;  // also caps residency at 7 CTAs per SM (7 x 64 TMEM columns)
+// 8192 (W2) + 16384 (H1 tile) + 1808 (small weights) + 16 (barrier, TMEM address) + 1008
+// (alignment) bytes. At 27 KB at most 8 CTAs fit on an SM, and 8 x 64 TMEM columns is
+// exactly the SM's 512, so no CTA waits in tcgen05.alloc.
+constexpr int MLP_INFER_SMEM = 27 * 1024;
+static_assert(8192 + 16384 + MLP_SW_N * 4 + 16 + 1008 <= MLP_INFER_SMEM, "inference tile layout fits");
+static_assert((228 * 1024) / (MLP_INFER_SMEM + 1024) <= 8, "at most 8 CTAs (512 TMEM columns) per SM");
 
 template <class IO>
 static __global__ void __launch_bounds__(MLP_THREADS) k_mlp_infer(MlpView mv, IO io, int n, int *err, int errbit) {

@@ -297,16 +297,31 @@ static __global__ void __launch_bounds__(RED_VALUES * RED_PARTS) k_body_reduce(B
   const int val = t / RED_PARTS, p = t % RED_PARTS;
   double s = 0.0;
   if (val < RED_VALUES) {
-    for (int d = B.dstart + p; d < B.dstart + B.dcount; d += RED_PARTS) {
-      const double *row = acc + (size_t)d * ACC_STRIDE;
-      if (val < 3 + NJAC) s += row[val];
-      else {
-        const V4<T> xj = xd[d];
-        const double rx = (double)xj.x - B.x[0], ry = (double)xj.y - B.x[1], rz = (double)xj.z - B.x[2];
-        const double fx = row[0], fy = row[1], fz = row[2];
-        const int comp = val - 3 - NJAC;
-        s += comp == 0 ? ry * fz - rz * fy : (comp == 1 ? rz * fx - rx * fz : rx * fy - ry * fx);
+    // the rows d = dstart + p, + RED_PARTS, ... are summed in this order; UNROLL of them
+    // are loaded before their additions so the loads overlap
+    constexpr int UNROLL = 8;
+    const int dend = B.dstart + B.dcount;
+    for (int d0 = B.dstart + p; d0 < dend; d0 += UNROLL * RED_PARTS) {
+      double t[UNROLL];
+#pragma unroll
+      for (int u = 0; u < UNROLL; u++) {
+        const int d = d0 + u * RED_PARTS;
+        t[u] = 0.0;
+        if (d < dend) {
+          const double *row = acc + (size_t)d * ACC_STRIDE;
+          if (val < 3 + NJAC) t[u] = row[val];
+          else {
+            const V4<T> xj = xd[d];
+            const double rx = (double)xj.x - B.x[0], ry = (double)xj.y - B.x[1], rz = (double)xj.z - B.x[2];
+            const double fx = row[0], fy = row[1], fz = row[2];
+            const int comp = val - 3 - NJAC;
+            t[u] = comp == 0 ? ry * fz - rz * fy : (comp == 1 ? rz * fx - rx * fz : rx * fy - ry * fx);
+          }
+        }
       }
+#pragma unroll
+      for (int u = 0; u < UNROLL; u++)
+        if (d0 + u * RED_PARTS < dend) s += t[u];
     }
   }
   part[t] = s;
@@ -468,10 +483,20 @@ static __global__ void __launch_bounds__(128) k_rigid_step(BodyState *__restrict
   __shared__ ChainCoef C;
   __shared__ double A[NSTATE * NSTATE];
   __shared__ double Gold[NSTATE * 6];
+  // the body record is worked on in shared memory (the single-thread parts read it
+  // many times) and written back at the end
+  __shared__ BodyState sB;
+  static_assert(sizeof(BodyState) % 8 == 0, "BodyState copies as 8-byte words");
   const int b = blockIdx.x;
   if (b >= nbodies) return;
-  BodyState &B = bs[b];
   const int t = threadIdx.x;
+  {
+    const unsigned long long *src = reinterpret_cast<const unsigned long long *>(bs + b);
+    unsigned long long *dst = reinterpret_cast<unsigned long long *>(&sB);
+    for (int k = t; k < (int)(sizeof(BodyState) / 8); k += blockDim.x) dst[k] = src[k];
+  }
+  __syncthreads();
+  BodyState &B = sB;
   const bool chain = B.dyn && !B.anim && rc.enable_gradient;
   if (t == 0) B.chain_ran = chain ? 1 : 0;
   if (chain) {
@@ -568,6 +593,12 @@ static __global__ void __launch_bounds__(128) k_rigid_step(BodyState *__restrict
     for (int i = 0; i < 3; i++)
       for (int j = 0; j < 3; j++) B.I[3 * i + j] = RI[3 * i] * RT[j] + RI[3 * i + 1] * RT[3 + j] + RI[3 * i + 2] * RT[6 + j];
     inv3<double>(B.I, B.Iinv);
+  }
+  __syncthreads();
+  {
+    const unsigned long long *src = reinterpret_cast<const unsigned long long *>(&sB);
+    unsigned long long *dst = reinterpret_cast<unsigned long long *>(bs + b);
+    for (int k = t; k < (int)(sizeof(BodyState) / 8); k += blockDim.x) dst[k] = src[k];
   }
 }
 

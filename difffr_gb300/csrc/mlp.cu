@@ -297,7 +297,7 @@ int dfsph_mlp_predict(dfsph_mlp *m, const float *x, float *y, int64_t n) {
     check_device_ptr(x, "x");
     check_device_ptr(y, "y");
     const int ntiles = (int)((n + MLP_TILE - 1) / MLP_TILE);
-    const int grid = std::min(ntiles, m->nparts * 7);
+    const int grid = std::min(ntiles, m->nparts * 8);
     DF_CK(cudaMemsetAsync(m->err, 0, sizeof(int), m->stream));
     k_mlp_infer<MlpArrayIO><<<grid, MLP_THREADS, MLP_INFER_SMEM, m->stream>>>(mlp_view(m), MlpArrayIO{x, y}, (int)n,
                                                                              m->err, 1);
