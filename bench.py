@@ -37,6 +37,20 @@ ALGO_BYTES = {
 }
 
 
+# DRAM bytes per particle and launch (dram__bytes_read.sum + dram__bytes_write.sum) from the
+# ncu capture summarised in profiles/fluid_passes_dam_break_262k.md (262,144 particles, L2
+# flushed by ncu before each launch), scaled by the launch's particle count.
+MEASURED_TRAFFIC = {"density_pass": 178.3, "velocity_pass": 179.5}
+
+
+def load_sm_max_mhz():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f).get("sm_max_mhz", 2070.0))
+    return 2070.0
+
+
 def load_peaks():
     p = os.path.join(HERE, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -47,7 +61,11 @@ def load_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    """SM clock and clock-event (throttle) reasons sampled during the timed region: NVML
+    read through ctypes every 2 ms (a background thread), or nvidia-smi every 200 ms
+    where NVML cannot be loaded. Read-only: no clock or setting is changed."""
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -56,8 +74,44 @@ class ClockSampler:
         self.gpu = gpu_index
         self.proc = None
         self.path = None
+        self.thread = None
+        self.samples = []
+        self.max_mhz = None
+
+    def _nvml(self):
+        import ctypes
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit")
+        dev = ctypes.c_void_p()
+        if lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(self.gpu), ctypes.byref(dev)) != 0:
+            raise RuntimeError("nvml handle")
+        reasons_fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            getattr(lib, "nvmlDeviceGetCurrentClocksThrottleReasons")
+        mx = ctypes.c_uint()
+        if lib.nvmlDeviceGetMaxClockInfo(dev, ctypes.c_int(1), ctypes.byref(mx)) == 0:
+            self.max_mhz = float(mx.value)
+        return lib, dev, reasons_fn
 
     def start(self):
+        import threading
+        try:
+            import ctypes
+            lib, dev, reasons_fn = self._nvml()
+            self.stop_flag = threading.Event()
+
+            def run():
+                clk, rs = ctypes.c_uint(), ctypes.c_ulonglong()
+                while not self.stop_flag.is_set():
+                    if lib.nvmlDeviceGetClockInfo(dev, ctypes.c_int(1), ctypes.byref(clk)) == 0 and \
+                            reasons_fn(dev, ctypes.byref(rs)) == 0:
+                        self.samples.append((float(clk.value), int(rs.value)))
+                    time.sleep(0.002)
+            self.thread = threading.Thread(target=run, daemon=True)
+            self.thread.start()
+            return
+        except Exception:
+            self.thread = None
         try:
             fd, self.path = tempfile.mkstemp(suffix=".csv")
             os.close(fd)
@@ -69,6 +123,18 @@ class ClockSampler:
 
     def stop(self):
         out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if self.thread is not None:
+            self.stop_flag.set()
+            self.thread.join(timeout=2)
+            if self.samples:
+                reasons = set()
+                for _, r in self.samples:
+                    for bit, nm in self.REASONS.items():
+                        if r & bit:
+                            reasons.add(nm)
+                out = {"sm_mhz": statistics.median(c for c, _ in self.samples), "sm_max_mhz": self.max_mhz,
+                       "reasons": sorted(reasons), "samples": len(self.samples), "source": "nvml, 2 ms"}
+            return out
         if self.proc is None:
             return out
         self.proc.terminate()
@@ -94,7 +160,7 @@ class ClockSampler:
         os.unlink(self.path)
         if sm:
             out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
-                   "samples": len(sm)}
+                   "samples": len(sm), "source": "nvidia-smi, 200 ms"}
         return out
 
 
@@ -223,16 +289,21 @@ def run_ours(args):
     units_per_launch = d["units"] / max(d["launches"], 1)
     algo_bytes = ALGO_BYTES.get(dom, 32) * units_per_launch
     achieved = algo_bytes / avg_launch_s / 1e9
-    traffic = None
-    tfile = os.path.join(HERE, "profiles", "traffic.json")
-    if os.path.exists(tfile):
-        try:
-            with open(tfile) as f:
-                tj = json.load(f)
-            if dom in tj:
-                traffic = tj[dom]["bytes_per_particle"] * units_per_launch
-        except Exception:
-            traffic = None
+    traffic = MEASURED_TRAFFIC[dom] * units_per_launch if dom in MEASURED_TRAFFIC else None
+    # the L1 side of the same kernel: each neighbour visit gathers one 32-byte record (the
+    # density and XSPH passes; 16 bytes in the velocity pass) and reads a 4-byte list entry
+    from difffr_gb300 import _abi as abi_mod
+    nbar = sim.neighbor_total(abi_mod.NB_FLUID_FLUID) / max(sim.n_fluid, 1)
+    rec = {"density_pass": 32, "xsph_advect": 32, "velocity_pass": 16}.get(dom)
+    l1 = None
+    if rec is not None:
+        import torch
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        l1_peak = 128.0 * sms * load_sm_max_mhz() * 1e6 / 1e9  # GB/s: 128 B per clock per SM
+        l1_achieved = nbar * (rec + 4) * units_per_launch / avg_launch_s / 1e9
+        l1 = {"fluid_neighbours_per_particle": nbar, "bytes_per_particle": nbar * (rec + 4),
+              "achieved": l1_achieved, "peak": l1_peak, "unit": "GB/s", "frac": l1_achieved / l1_peak,
+              "peak_basis": "128 B per clock per SM at the maximum SM clock"}
 
     # ---- forward-only steps/s (no pair Jacobians, no tape)
     sim_f = DiffDFSPH(make_scene(args, enable_gradient=0, seed=rank))
@@ -300,6 +371,7 @@ def run_ours(args):
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "algo_bytes_per_particle": ALGO_BYTES.get(dom, 32),
                          "avg_launch_us": avg_launch_s * 1e6},
+            "l1_gather": l1,
             "kernel_ms_per_step": {k: v["ms"] / args.steps for k, v in prof.items()},
             "clocks": clk,
             "cpu_baseline": cpu,

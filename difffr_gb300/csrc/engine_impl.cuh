@@ -863,6 +863,17 @@ void Engine<T>::neighbors(int which, int64_t *start, int32_t *idx, int64_t *tota
   std::vector<int> d2b(std::max(nd_, 1));
   if (nd_) DF_CK(cudaMemcpy(d2b.data(), dynSortedToBody_.p, nd_ * sizeof(int), cudaMemcpyDeviceToHost));
   auto bmap = [&](int k) { return k < ns_ ? static_orig_[k] : dyn_orig_[d2b[k - ns_]]; };
+  if ((which == DFSPH_NB_FLUID_FLUID || which == DFSPH_NB_FLUID_BOUNDARY) && !start && !idx) {
+    // total only: the list lengths suffice
+    std::vector<int> cnt(std::max(n_, 1));
+    if (n_)
+      DF_CK(cudaMemcpy(cnt.data(), which == DFSPH_NB_FLUID_FLUID ? fcount_.p : bcount_.p, n_ * sizeof(int),
+                       cudaMemcpyDeviceToHost));
+    int64_t t = 0;
+    for (int i = 0; i < n_; i++) t += cnt[i];
+    if (total) *total = t;
+    return;
+  }
   if (which == DFSPH_NB_FLUID_FLUID || which == DFSPH_NB_FLUID_BOUNDARY) {
     const bool ff = which == DFSPH_NB_FLUID_FLUID;
     const int K = ff ? fc_.kf : fc_.kb;

@@ -91,6 +91,12 @@ class DiffDFSPH:
     def velocities(self):
         return self.field(_abi.FIELD_V)
 
+    def neighbor_total(self, which):
+        """Number of (particle, neighbour) pairs of a set after the last step."""
+        tot = c_int64()
+        check(self.lib, self.lib.dfsph_get_neighbors(self.h, int(which), None, None, byref(tot)))
+        return tot.value
+
     def neighbors(self, which):
         tot = c_int64()
         check(self.lib, self.lib.dfsph_get_neighbors(self.h, int(which), None, None, byref(tot)))

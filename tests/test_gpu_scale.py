@@ -55,3 +55,32 @@ def test_pool_thousand_step_checkpointed_adjoint():
     assert r["forward_identical"]
     assert r["max_rel_grad_diff_checkpointed_vs_direct"] <= 1e-12
     assert np.all(np.isfinite(r["grad"]))
+
+
+def test_config0_fp64_trajectory_matches_oracle(gpu_lib, oracle_lib):
+    """The reference's CPU-runnable configuration (8k particles, FP64, sphere dropped into
+    the tank with v = (0.5, 0, 0), omega = (0, 1, 0)), 200 steps: rigid state within 1e-6
+    relative of the FP64 oracle and the gradient blocks (forward chain) with cosine
+    >= 0.9999 per block; the same pressure and divergence sweep counts."""
+    from difffr_gb300.sim import DiffDFSPH
+    sc = scn.config0(precision=_abi.DFSPH_FP64, enable_gradient=1)
+    steps = 200
+    gpu, ref = DiffDFSPH(sc), oracle_lib.Oracle(sc)
+    tot_g = tot_r = 0
+    for _ in range(steps):
+        sg = gpu.step(1)
+        sr = ref.step(1)
+        tot_g += sg["pressure_iterations"] + sg["divergence_iterations"]
+        tot_r += sr["pressure_iterations"] + sr["divergence_iterations"]
+    assert tot_g == tot_r
+    for a, r in zip(gpu.rigid_state(1), ref.rigid_state(1)):
+        assert np.max(np.abs(a - r)) <= 1e-6 * max(np.max(np.abs(r)), 1e-3), (a, r)
+    bg, br = gpu.rigid_grad_blocks(1), ref.rigid_grad_blocks(1)
+    for k in bg:
+        u, v = bg[k].ravel(), br[k].ravel()
+        if np.linalg.norm(v) < 1e-12:  # a block the gradient mode leaves at zero
+            assert np.linalg.norm(u) < 1e-12, (k, u)
+            continue
+        cos = float(u @ v / (np.linalg.norm(u) * np.linalg.norm(v)))
+        assert cos >= 0.9999, (k, cos)
+    gpu.close()
