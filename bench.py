@@ -316,11 +316,12 @@ def run_ours(args):
     sim_f.close()
 
     # ---- end to end through the public API with host buffers: an optimisation-loop
-    # trajectory: set the initial rigid velocity, reset (initial fluid state uploaded from
-    # host memory), K steps each followed by a rigid-state read-back, then the adjoint.
+    # trajectory: the initial rigid velocities from host memory, reset (the context
+    # restores the initial fluid state it holds on the device and uploads the bodies'
+    # initial records), K steps each followed by a rigid-state read-back to the host,
+    # then the adjoint with its host input and output.
     n = sim.n_fluid
     n_boundary = sim.n_boundary
-    elt = 4
     t0 = time.perf_counter()
     for b in range(nb):
         v0, w0 = sim.rigid_init(b)
@@ -334,9 +335,9 @@ def run_ours(args):
     sim.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e_s = allmax(pg, e2e_s)
-    body_state_bytes = 1656  # one device BodyState record per body per read-back
-    h2d = (n * (4 * elt * 2 + 4 * 2) + nb * 13 * 8) / args.steps
-    d2h = nb * body_state_bytes + (nb * 13 * 8) / args.steps
+    body_state_bytes = 1656  # one device BodyState record per body per transfer
+    h2d = (nb * body_state_bytes + 2 * nb * 13 * 8) / args.steps   # reset's body records, adjoint input
+    d2h = nb * body_state_bytes + (nb * 6 * 8) / args.steps         # per-step read-back, gradient
     e2e_value = world * args.steps / e2e_s
 
     # ---- learned warm start vs the reference warm start (collapse phase of a held-out seed)

@@ -156,6 +156,11 @@ static __global__ void k_ml_scatter(int n, const float4 *__restrict__ F, const f
   y[k] = kfin[i];
 }
 
+static __global__ void k_iota2(int n, int *__restrict__ a, int *__restrict__ b) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) { a[i] = i; b[i] = i; }
+}
+
 // ----------------------------------------------------------------- engine
 template <class T>
 class Engine : public EngineBase {
@@ -220,6 +225,7 @@ class Engine : public EngineBase {
 
   // fluid (sorted order), double-buffered where the sort gathers
   DBuf<Rec<T>> R_[2];
+  DBuf<Rec<T>> R_init_;  // initial records (caller order), restored by reset()
   DBuf<V4<T>> Q_;
   DBuf<T> kappa_[2], kappaV_[2];
   DBuf<int> perm_[2];

@@ -345,15 +345,21 @@ template <class T>
 void Engine<T>::upload_fluid_initial() {
   cur_ = 0;
   if (n_ == 0) return;
-  std::vector<Rec<T>> rh(n_);
-  std::vector<int> ph(n_);
-  for (int i = 0; i < n_; i++) {
-    rh[i].x = V4<T>{(T)x_init_[3 * i], (T)x_init_[3 * i + 1], (T)x_init_[3 * i + 2], T(0)};
-    rh[i].v = V4<T>{(T)v_init_[3 * i], (T)v_init_[3 * i + 1], (T)v_init_[3 * i + 2], T(0)};
-    ph[i] = i;
+  // the initial records are converted and uploaded once; later resets copy them on the device
+  if (R_init_.n < (size_t)n_) {
+    std::vector<Rec<T>> rh(n_);
+    for (int i = 0; i < n_; i++) {
+      rh[i].x = V4<T>{(T)x_init_[3 * i], (T)x_init_[3 * i + 1], (T)x_init_[3 * i + 2], T(0)};
+      rh[i].v = V4<T>{(T)v_init_[3 * i], (T)v_init_[3 * i + 1], (T)v_init_[3 * i + 2], T(0)};
+    }
+    R_init_.alloc(n_);
+    DF_CK(cudaMemcpyAsync(R_init_.p, rh.data(), n_ * sizeof(Rec<T>), cudaMemcpyHostToDevice, stream_));
+    DF_CK(cudaStreamSynchronize(stream_));
   }
-  DF_CK(cudaMemcpyAsync(R_[0].p, rh.data(), n_ * sizeof(Rec<T>), cudaMemcpyHostToDevice, stream_));
-  DF_CK(cudaMemcpyAsync(perm_[0].p, ph.data(), n_ * sizeof(int), cudaMemcpyHostToDevice, stream_));
+  DF_CK(cudaMemcpyAsync(R_[0].p, R_init_.p, n_ * sizeof(Rec<T>), cudaMemcpyDeviceToDevice, stream_));
+  // perm[1] must also be a valid permutation before the first gather
+  k_iota2<<<blocks(n_), 256, 0, stream_>>>(n_, perm_[0].p, perm_[1].p);
+  launched();
   DF_CK(cudaMemsetAsync(kappa_[0].p, 0, n_ * sizeof(T), stream_));
   DF_CK(cudaMemsetAsync(kappaV_[0].p, 0, n_ * sizeof(T), stream_));
   DF_CK(cudaMemsetAsync(rho_.p, 0, n_ * sizeof(T), stream_));
@@ -362,11 +368,9 @@ void Engine<T>::upload_fluid_initial() {
   DF_CK(cudaMemsetAsync(sumgrad_.p, 0, n_ * sizeof(V4<T>), stream_));
   DF_CK(cudaMemsetAsync(fcount_.p, 0, n_ * sizeof(int), stream_));
   DF_CK(cudaMemsetAsync(bcount_.p, 0, n_ * sizeof(int), stream_));
-  // perm[1] must also be a valid permutation before the first gather
-  DF_CK(cudaMemcpyAsync(perm_[1].p, ph.data(), n_ * sizeof(int), cudaMemcpyHostToDevice, stream_));
+  check_launch();
   DF_CK(cudaStreamSynchronize(stream_));
 }
-
 template <class T>
 void Engine<T>::body_state_download(std::vector<BodyState> &out) {
   out.resize(nb_);
