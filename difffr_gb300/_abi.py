@@ -66,6 +66,9 @@ class DfsphParams(ctypes.Structure):
         ("target_time", c_double),
         ("max_fluid_neighbors", c_int32),
         ("max_boundary_neighbors", c_int32),
+        ("surface_tension_method", c_int32),
+        ("surface_tension", c_double),
+        ("surface_tension_boundary", c_double),
     ]
 
 

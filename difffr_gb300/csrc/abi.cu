@@ -86,6 +86,9 @@ int dfsph_default_params(dfsph_params *p) {
   p->release_rigid_body_mode = 0;
   p->uniform_accelerate_rb_time = 0.0;
   p->target_time = 0.8;
+  p->surface_tension_method = 0;
+  p->surface_tension = 0.05;
+  p->surface_tension_boundary = 0.01;
   return DFSPH_OK;
 }
 

@@ -227,6 +227,7 @@ class Engine : public EngineBase {
   DBuf<Rec<T>> R_[2];
   DBuf<Rec<T>> R_init_;  // initial records (caller order), restored by reset()
   DBuf<V4<T>> Q_;
+  DBuf<V4<T>> N_;  // surface-tension normals and densities (when enabled)
   DBuf<T> kappa_[2], kappaV_[2];
   DBuf<int> perm_[2];
   int cur_ = 0;

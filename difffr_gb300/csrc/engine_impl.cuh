@@ -88,6 +88,16 @@ Engine<T>::Engine(const dfsph_scene *sc) {
   fc_.invH2 = T(1) / (fc_.dt * fc_.dt);
   fc_.eps = T(1.0e-5);
   fc_.visc = (T)P_.viscosity;
+  {  // Akinci2013 surface tension constants (SPHKernels.h:446-452, 516-520)
+    const double hs = 4.0 * P_.particle_radius;
+    fc_.st_k = (T)P_.surface_tension;
+    fc_.st_kb = (T)P_.surface_tension_boundary;
+    fc_.coh_k = (T)(32.0 / (M_PI * std::pow(hs, 9.0)));
+    fc_.coh_c = (T)(std::pow(hs, 6.0) / 64.0);
+    fc_.adh_k = (T)(0.007 / std::pow(hs, 3.25));
+  }
+  if (P_.surface_tension_method != 0 && P_.surface_tension_method != 2)
+    throw DfsphException(DFSPH_ERR_UNSUPPORTED, "surface_tension_method: 0 (none) or 2 (Akinci2013)");
   fc_.gx = (T)P_.gravity[0]; fc_.gy = (T)P_.gravity[1]; fc_.gz = (T)P_.gravity[2];
   // list capacities, rounded up to whole 16-byte groups for the vector loads
   fc_.kf = ((P_.max_fluid_neighbors > 0 ? P_.max_fluid_neighbors : 96) + 3) / 4 * 4;
@@ -212,6 +222,7 @@ Engine<T>::Engine(const dfsph_scene *sc) {
   for (int k = 0; k < 2; k++) { R_[k].alloc(N); kappa_[k].alloc(N); kappaV_[k].alloc(N); perm_[k].alloc(N); }
   Q_.alloc(N);
   rho_.alloc(N); alpha_.alloc(N); rhoAdv_.alloc(N); sumgrad_.alloc(N);
+  if (P_.surface_tension_method == 2) N_.alloc(N);
   fcount_.alloc(N); bcount_.alloc(N);
   // +8 entries: a batched 16-byte load may read up to 7 entries past a short last row
   flist_.alloc(N * (size_t)fc_.kf + 8);
@@ -642,9 +653,20 @@ int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
       else { last_iters_v_ = 0; last_err_v_ = 0.0; }
       const int nv = 1 - cur_;
       pbegin();
-      k_xsph_advect<T><<<blocks(n_ * LPP), 256, 0, stream_>>>(fc_, R_[cur_].p, R_[nv].p, flist_.p, fcount_.p,
-                                                        kappaV_[cur_].p,
-                                                        (P_.enable_divergence_solver && P_.use_divergence_warmstart) ? 1 : 0);
+      {
+        const int scale_kv = (P_.enable_divergence_solver && P_.use_divergence_warmstart) ? 1 : 0;
+        if (P_.surface_tension_method == 2) {
+          k_normals<T><<<blocks(n_), 256, 0, stream_>>>(fc_, R_[cur_].p, flist_.p, fcount_.p, rho_.p, N_.p);
+          k_xsph_advect<T, true><<<blocks(n_ * LPP), 256, 0, stream_>>>(fc_, R_[cur_].p, R_[nv].p, flist_.p,
+                                                                        fcount_.p, kappaV_[cur_].p, scale_kv, N_.p,
+                                                                        BR_.p, blist_.p, bcount_.p);
+          launched();
+        } else {
+          k_xsph_advect<T, false><<<blocks(n_ * LPP), 256, 0, stream_>>>(fc_, R_[cur_].p, R_[nv].p, flist_.p,
+                                                                         fcount_.p, kappaV_[cur_].p, scale_kv, nullptr,
+                                                                         nullptr, nullptr, nullptr);
+        }
+      }
       launched();
       pend(DFSPH_K_XSPH, n_);
       // the advected state lives in the other record buffer: swap the record pair only

@@ -30,7 +30,38 @@ struct FluidConsts {
   Cubic<T> kc;
   Grid<T> grid;
   int kf, kb;  // list capacities
+  // Akinci2013 surface tension: coefficients, cohesion kernel k and c, adhesion kernel k
+  T st_k, st_kb, coh_k, coh_c, adh_k;
 };
+
+// |r|^2 summed as Eigen's squaredNorm sums a 3-vector (float: x^2 + (y^2 + z^2); double:
+// (x^2 + y^2) + z^2), without contraction: the surface-tension kernels branch on |r|
+// against h/2, and the reference's cohesion kernel is discontinuous there (its constant
+// term h^6/64 is not scaled by k), so the branch has to be decided as the reference does.
+template <class T> static __device__ __forceinline__ T sqnorm_ref(T x, T y, T z);
+template <> __device__ __forceinline__ float sqnorm_ref<float>(float x, float y, float z) {
+  return __fadd_rn(__fmul_rn(x, x), __fadd_rn(__fmul_rn(y, y), __fmul_rn(z, z)));
+}
+template <> __device__ __forceinline__ double sqnorm_ref<double>(double x, double y, double z) {
+  return __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
+}
+
+// CohesionKernel (SPHKernels.h:437-506) and AdhesionKernel (:508-559) with support h,
+// evaluated at r1 = |r| (IEEE square root of r2), r2 = |r|^2 <= h^2; the comparison with
+// 0.5 h is made in double, as the reference's mixed-type expression does.
+template <class T>
+static __device__ __forceinline__ T cohesion_W(T r1, T r2, const FluidConsts<T> &c) {
+  const T d = c.kc.h - r1;
+  const T d3 = d * d * d;
+  return ((double)r1 > 0.5 * (double)c.kc.h) ? c.coh_k * d3 * (r2 * r1) : c.coh_k * T(2) * d3 * (r2 * r1) - c.coh_c;
+}
+template <class T>
+static __device__ __forceinline__ T adhesion_W(T r1, T r2, const FluidConsts<T> &c) {
+  if (!((double)r1 > 0.5 * (double)c.kc.h)) return T(0);
+  T a = -T(4) * r2 / c.kc.h + T(6) * r1 - T(2) * c.kc.h;
+  a = a > T(0) ? a : T(0);  // rounding can take the argument below 0 at |r| = h
+  return c.adh_k * sqrt(sqrt(a));
+}
 
 template <class T>
 struct alignas(8 * sizeof(T)) Rec {
@@ -462,11 +493,16 @@ static __global__ void __launch_bounds__(256, DFSPH_VELOCITY_MIN_BLOCKS) k_veloc
 // Viscosity_XSPH.cpp:35-110, TimeStepDiffDFSPH.cpp:588-605); also kappaV *= dt
 // (end of the divergence solve, :870-880) when scale_kappaV is set.
 // v[j].w holds m_j / rho_j.
-template <class T>
+// ST: Akinci2013 surface tension first (SurfaceTension_Akinci2013.cpp:60-148; it runs before
+// the viscosity, Simulation.cpp:618-631): cohesion and curvature over fluid neighbours with
+// K_ij = 2 rho0 / (rho_i + rho_j), adhesion over boundary neighbours; N[j] = (n_j, rho_j).
+template <class T, bool ST>
 static __global__ void __launch_bounds__(256, DFSPH_XSPH_MIN_BLOCKS) k_xsph_advect(FluidConsts<T> c, const Rec<T> *__restrict__ R,
                                                             Rec<T> *__restrict__ R_out, const int *__restrict__ flist,
                                                             const int *__restrict__ fcount, T *__restrict__ kappaV,
-                                                            int scale_kappaV) {
+                                                            int scale_kappaV, const V4<T> *__restrict__ N,
+                                                            const Rec<T> *__restrict__ BR, const int *__restrict__ blist,
+                                                            const int *__restrict__ bcount) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = t / LPP, s = t % LPP;
   const bool live = i < c.n;
@@ -475,6 +511,34 @@ static __global__ void __launch_bounds__(256, DFSPH_XSPH_MIN_BLOCKS) k_xsph_adve
   if (live) {
     ri = ld_rec(R + i);
     const V4<T> xi = ri.x, vi = ri.v;
+    if (ST) {
+      const V4<T> ni = N[i];
+      for_neighbors_sub<DFSPH_XSPH_BATCH, Rec<T>>(fcount[i], flist, c.n, i, s,
+                                                  [&](int j) { return Rec<T>{R[j].x, N[j]}; }, [&](const Rec<T> &d) {
+        const V4<T> xj = d.x, nj = d.v;
+        const T Kij = T(2) * c.rho0 / (ni.w + nj.w);
+        const T rx = xi.x - xj.x, ry = xi.y - xj.y, rz = xi.z - xj.z;
+        const T r2 = sqnorm_ref(rx, ry, rz);
+        T cx = T(0), cy = T(0), cz = T(0);
+        if (r2 > T(1.0e-9)) {
+          const T r1 = sqrt(r2);
+          const T f = c.st_k * c.m * cohesion_W(r1, r2, c) / r1;
+          cx = -f * rx; cy = -f * ry; cz = -f * rz;
+        }
+        cx -= c.st_k * (ni.x - nj.x); cy -= c.st_k * (ni.y - nj.y); cz -= c.st_k * (ni.z - nj.z);
+        ax += Kij * cx; ay += Kij * cy; az += Kij * cz;
+      });
+      for_neighbors_sub<DFSPH_XSPH_BATCH, V4<T>>(bcount[i], blist, c.n, i, s, [&](int j) { return BR[j].x; },
+                                                 [&](const V4<T> &xj) {
+        const T rx = xi.x - xj.x, ry = xi.y - xj.y, rz = xi.z - xj.z;
+        const T r2 = sqnorm_ref(rx, ry, rz);
+        if (r2 > T(1.0e-9)) {
+          const T r1 = sqrt(r2);
+          const T f = c.st_kb * c.rho0 * xj.w * adhesion_W(r1, r2, c) / r1;
+          ax -= f * rx; ay -= f * ry; az -= f * rz;
+        }
+      });
+    }
     const T cvis = c.invH * c.visc;
     for_neighbors_sub<DFSPH_XSPH_BATCH, Rec<T>>(fcount[i], flist, c.n, i, s, [&](int j) { return ld_rec(R + j); },
                                  [&](const Rec<T> &d) {
@@ -493,6 +557,25 @@ static __global__ void __launch_bounds__(256, DFSPH_XSPH_MIN_BLOCKS) k_xsph_adve
     R_out[i] = Rec<T>{ri.x, V4<T>{vi.x + c.dt * ax, vi.y + c.dt * ay, vi.z + c.dt * az, vi.w}};
     if (scale_kappaV) kappaV[i] *= c.dt;
   }
+}
+
+// Surface-tension normals (SurfaceTension_Akinci2013.cpp:28-58): n_i = h sum_j (m_j/rho_j)
+// grad W_ij over fluid neighbours; N[i] = (n_i, rho_i) for the force part of the XSPH pass.
+template <class T>
+static __global__ void __launch_bounds__(256) k_normals(FluidConsts<T> c, const Rec<T> *__restrict__ R,
+                                                        const int *__restrict__ flist, const int *__restrict__ fcount,
+                                                        const T *__restrict__ rho, V4<T> *__restrict__ N) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= c.n) return;
+  const V4<T> xi = R[i].x;
+  T nx = T(0), ny = T(0), nz = T(0);
+  for_neighbors_sub<DFSPH_XSPH_BATCH, Rec<T>>(fcount[i], flist, c.n, i, 0, [&](int j) { return ld_rec(R + j); },
+                                              [&](const Rec<T> &d) {
+    const T rx = xi.x - d.x.x, ry = xi.y - d.x.y, rz = xi.z - d.x.z;
+    const T g = d.v.w * KEval<T>::G(rx * rx + ry * ry + rz * rz, c.kc);
+    nx += g * rx; ny += g * ry; nz += g * rz;
+  });
+  N[i] = V4<T>{c.kc.h * nx, c.kc.h * ny, c.kc.h * nz, rho[i]};
 }
 
 // x += dt v (TimeStepDiffDFSPH.cpp:613-635); kappa *= dt^2 (:752-767) when requested.

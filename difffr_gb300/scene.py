@@ -51,6 +51,9 @@ class Params:
     target_time: float = 0.8
     max_fluid_neighbors: int = 0
     max_boundary_neighbors: int = 0
+    surface_tension_method: int = 0
+    surface_tension: float = 0.05
+    surface_tension_boundary: float = 0.01
 
 
 @dataclass

@@ -29,6 +29,8 @@ CONFIG_KEYS = {
     "enableDivergenceSolver": "enable_divergence_solver", "gradientMode": "gradient_mode",
     "useReleaseRigidBodyMode": "release_rigid_body_mode", "targetTime": "target_time",
     "uniformAccelerateRBTime": "uniform_accelerate_rb_time",
+    "surfaceTensionMethod": "surface_tension_method", "surfaceTension": "surface_tension",
+    "surfaceTensionBoundary": "surface_tension_boundary", "viscosity": "viscosity",
 }
 
 
@@ -74,7 +76,12 @@ def load_scene(path_or_dict, precision=0, seed=0):
         fn = {"config0": scn.config0, "config1": scn.config1, "config2": scn.config2, "config4": scn.config4,
               "small_contact": scn.small_contact_scene}[name]
         return fn(seed=data.get("seed", seed), **data.get("overrides", {}))
-    cfg = data.get("Configuration", {})
+    cfg = dict(data.get("Configuration", {}))
+    # fluid material keys ("Materials" entries, SceneLoader.cpp) apply to the one fluid
+    for mat in data.get("Materials", []):
+        for k in ("surfaceTensionMethod", "surfaceTension", "surfaceTensionBoundary", "viscosity"):
+            if k in mat:
+                cfg[k] = mat[k]
     kw = {}
     for k, v in CONFIG_KEYS.items():
         if k in cfg:

@@ -89,6 +89,10 @@ typedef struct dfsph_params {
   double  target_time;                 /* targetTime, default 0.8 */
   int32_t max_fluid_neighbors;         /* capacity of each fluid particle's fluid list (0 = default 96) */
   int32_t max_boundary_neighbors;      /* capacity of each fluid particle's boundary list (0 = default 96) */
+  int32_t surface_tension_method;      /* 0 none, 2 Akinci2013 (SurfaceTension_Akinci2013.cpp:28-148);
+                                          scene "surfaceTensionMethod"; default 0 */
+  double  surface_tension;             /* "surfaceTension", default 0.05 (SurfaceTensionBase.cpp:12) */
+  double  surface_tension_boundary;    /* "surfaceTensionBoundary", default 0.01 (SurfaceTensionBase.cpp:13) */
 } dfsph_params;
 
 /*

@@ -67,6 +67,8 @@ def lib():
         L.orc_kernel_eval_f.argtypes = [c_float, c_int, fp, fp, fp, fp]
         L.orc_quat_eval.argtypes = [c_int, dp, dp, dp, dp, dp, dp]
         L.orc_mlp_eval.argtypes = [fp, fp, fp, fp, c_int64, fp, dp]
+        L.orc_st_kernel_eval.argtypes = [c_double, c_int, dp, dp, dp]
+        L.orc_st_kernel_eval_f.argtypes = [c_float, c_int, fp, fp, fp]
         L.orc_mlp_eval.restype = c_double
         _lib = L
     return _lib
@@ -202,6 +204,21 @@ def kernel_eval_f(h, r):
     fp = lambda a: a.ctypes.data_as(POINTER(c_float))
     lib().orc_kernel_eval_f(float(h), n, fp(r), fp(W), fp(G), fp(H))
     return W, G, H
+
+
+def st_kernel_eval(h, r, single=False):
+    """Oracle surface-tension kernels (cohesion, adhesion) at offsets r[n,3], in double or
+    (single=True) float."""
+    dt = np.float32 if single else np.float64
+    r = np.ascontiguousarray(r, dtype=dt)
+    n = r.shape[0]
+    C, A = np.zeros(n, dt), np.zeros(n, dt)
+    if single:
+        fp = lambda a: a.ctypes.data_as(POINTER(c_float))
+        lib().orc_st_kernel_eval_f(float(h), n, fp(r), fp(C), fp(A))
+    else:
+        lib().orc_st_kernel_eval(float(h), n, _p(r), _p(C), _p(A))
+    return C, A
 
 
 def quat_eval(q, p):

@@ -232,6 +232,49 @@ template <class T> struct Cubic {
   }
 };
 
+// ---------------------------------------------------------------- surface-tension kernels
+// SPlisHSPlasH/SPHKernels.h:437-506 (CohesionKernel) and :508-559 (AdhesionKernel), both
+// with the support radius h; the mixed float/double comparisons against 0.5 * radius are
+// kept as in the reference.
+template <class T> struct CohesionK {
+  T radius, k, c;
+  void set(T h) {
+    radius = h;
+    const T pi = static_cast<T>(M_PI);
+    k = static_cast<T>(32.0) / (pi * std::pow(radius, static_cast<T>(9.0)));
+    c = std::pow(radius, static_cast<T>(6.0)) / static_cast<T>(64.0);
+  }
+  T W(const V3<T> &r) const {
+    T res = 0;
+    const T r2 = dot(r, r);
+    if (r2 <= radius * radius) {
+      const T r1 = std::sqrt(r2);
+      const T r3 = r2 * r1;
+      if (r1 > 0.5 * radius) res = k * std::pow(radius - r1, static_cast<T>(3.0)) * r3;
+      else res = k * static_cast<T>(2.0) * std::pow(radius - r1, static_cast<T>(3.0)) * r3 - c;
+    }
+    return res;
+  }
+};
+template <class T> struct AdhesionK {
+  T radius, k;
+  void set(T h) {
+    radius = h;
+    k = static_cast<T>(0.007) / std::pow(radius, static_cast<T>(3.25));
+  }
+  T W(const V3<T> &r) const {
+    T res = 0;
+    const T r2 = dot(r, r);
+    if (r2 <= radius * radius) {
+      const T rl = std::sqrt(r2);
+      if (rl > 0.5 * radius)
+        res = k * std::pow(-static_cast<T>(4.0) * r2 / radius + static_cast<T>(6.0) * rl - static_cast<T>(2.0) * radius,
+                           static_cast<T>(0.25));
+    }
+    return res;
+  }
+};
+
 // ---------------------------------------------------------------- neighbour search
 // Fixed-radius search with the predicate |xi - xj|^2 < h^2, evaluated as
 // ((dx*dx + dy*dy) + dz*dz) < h*h in the fluid scalar type. Rows are sorted ascending.
@@ -318,8 +361,11 @@ struct Sim : Base {
   F r, h, rho0, Vf, mf, visc, dt, invH, invH2, eps;
   V3F grav;
   Cubic<F> K;
+  CohesionK<F> KC;
+  AdhesionK<F> KA;
   int64_t nf = 0, nbp = 0;
   std::vector<V3F> x, v, a, x_init, v_init;
+  std::vector<V3F> normals;  // surface-tension normals (SurfaceTension_Akinci2013.cpp:28-58)
   std::vector<F> rho, factor, kappa, kappaV, rhoAdv;
   std::vector<V3F> sumgrad;
   std::vector<V3F> bx, bv, bx0;
@@ -357,6 +403,8 @@ struct Sim : Base {
     r = (F)P.particle_radius;
     h = F(4) * r;  // Simulation.cpp:385
     K.set(h);
+    KC.set(h);
+    KA.set(h);
     rho0 = (F)P.density0;
     const F diam = F(2) * r;
     Vf = F(0.8) * diam * diam * diam;  // FluidModel.cpp:255-272
@@ -851,10 +899,50 @@ struct Sim : Base {
     compute_densities();
     compute_factor();
     if (P.enable_divergence_solver) divergence_solve(); else { itersV = 0; lastErrV = 0; }
-    // clearAccelerations (TimeStep.cpp:66-81) + Viscosity_XSPH::step (Viscosity_XSPH.cpp:35-110)
+    // clearAccelerations (TimeStep.cpp:66-81), SurfaceTension_Akinci2013::step when enabled
+    // (SurfaceTension_Akinci2013.cpp:28-148; Simulation::computeNonPressureForces runs it
+    // before the viscosity, Simulation.cpp:618-631), Viscosity_XSPH::step (Viscosity_XSPH.cpp:35-110)
+    const bool st = P.surface_tension_method == 2;
+    if (st) {
+      normals.assign(nf, V3F::zero());
+#pragma omp parallel for schedule(static)
+      for (int64_t i = 0; i < nf; i++) {  // computeNormals (:28-58)
+        V3F ni = V3F::zero();
+        for (int64_t s = ffS[i]; s < ffS[i + 1]; s++) {
+          const int j = ff[s];
+          ni += (mf / rho[j]) * K.gradW(x[i] - x[j]);
+        }
+        normals[i] = h * ni;
+      }
+    }
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < nf; i++) {
       V3F ai = grav;
+      if (st) {
+        const F kst = (F)P.surface_tension, kb = (F)P.surface_tension_boundary;
+        for (int64_t s = ffS[i]; s < ffS[i + 1]; s++) {  // cohesion and curvature (:84-107)
+          const int j = ff[s];
+          const F Kij = F(2.0) * rho0 / (rho[i] + rho[j]);
+          V3F accel = V3F::zero();
+          V3F xixj = x[i] - x[j];
+          const F length2 = dot(xixj, xixj);
+          if (length2 > F(1.0e-9)) {
+            xixj = (F(1.0) / std::sqrt(length2)) * xixj;
+            accel -= kst * mf * xixj * KC.W(x[i] - x[j]);
+          }
+          accel -= kst * (normals[i] - normals[j]);
+          ai += Kij * accel;
+        }
+        for (int64_t s = fbS[i]; s < fbS[i + 1]; s++) {  // adhesion (:112-124)
+          const int j = fb[s];
+          V3F xixj = x[i] - bx[j];
+          const F length2 = dot(xixj, xixj);
+          if (length2 > F(1.0e-9)) {
+            xixj = (F(1.0) / std::sqrt(length2)) * xixj;
+            ai -= kb * rho0 * psi[j] * xixj * KA.W(x[i] - bx[j]);
+          }
+        }
+      }
       for (int64_t s = ffS[i]; s < ffS[i + 1]; s++) {
         const int j = ff[s];
         ai -= invH * visc * (mf / rho[j]) * (v[i] - v[j]) * K.W(x[i] - x[j]);
@@ -1070,6 +1158,25 @@ void orc_kernel_eval_f(float h, int n, const float *r, float *W, float *gradW, f
     for (int c = 0; c < 3; c++) gradW[3 * i + c] = g[c];
     orc::M3<float> H = K.gradGradW(v);
     for (int a = 0; a < 3; a++) for (int b = 0; b < 3; b++) gradGradW[9 * i + 3 * a + b] = H(a, b);
+  }
+}
+// Surface-tension kernel probes (cohesion and adhesion, support h) for the golden-vector pin.
+void orc_st_kernel_eval(double h, int n, const double *r, double *C, double *A) {
+  orc::CohesionK<double> KC; KC.set(h);
+  orc::AdhesionK<double> KA; KA.set(h);
+  for (int i = 0; i < n; i++) {
+    orc::V3<double> v = orc::v3<double>(r[3 * i], r[3 * i + 1], r[3 * i + 2]);
+    C[i] = KC.W(v);
+    A[i] = KA.W(v);
+  }
+}
+void orc_st_kernel_eval_f(float h, int n, const float *r, float *C, float *A) {
+  orc::CohesionK<float> KC; KC.set(h);
+  orc::AdhesionK<float> KA; KA.set(h);
+  for (int i = 0; i < n; i++) {
+    orc::V3<float> v = orc::v3<float>(r[3 * i], r[3 * i + 1], r[3 * i + 2]);
+    C[i] = KC.W(v);
+    A[i] = KA.W(v);
   }
 }
 // Quaternion Jacobian probes: q (w,x,y,z), p (3) -> RqP(12), RqTp(12), pq(16) for p=(0,p), wq(12)

@@ -5,7 +5,8 @@
 // stdin (binary): double h, int32 n, n x 3 doubles (kernel offsets), int32 m,
 //                 m x (4 + 3) doubles (quaternion w,x,y,z and a point p)
 // stdout (binary, Real = float or double per build): for each offset W, gradW[3],
-//                 gradGradW[9]; for each (q, p): Rqp[12] RqTp[12] pq[16] wq[12]
+//                 gradGradW[9]; for each (q, p): Rqp[12] RqTp[12] pq[16] wq[12]; then
+//                 for each offset the cohesion and adhesion kernels (support h)
 #include <cstdio>
 #include <cstdint>
 #include <vector>
@@ -44,6 +45,13 @@ int main() {
     for (int a = 0; a < 3; a++) for (int b = 0; b < 4; b++) put(B(a, b));
     for (int a = 0; a < 4; a++) for (int b = 0; b < 4; b++) put(C(a, b));
     for (int a = 0; a < 4; a++) for (int b = 0; b < 3; b++) put(D(a, b));
+  }
+  SPH::CohesionKernel::setRadius((Real)h);
+  SPH::AdhesionKernel::setRadius((Real)h);
+  for (int i = 0; i < n; i++) {
+    Vector3r v((Real)r[3 * i], (Real)r[3 * i + 1], (Real)r[3 * i + 2]);
+    put(SPH::CohesionKernel::W(v));
+    put(SPH::AdhesionKernel::W(v));
   }
   return 0;
 }

@@ -45,11 +45,14 @@ def run(binary, h, r, qp, dtype):
     out = subprocess.run([binary], input=blob, capture_output=True, check=True).stdout
     a = np.frombuffer(out, dtype=dtype)
     nk = r.shape[0] * 13
+    nq = qp.shape[0] * 52
     k = a[:nk].reshape(-1, 13)
-    qq = a[nk:].reshape(-1, 52)
+    qq = a[nk:nk + nq].reshape(-1, 52)
+    st = a[nk + nq:].reshape(-1, 2)
     return {"W": k[:, 0], "gradW": k[:, 1:4], "gradGradW": k[:, 4:13].reshape(-1, 3, 3),
             "Rqp": qq[:, 0:12].reshape(-1, 3, 4), "RqTp": qq[:, 12:24].reshape(-1, 3, 4),
-            "pq": qq[:, 24:40].reshape(-1, 4, 4), "wq": qq[:, 40:52].reshape(-1, 4, 3)}
+            "pq": qq[:, 24:40].reshape(-1, 4, 4), "wq": qq[:, 40:52].reshape(-1, 4, 3),
+            "cohesion": st[:, 0], "adhesion": st[:, 1]}
 
 
 def main():

@@ -162,3 +162,30 @@ def test_neighbor_overflow_reports_device_error(gpu_lib):
     with pytest.raises(_abi.DfsphError) as e:
         g.step(1)
     assert e.value.code == _abi.DFSPH_ERR_DEVICE
+
+
+@pytest.mark.parametrize("precision", [_abi.DFSPH_FP64, _abi.DFSPH_FP32])
+def test_surface_tension_akinci2013_matches_oracle(gpu_lib, oracle_lib, precision):
+    """Akinci2013 surface tension (cohesion, curvature, boundary adhesion) with the
+    reference scenes' coefficient 0.5 and a boundary coefficient 0.1, against the oracle:
+    FP64 over 4 steps, FP32 over 3 steps, every field and the rigid state within 1e-9 (FP64)
+    or 1e-4 (FP32, max norm). The reference's cohesion kernel is discontinuous at |r| = h/2
+    (SPHKernels.h:471-473 subtracts h^6/64 unscaled by k), which is the lattice spacing of
+    these scenes: once FP32 positions differ in their last bits, a pair sitting within that
+    distance of h/2 takes the other branch, and its ~8 m/s^2 jump spreads through the next
+    pressure solve. FP32 runs are compared before that happens."""
+    sc = scn.small_contact_scene(precision=precision, surface_tension_method=2, surface_tension=0.5,
+                                 surface_tension_boundary=0.1)
+    gpu, ref = make(sc), oracle_lib.Oracle(sc)
+    steps = 4 if precision == _abi.DFSPH_FP64 else 3
+    gpu.step(steps)
+    ref.step(steps)
+    tol = 1e-9 if precision == _abi.DFSPH_FP64 else 1e-4
+    for f in (_abi.FIELD_X, _abi.FIELD_DENSITY, _abi.FIELD_V):
+        assert rel(gpu.field(f), ref.field(f)) < tol, f
+    assert rel(gpu.rigid_state(1)[0], ref.rigid_state(1)[0]) < tol
+    # the surface tension changes the flow (not a no-op)
+    plain = scn.small_contact_scene(precision=precision)
+    g2 = make(plain)
+    g2.step(steps)
+    assert rel(g2.field(_abi.FIELD_V), gpu.field(_abi.FIELD_V)) > 10 * tol

@@ -27,6 +27,19 @@ def test_cubic_kernel_float_bit_exact(oracle_lib, gold):
     assert np.array_equal(H, gold["float_gradGradW"])
 
 
+def test_surface_tension_kernels_bit_exact(oracle_lib, gold):
+    """Cohesion and adhesion kernels (SPHKernels.h:437-559) against the reference's own
+    compiled sources, double and float builds. At |r| = h exactly the float adhesion kernel
+    takes the 0.25 power of a slightly negative number and both give NaN (compared as equal);
+    the GPU kernel clamps that argument at zero, and neighbour pairs have |r| < h."""
+    C, A = oracle_lib.st_kernel_eval(float(gold["h"]), gold["r"])
+    assert np.array_equal(C, gold["double_cohesion"])
+    assert np.array_equal(A, gold["double_adhesion"])
+    Cf, Af = oracle_lib.st_kernel_eval(float(gold["h"]), gold["r"].astype(np.float32), single=True)
+    assert np.array_equal(Cf, gold["float_cohesion"])
+    assert np.array_equal(Af, gold["float_adhesion"], equal_nan=True)
+
+
 def test_quaternion_jacobians_bit_exact(oracle_lib, gold):
     a, b, c, d = oracle_lib.quat_eval(gold["qp"][:, :4], gold["qp"][:, 4:])
     assert np.array_equal(a, gold["double_Rqp"])
