@@ -374,6 +374,15 @@ class _SimulatorBase:
              loadFluidPos=False, loadFluidPosAndVel=False, outputDir="", param="", scene=None, precision=0):
         from .scene_json import load_scene
         self._scene = scene if scene is not None else load_scene(sceneFile, precision=precision)
+        if stateFile and (loadFluidPos or loadFluidPosAndVel):
+            # initial fluid from a saved state (SimulatorBase::init with loadFluidPos[AndVel]):
+            # the state's particles replace the scene's fluid
+            import dataclasses
+            from .partio_bgeo import read_bgeo
+            st = read_bgeo(stateFile)
+            x = st["position"].astype(np.float64)
+            v = st["velocity"].astype(np.float64) if (loadFluidPosAndVel and "velocity" in st) else np.zeros_like(x)
+            self._scene = dataclasses.replace(self._scene, fluid_x=x, fluid_v=v)
         self._stop_at = float(stopAt)
         if outputDir:
             self._output = outputDir
@@ -472,15 +481,42 @@ class _SimulatorBase:
 
     def saveState(self, path=""):
         """Snapshot of the full state kept on the device; returns a handle string usable
-        with loadStateWithRigidExisted (the reference writes .bin/.bgeo files instead)."""
+        with loadStateWithRigidExisted. When `path` is given, the fluid particles (position,
+        velocity, kappa, kappa_v, id) are also written there as
+        state_<time>_particle_Fluid.bgeo, the reference's state-export file."""
+        from . import _abi
         slot = self._sim.checkpoint_save()
         name = os.path.join(path or self._output, f"state_{slot}")
         self._saved[name] = slot
         self._saved[name + ".bin"] = slot
+        if path:
+            from .partio_bgeo import write_bgeo
+            os.makedirs(path, exist_ok=True)
+            t = self._sim.time()[0]
+            fn = os.path.join(path, f"state_{t:.6f}_particle_Fluid.bgeo")
+            write_bgeo(fn, self._sim.field(_abi.FIELD_X), velocity=self._sim.field(_abi.FIELD_V),
+                       kappa=self._sim.field(_abi.FIELD_KAPPA), kappa_v=self._sim.field(_abi.FIELD_KAPPA_V),
+                       id=np.arange(self._sim.n_fluid, dtype=np.int32))
+            self._saved[fn] = slot
         return name
 
     def loadStateWithRigidExisted(self, name):
-        self._sim.checkpoint_restore(self._saved[name])
+        """Restores a state saved in this session; a .bgeo file from elsewhere sets the fluid's
+        positions and velocities (and kappa fields when present) and keeps the rigid bodies."""
+        from . import _abi
+        if name in self._saved:
+            self._sim.checkpoint_restore(self._saved[name])
+            return
+        from .partio_bgeo import read_bgeo
+        st = read_bgeo(name)
+        if st["position"].shape[0] != self._sim.n_fluid:
+            raise ValueError(f"{name}: {st['position'].shape[0]} particles, the simulation has {self._sim.n_fluid}")
+        self._sim.set_field(_abi.FIELD_X, st["position"].astype(np.float64))
+        if "velocity" in st:
+            self._sim.set_field(_abi.FIELD_V, st["velocity"].astype(np.float64))
+        for key, fid in (("kappa", _abi.FIELD_KAPPA), ("kappa_v", _abi.FIELD_KAPPA_V)):
+            if key in st:
+                self._sim.set_field(fid, st[key].astype(np.float64).ravel())
 
     def cleanup(self):
         if self._sim is not None:

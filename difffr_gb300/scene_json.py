@@ -1,5 +1,8 @@
 """Scene JSON reader for the subset of the reference's scene format this library covers.
 
+Rigid bodies whose "geometryFile" is an OBJ file that exists are sampled from the mesh
+(difffr_gb300/mesh_sampling.py, regular triangle pattern at 1.5 r).
+
 Keys follow SPlisHSPlasH/Utilities/SceneLoader.cpp:41-200 (see the Params docstring for
 the Configuration keys). Fluid blocks are sampled as SimulatorBase::createFluidBlocks does
 for mode 0 (SimulatorBase.cpp:1638-1720: lattice at 2r starting at min + 2r,
@@ -44,6 +47,13 @@ def quat_from_axis_angle(axis, angle_deg):
     return (math.cos(h), *(math.sin(h) * a))
 
 
+def _quat_matrix(q):
+    w, x, y, z = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                     [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                     [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+
+
 def _body_samples(b, base_dir, r):
     sp = 2.0 * r
     scale = np.asarray(b.get("scale", [1.0, 1.0, 1.0]), dtype=np.float64)
@@ -52,7 +62,12 @@ def _body_samples(b, base_dir, r):
         path = pf if os.path.isabs(pf) else os.path.join(base_dir, pf)
         pts = np.load(path) if path.endswith(".npy") else np.loadtxt(path)
         return np.asarray(pts, dtype=np.float64).reshape(-1, 3) * scale[0]
-    g = os.path.basename(b.get("geometryFile", "")).lower()
+    gf = b.get("geometryFile", "")
+    gpath = gf if os.path.isabs(gf) else os.path.join(base_dir, gf)
+    if gf.lower().endswith(".obj") and os.path.exists(gpath):
+        from .mesh_sampling import sample_obj
+        return sample_obj(gpath, scale, r)
+    g = os.path.basename(gf).lower()
     if "box" in g:
         half = 0.5 * scale
         return scn.box_surface(-half, half, sp)
@@ -100,7 +115,31 @@ def load_scene(path_or_dict, precision=0, seed=0):
         steps = [int(round((hi[c] - lo[c]) / diam)) - 1 for c in range(3)]
         pts = scn.fluid_lattice(steps, diam, lo + diam, r, rng, jitter=bool(fb.get("jitter", False)))
         fluid.append(pts)
+    fvel = [np.zeros_like(b) for b in fluid]
+    for fm in data.get("FluidModels", []):
+        # particle files: the reference's readParticles (PartioReaderWriter.cpp) with the
+        # model's scale, rotation and translation
+        pf = fm.get("particleFile", "")
+        path = pf if os.path.isabs(pf) else os.path.join(base_dir, pf)
+        if path.endswith(".bgeo"):
+            from .partio_bgeo import read_bgeo
+            st = read_bgeo(path)
+            pos = st["position"].astype(np.float64)
+            vel = st["velocity"].astype(np.float64) if "velocity" in st else np.zeros_like(pos)
+        else:
+            pos = np.asarray(np.load(path) if path.endswith(".npy") else np.loadtxt(path), dtype=np.float64).reshape(-1, 3)
+            vel = np.zeros_like(pos)
+        sc_ = np.asarray(fm.get("scale", [1.0, 1.0, 1.0]), dtype=np.float64)
+        q = quat_from_axis_angle(fm.get("rotationAxis", [1, 0, 0]), float(fm.get("rotationAngle", 0.0)))
+        Rm = _quat_matrix(q)
+        pos = (pos * sc_) @ Rm.T + np.asarray(fm.get("translation", [0, 0, 0]), dtype=np.float64)
+        vel = vel @ Rm.T
+        if "initialVelocity" in fm:
+            vel = vel + np.asarray(fm["initialVelocity"], dtype=np.float64)
+        fluid.append(pos)
+        fvel.append(vel)
     fx = np.vstack(fluid) if fluid else np.zeros((0, 3))
+    fv = np.vstack(fvel) if fluid else np.zeros((0, 3))
     bodies = []
     for b in data.get("RigidBodies", []):
         q = quat_from_axis_angle(b.get("rotationAxis", [1, 0, 0]), float(b.get("rotationAngle", 0.0)))
@@ -111,7 +150,7 @@ def load_scene(path_or_dict, precision=0, seed=0):
             init_angular_velocity=tuple(b.get("initAngularVelocity", [0, 0, 0])),
             target_x=tuple(b.get("targetX", [0.8, 2.0, 0.0]))))
         bodies[-1].target_angle_in_degree = tuple(b.get("targetAngleInDegree", [0, 0, 0]))
-    sc = scn.Scene(params=params, fluid_x=fx, fluid_v=np.zeros_like(fx), bodies=bodies,
+    sc = scn.Scene(params=params, fluid_x=fx, fluid_v=fv, bodies=bodies,
                    name=os.path.basename(str(path_or_dict)))
     sc.use_rigid_gradient_manager = bool(cfg.get("useRigidGradientManager", False))
     return sc

@@ -180,3 +180,30 @@ def test_pysplishsplash_optimisation_loop(gpu_lib):
     base.singleTimeStep()
     assert np.array_equal(np.asarray(bm.get_position_rb()), s1)
     base.cleanup()
+
+
+def test_pysplishsplash_state_files(gpu_lib, tmp_path):
+    """saveState(path) writes the fluid as the reference's state_<t>_particle_Fluid.bgeo;
+    loadStateWithRigidExisted(file) sets the fluid back from it."""
+    import glob
+    from difffr_gb300.pysplishsplash import Exec
+    sc = scn.small_contact_scene(precision=_abi.DFSPH_FP32)
+    base = Exec.SimulatorBase()
+    base.init(scene=sc)
+    base.initSimulation()
+    base.singleTimeStep()
+    base.saveState(str(tmp_path))
+    files = glob.glob(str(tmp_path / "state_*_particle_Fluid.bgeo"))
+    assert len(files) == 1
+    x1 = base._sim.positions().copy()
+    v1 = base._sim.velocities().copy()
+    base.cleanup()
+    # a fresh simulator of the same scene takes the fluid from the file
+    other = Exec.SimulatorBase()
+    other.init(scene=sc)
+    other.initSimulation()
+    assert not np.allclose(other._sim.positions(), x1)
+    other.loadStateWithRigidExisted(files[0])
+    assert np.allclose(other._sim.positions(), x1, atol=1e-6)
+    assert np.allclose(other._sim.velocities(), v1, atol=1e-6)
+    other.cleanup()

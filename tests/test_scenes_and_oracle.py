@@ -176,3 +176,101 @@ def test_oracle_surface_tension_conserves_fluid_momentum(oracle_lib):
     v = o.field(_abi.FIELD_V)
     assert np.abs(v).max() > 1e-6  # the blob moves (surface tension acts)
     assert np.abs(v.sum(axis=0)).max() < 1e-9 * np.abs(v).sum()
+
+
+def _write_cube_obj(path):
+    v = [(-0.5, -0.5, 0.5), (0.5, -0.5, 0.5), (-0.5, 0.5, 0.5), (0.5, 0.5, 0.5),
+         (-0.5, 0.5, -0.5), (0.5, 0.5, -0.5), (-0.5, -0.5, -0.5), (0.5, -0.5, -0.5)]
+    quads = [(1, 2, 4, 3), (3, 4, 6, 5), (5, 6, 8, 7), (7, 8, 2, 1), (2, 8, 6, 4), (7, 1, 3, 5)]
+    with open(path, "w") as f:
+        f.write("# unit cube\n")
+        for p in v:
+            f.write("v %f %f %f\n" % p)
+        for q in quads:
+            f.write("f %d/1 %d/2 %d/3 %d/4\n" % q)
+
+
+def test_obj_regular_triangle_sampling(tmp_path):
+    from difffr_gb300.mesh_sampling import load_obj, regular_triangle_samples
+    path = tmp_path / "cube.obj"
+    _write_cube_obj(path)
+    v, f = load_obj(str(path), scale=(2.0, 1.0, 1.0))
+    assert v.shape == (8, 3) and f.shape == (12, 3)
+    assert np.allclose(v.min(0), (-1.0, -0.5, -0.5)) and np.allclose(v.max(0), (1.0, 0.5, 0.5))
+    d = 0.1
+    s = regular_triangle_samples(v, f, d)
+    # every sample lies on the box surface
+    on = np.isclose(np.abs(s[:, 0]), 1.0) | np.isclose(np.abs(s[:, 1]), 0.5) | np.isclose(np.abs(s[:, 2]), 0.5)
+    assert on.all()
+    inside = (np.abs(s[:, 0]) <= 1.0 + 1e-12) & (np.abs(s[:, 1]) <= 0.5 + 1e-12) & (np.abs(s[:, 2]) <= 0.5 + 1e-12)
+    assert inside.all()
+    # no point of the surface is farther than about d from a sample (probe a random set)
+    rng = np.random.default_rng(0)
+    probes = rng.uniform(-1, 1, size=(500, 3)) * np.array([1.0, 0.5, 0.5])
+    ax = rng.integers(0, 3, size=500)
+    probes[np.arange(500), ax] = np.sign(probes[np.arange(500), ax]) * np.array([1.0, 0.5, 0.5])[ax]
+    dist = np.min(np.linalg.norm(probes[:, None, :] - s[None, :, :], axis=2), axis=1)
+    assert dist.max() < d
+    # edges: 18 unique edges of the triangulated cube, vertices once
+    assert np.unique(np.round(s, 9), axis=0).shape[0] <= s.shape[0]
+
+
+def test_scene_json_obj_body(tmp_path):
+    path = tmp_path / "UnitBox.obj"
+    _write_cube_obj(path)
+    scene = {"Configuration": {"particleRadius": 0.02},
+             "RigidBodies": [{"geometryFile": "UnitBox.obj", "scale": [1, 1, 1], "isWall": True, "isDynamic": False}],
+             "FluidBlocks": [{"start": [-0.3, -0.3, -0.3], "end": [0.3, 0.3, 0.3]}]}
+    f = tmp_path / "s.json"
+    f.write_text(json.dumps(scene))
+    sc = load_scene(str(f))
+    b = sc.bodies[0].samples
+    assert np.all(np.max(np.abs(b), axis=1) > 0.5 - 1e-9)
+
+
+@pytest.mark.skipif(not os.path.isdir("/root/reference/experiments"), reason="reference checkout not present")
+def test_reference_scene_files_load():
+    """The reference's own scene files (read-only checkout, when present) load with their OBJ
+    bodies sampled from the meshes."""
+    base = "/root/reference/experiments/rigid_body_trajectory_optimization/scene"
+    sc = load_scene(os.path.join(base, "diff-stone-skipping.json"))
+    assert sc.params.surface_tension_method == 2 and sc.params.particle_radius == 0.015
+    assert sc.n_fluid > 100000 and len(sc.bodies) == 2
+    assert sc.bodies[1].is_dynamic and sc.bodies[1].samples.shape[0] > 100
+
+
+def test_bgeo_round_trip(tmp_path):
+    from difffr_gb300.partio_bgeo import read_bgeo, write_bgeo
+    rng = np.random.default_rng(1)
+    x = rng.normal(size=(1000, 3)).astype(np.float32)
+    v = rng.normal(size=(1000, 3)).astype(np.float32)
+    k = rng.normal(size=1000).astype(np.float32)
+    ids = np.arange(1000, dtype=np.int32)
+    p = tmp_path / "s.bgeo"
+    write_bgeo(str(p), x, velocity=v, kappa=k, id=ids)
+    d = read_bgeo(str(p))
+    assert np.array_equal(d["position"], x) and np.array_equal(d["velocity"], v)
+    assert np.array_equal(d["kappa"].ravel(), k) and np.array_equal(d["id"].ravel(), ids)
+
+
+def test_scene_json_fluid_model_from_bgeo(tmp_path):
+    from difffr_gb300.partio_bgeo import write_bgeo
+    x = np.array([[0.1, 0.2, 0.3], [0.15, 0.2, 0.3]], np.float32)
+    v = np.array([[1.0, 0.0, 0.0], [0.0, 2.0, 0.0]], np.float32)
+    write_bgeo(str(tmp_path / "fluid.bgeo"), x, velocity=v)
+    sc = load_scene({"Configuration": {"particleRadius": 0.025},
+                     "FluidModels": [{"particleFile": str(tmp_path / "fluid.bgeo"), "translation": [1, 0, 0],
+                                      "rotationAxis": [0, 0, 1], "rotationAngle": 90}]})
+    assert sc.n_fluid == 2
+    assert np.allclose(sc.fluid_x[0], [1 - 0.2, 0.1, 0.3], atol=1e-6)
+    assert np.allclose(sc.fluid_v[1], [-2.0, 0.0, 0.0], atol=1e-6)
+
+
+@pytest.mark.skipif(not os.path.isdir("/root/reference/experiments"), reason="reference checkout not present")
+def test_reference_state_file_reads():
+    from difffr_gb300.partio_bgeo import read_bgeo
+    d = read_bgeo("/root/reference/experiments/rigid_body_trajectory_optimization/state/billiards/"
+                  "state_17_particle_Fluid.bgeo")
+    assert d["position"].shape == (87374, 3) and d["velocity"].shape == (87374, 3)
+    assert {"id", "kappa", "kappa_v"} <= set(d)
+    assert np.all(np.isfinite(d["position"])) and np.abs(d["position"]).max() < 2.0
