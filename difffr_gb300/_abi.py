@@ -69,6 +69,10 @@ class DfsphParams(ctypes.Structure):
         ("surface_tension_method", c_int32),
         ("surface_tension", c_double),
         ("surface_tension_boundary", c_double),
+        ("cfl_method", c_int32),
+        ("cfl_factor", c_double),
+        ("cfl_min_time_step", c_double),
+        ("cfl_max_time_step", c_double),
     ]
 
 
@@ -110,6 +114,7 @@ class DfsphStepStats(ctypes.Structure):
         ("total_pressure_iterations", c_int64),
         ("total_divergence_iterations", c_int64),
         ("time", c_double),
+        ("time_step", c_double),
     ]
 
     def as_dict(self):

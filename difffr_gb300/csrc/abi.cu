@@ -89,6 +89,10 @@ int dfsph_default_params(dfsph_params *p) {
   p->surface_tension_method = 0;
   p->surface_tension = 0.05;
   p->surface_tension_boundary = 0.01;
+  p->cfl_method = 0;
+  p->cfl_factor = 0.5;
+  p->cfl_min_time_step = 0.0001;
+  p->cfl_max_time_step = 0.005;
   return DFSPH_OK;
 }
 

@@ -256,7 +256,7 @@ class Engine : public EngineBase {
     DBuf<int> perm;
     DBuf<BodyState> bs;
     DBuf<V4<T>> xd, vd;
-    double t = 0;
+    double t = 0, dt = 0;
     int64_t sc = 0;
     bool finished = false;
     std::vector<int> anim;
@@ -276,6 +276,8 @@ class Engine : public EngineBase {
   int64_t tape_len_ = 0, tape_cap_ = 0;
 
   // trajectory state (host)
+  double dt_cur_ = 0.0;  // the time step size (changes under CFL)
+  DBuf<unsigned long long> speed2_;  // CFL: max squared speed (bits of a non-negative double)
   double t_ = 0.0;
   int64_t step_count_ = 0;
   bool finished_ = false;
@@ -334,6 +336,8 @@ class Engine : public EngineBase {
   void compute_psi();
   void begin_step();
   void solve(bool pressure);
+  void set_dt(double h);
+  double cfl_time_step();
   void solve_impl(bool pressure);
   void launch_density(int mode, T *kappa_io, bool partials, float4 *feat = nullptr);
   void launch_mlp_warmstart(T *kap);

@@ -83,10 +83,12 @@ Engine<T>::Engine(const dfsph_scene *sc) {
   const T diam = T(2) * r;
   fc_.V = T(0.8) * diam * diam * diam;
   fc_.m = fc_.V * fc_.rho0;
-  fc_.dt = (T)P_.time_step;
-  fc_.invH = T(1) / fc_.dt;
-  fc_.invH2 = T(1) / (fc_.dt * fc_.dt);
   fc_.eps = T(1.0e-5);
+  if (!(P_.time_step > 0)) throw DfsphException(DFSPH_ERR_INVALID_ARG, "time_step must be positive");
+  if (P_.cfl_method != 0 && P_.cfl_method != 1)
+    throw DfsphException(DFSPH_ERR_UNSUPPORTED, "cfl_method: 0 (fixed) or 1 (CFL)");
+  if (P_.cfl_method == 1 && !(P_.cfl_min_time_step > 0 && P_.cfl_max_time_step >= P_.cfl_min_time_step))
+    throw DfsphException(DFSPH_ERR_INVALID_ARG, "CFL time step bounds");
   fc_.visc = (T)P_.viscosity;
   {  // Akinci2013 surface tension constants (SPHKernels.h:446-452, 516-520)
     const double hs = 4.0 * P_.particle_radius;
@@ -102,14 +104,8 @@ Engine<T>::Engine(const dfsph_scene *sc) {
   // list capacities, rounded up to whole 16-byte groups for the vector loads
   fc_.kf = ((P_.max_fluid_neighbors > 0 ? P_.max_fluid_neighbors : 96) + 3) / 4 * 4;
   fc_.kb = ((P_.max_boundary_neighbors > 0 ? P_.max_boundary_neighbors : 96) + 3) / 4 * 4;
-  // gradient coefficients: computeGradient's Real 1/dt/dt, 1/dt and the unsigned copy of :1266
-  const T cg2 = T(1) / fc_.dt / fc_.dt, cg1 = T(1) / fc_.dt;
-  pcP_.cReal = cg2;
-  pcD_.cReal = cg1;
-  pcP_.cTrunc = P_.truncate_gradient_coeff ? (T)(unsigned int)cg2 : cg2;
-  pcD_.cTrunc = P_.truncate_gradient_coeff ? (T)(unsigned int)cg1 : cg1;
   pcP_.optimize_rotation = pcD_.optimize_rotation = P_.optimize_rotation;
-  rc_.dt = (double)fc_.dt;
+  set_dt(P_.time_step);
   rc_.gx = (double)fc_.gx; rc_.gy = (double)fc_.gy; rc_.gz = (double)fc_.gz;
   rc_.gradient_mode = P_.gradient_mode;
   rc_.gyroscopic = P_.rigid_body_mode == DFSPH_RB_GYROSCOPIC;
@@ -222,6 +218,7 @@ Engine<T>::Engine(const dfsph_scene *sc) {
   for (int k = 0; k < 2; k++) { R_[k].alloc(N); kappa_[k].alloc(N); kappaV_[k].alloc(N); perm_[k].alloc(N); }
   Q_.alloc(N);
   rho_.alloc(N); alpha_.alloc(N); rhoAdv_.alloc(N); sumgrad_.alloc(N);
+  speed2_.alloc(1);
   if (P_.surface_tension_method == 2) N_.alloc(N);
   fcount_.alloc(N); bcount_.alloc(N);
   // +8 entries: a batched 16-byte load may read up to 7 entries past a short last row
@@ -415,6 +412,7 @@ void Engine<T>::reset() {
   step_count_ = 0;
   finished_ = false;
   tape_len_ = 0;
+  set_dt(P_.time_step);
   DF_CK(cudaStreamSynchronize(stream_));
 }
 
@@ -437,7 +435,7 @@ void Engine<T>::begin_step() {
   BeginCmd cmd;
   std::memset(&cmd, 0, sizeof(cmd));
   cmd.n = nb_;
-  const double uat = P_.uniform_accelerate_rb_time, dt = P_.time_step;
+  const double uat = P_.uniform_accelerate_rb_time, dt = dt_cur_;
   for (int b = 0; b < nb_; b++) {
     if (!body_dyn_[b]) { cmd.anim[b] = anim_[b]; continue; }
     if (P_.release_rigid_body_mode) {
@@ -632,6 +630,7 @@ int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
   int rc = DFSPH_OK;
   int64_t ti = 0, tv = 0;
   for (int s = 0; s < nsteps; s++) {
+    const double h_step = dt_cur_;  // the step's initial size (positions, time)
     begin_step();
     sort_fluid();
     sort_dynamic();
@@ -671,6 +670,10 @@ int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
       pend(DFSPH_K_XSPH, n_);
       // the advected state lives in the other record buffer: swap the record pair only
       std::swap(R_[cur_].p, R_[nv].p);
+      // CFL: the new step size takes effect from the pressure solve on, as in the reference
+      // (updateTimeStepSize runs after the non-pressure forces, TimeStepDiffDFSPH.cpp:583;
+      // the advection, position update and time advance keep the step's initial size)
+      if (P_.cfl_method == 1) set_dt(cfl_time_step());
       solve(true);
       if (ml_record_ && P_.use_pressure_warmstart) {
         k_ml_target<T><<<blocks(n_), 256, 0, stream_>>>(n_, kappa_[cur_].p, kfin_.p);
@@ -678,13 +681,13 @@ int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
       }
       pbegin();
       k_integrate<T><<<blocks(n_), 256, 0, stream_>>>(fc_, R_[cur_].p, kappa_[cur_].p,
-                                                      P_.use_pressure_warmstart ? 1 : 0);
+                                                      P_.use_pressure_warmstart ? 1 : 0, (T)h_step);
       launched();
       pend(DFSPH_K_INTEGRATE, n_);
     } else {
       last_iters_ = last_iters_v_ = 0;
     }
-    t_ += P_.time_step;
+    t_ += h_step;
     rigid_end();
     finished_ = t_ >= P_.target_time + P_.uniform_accelerate_rb_time;
     ti += last_iters_;
@@ -704,6 +707,7 @@ int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
     st->total_pressure_iterations = ti;
     st->total_divergence_iterations = tv;
     st->time = t_;
+    st->time_step = dt_cur_;
   }
   return rc;
 }
@@ -1037,7 +1041,7 @@ int Engine<T>::checkpoint_save() {
   DF_CK(cudaMemcpyAsync(s->xd.p, xd_.p, ND * sizeof(V4<T>), cudaMemcpyDeviceToDevice, stream_));
   DF_CK(cudaMemcpyAsync(s->vd.p, vd_.p, ND * sizeof(V4<T>), cudaMemcpyDeviceToDevice, stream_));
   DF_CK(cudaStreamSynchronize(stream_));
-  s->t = t_; s->sc = step_count_; s->finished = finished_; s->anim = anim_;
+  s->t = t_; s->sc = step_count_; s->finished = finished_; s->anim = anim_; s->dt = dt_cur_;
   for (size_t k = 0; k < snaps_.size(); k++)
     if (!snaps_[k]) { snaps_[k] = std::move(s); return (int)k; }
   snaps_.push_back(std::move(s));
@@ -1060,6 +1064,7 @@ void Engine<T>::checkpoint_restore(int slot) {
   if (nd_ > 0) DF_CK(cudaMemsetAsync(acc_.p, 0, (size_t)nd_ * ACC_STRIDE * sizeof(double), stream_));
   DF_CK(cudaStreamSynchronize(stream_));
   t_ = s.t; step_count_ = s.sc; finished_ = s.finished; anim_ = s.anim;
+  set_dt(s.dt);
 }
 
 template <class T>
@@ -1151,5 +1156,46 @@ int64_t Engine<T>::ml_capture(float *x, float *y, int64_t cap) {
   check_launch();
   DF_CK(cudaStreamSynchronize(stream_));
   return std::min<int64_t>((int64_t)last_scan + last_flag, cap);
+}
+// ----------------------------------------------------------------- time step size
+// The constants that follow from the time step (the TimeManager's size in the reference):
+// dt, 1/dt, 1/dt^2 of the passes, computeGradient's Real 1/dt/dt and 1/dt with the
+// unsigned copy of TimeStepDiffDFSPH.cpp:1266, and the rigid integration's dt.
+template <class T>
+void Engine<T>::set_dt(double h) {
+  dt_cur_ = h;
+  fc_.dt = (T)h;
+  fc_.invH = T(1) / fc_.dt;
+  fc_.invH2 = T(1) / (fc_.dt * fc_.dt);
+  const T cg2 = T(1) / fc_.dt / fc_.dt, cg1 = T(1) / fc_.dt;
+  pcP_.cReal = cg2;
+  pcD_.cReal = cg1;
+  pcP_.cTrunc = P_.truncate_gradient_coeff ? (T)(unsigned int)cg2 : cg2;
+  pcD_.cTrunc = P_.truncate_gradient_coeff ? (T)(unsigned int)cg1 : cg1;
+  rc_.dt = (double)fc_.dt;
+}
+
+// Simulation::updateTimeStepSizeCFL (Simulation.cpp:541-616): max(0.1, |v + h a|^2 over the
+// fluid, |v_j|^2 over samples of dynamic or animated bodies); h' = factor 0.4 2r / sqrt(max)
+// clamped to [min, max]. The fluid records hold v + h a once the XSPH pass has run.
+template <class T>
+double Engine<T>::cfl_time_step() {
+  DF_CK(cudaMemsetAsync(speed2_.p, 0, sizeof(unsigned long long), stream_));
+  if (n_ > 0) {
+    k_max_speed2<T><<<std::min(blocks(n_), num_sms_ * 8), 256, 0, stream_>>>(n_, R_[cur_].p, nd_, vd_.p, bodyd_.p,
+                                                                           bs_.p, speed2_.p);
+    launched();
+  }
+  unsigned long long bits = 0;
+  DF_CK(cudaMemcpyAsync(&bits, speed2_.p, sizeof(bits), cudaMemcpyDeviceToHost, stream_));
+  DF_CK(cudaStreamSynchronize(stream_));
+  double m;
+  std::memcpy(&m, &bits, sizeof(m));
+  const T maxVel = std::max((T)0.1, (T)m);
+  const T diameter = T(2) * (T)P_.particle_radius;
+  T h = (T)P_.cfl_factor * T(0.4) * (diameter / std::sqrt(maxVel));
+  h = std::min(h, (T)P_.cfl_max_time_step);
+  h = std::max(h, (T)P_.cfl_min_time_step);
+  return (double)h;
 }
 }  // namespace dfsph

@@ -578,13 +578,15 @@ static __global__ void __launch_bounds__(256) k_normals(FluidConsts<T> c, const 
   N[i] = V4<T>{c.kc.h * nx, c.kc.h * ny, c.kc.h * nz, rho[i]};
 }
 
-// x += dt v (TimeStepDiffDFSPH.cpp:613-635); kappa *= dt^2 (:752-767) when requested.
+// x += h v with the step's initial size h (TimeStepDiffDFSPH.cpp:613-635); kappa *= dt^2
+// with the current size (:752-767) when requested.
 template <class T>
-static __global__ void k_integrate(FluidConsts<T> c, Rec<T> *__restrict__ R, T *__restrict__ kappa, int scale_kappa) {
+static __global__ void k_integrate(FluidConsts<T> c, Rec<T> *__restrict__ R, T *__restrict__ kappa, int scale_kappa,
+                                   T h) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= c.n) return;
   Rec<T> r = R[i];
-  r.x.x += c.dt * r.v.x; r.x.y += c.dt * r.v.y; r.x.z += c.dt * r.v.z;
+  r.x.x += h * r.v.x; r.x.y += h * r.v.y; r.x.z += h * r.v.z;
   R[i].x = r.x;
   if (scale_kappa) kappa[i] *= c.dt * c.dt;
 }

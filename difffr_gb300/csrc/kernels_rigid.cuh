@@ -275,6 +275,36 @@ static __global__ void __launch_bounds__(128) k_pairs(FluidConsts<T> c, PairCons
   }
 }
 
+// CFL: max squared speed over the fluid records and the samples of dynamic or animated
+// bodies, folded into *out as the bits of a non-negative double (ordered like integers).
+template <class T>
+static __global__ void __launch_bounds__(256) k_max_speed2(int n, const Rec<T> *__restrict__ R, int nd,
+                                                           const V4<T> *__restrict__ vd, const int *__restrict__ bodyd,
+                                                           const BodyState *__restrict__ bs,
+                                                           unsigned long long *__restrict__ out) {
+  T m = T(0);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const V4<T> v = R[i].v;
+    const T s = sqnorm_ref(v.x, v.y, v.z);
+    m = s > m ? s : m;
+  }
+  for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < nd; d += gridDim.x * blockDim.x) {
+    const BodyState &B = bs[bodyd[d]];
+    if (!(B.dyn || B.anim)) continue;
+    const V4<T> v = vd[d];
+    const T s = sqnorm_ref(v.x, v.y, v.z);
+    m = s > m ? s : m;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const T q = __shfl_xor_sync(0xffffffffu, m, o);
+    m = q > m ? q : m;
+  }
+  if ((threadIdx.x & 31) == 0) {
+    const double md = (double)m;
+    atomicMax(out, (unsigned long long)__double_as_longlong(md));
+  }
+}
+
 // ------------------------------------------------------------------ per-body reduction
 // One block per body: sums the accumulator rows of its dynamic samples in a fixed
 // order (8 interleaved partials per value, then in order), forms the torque

@@ -54,6 +54,10 @@ class Params:
     surface_tension_method: int = 0
     surface_tension: float = 0.05
     surface_tension_boundary: float = 0.01
+    cfl_method: int = 0
+    cfl_factor: float = 0.5
+    cfl_min_time_step: float = 0.0001
+    cfl_max_time_step: float = 0.005
 
 
 @dataclass

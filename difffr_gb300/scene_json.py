@@ -34,6 +34,8 @@ CONFIG_KEYS = {
     "uniformAccelerateRBTime": "uniform_accelerate_rb_time",
     "surfaceTensionMethod": "surface_tension_method", "surfaceTension": "surface_tension",
     "surfaceTensionBoundary": "surface_tension_boundary", "viscosity": "viscosity",
+    "cflMethod": "cfl_method", "cflFactor": "cfl_factor", "cflMinTimeStepSize": "cfl_min_time_step",
+    "cflMaxTimeStepSize": "cfl_max_time_step",
 }
 
 

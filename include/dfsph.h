@@ -93,6 +93,11 @@ typedef struct dfsph_params {
                                           scene "surfaceTensionMethod"; default 0 */
   double  surface_tension;             /* "surfaceTension", default 0.05 (SurfaceTensionBase.cpp:12) */
   double  surface_tension_boundary;    /* "surfaceTensionBoundary", default 0.01 (SurfaceTensionBase.cpp:13) */
+  int32_t cfl_method;                  /* 0 fixed time_step, 1 CFL (Simulation.cpp:524-616); "cflMethod";
+                                          default 0 */
+  double  cfl_factor;                  /* "cflFactor", default 0.5 */
+  double  cfl_min_time_step;           /* "cflMinTimeStepSize", default 0.0001 */
+  double  cfl_max_time_step;           /* "cflMaxTimeStepSize", default 0.005 */
 } dfsph_params;
 
 /*
@@ -137,6 +142,7 @@ typedef struct dfsph_step_stats {
   int64_t total_pressure_iterations;   /* summed over the steps of this call */
   int64_t total_divergence_iterations;
   double  time;                        /* simulated time after the call */
+  double  time_step;                   /* time step size after the call (changes under CFL) */
 } dfsph_step_stats;
 
 /* Fluid fields for dfsph_copy_field (reference FluidModel / SimulationDataDiffDFSPH

@@ -13,6 +13,7 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(_HERE, "dfsph_oracle.cpp")
 SRCS = [SRC, os.path.join(_HERE, "mlp_oracle.cpp")]
+DEPS = SRCS + [os.path.join(_HERE, "..", "include", "dfsph.h")]  # the scene structs it reads
 LIB = os.path.join(_HERE, "_build", "liboracle_dfsph.so")
 
 MODE_F32 = 0       # <float, float>   the reference's default float build
@@ -23,7 +24,7 @@ MODE_F64 = 2       # <double, double> the reference's USE_DOUBLE build
 def build(force=False):
     """Compiles the oracle with g++ (OpenMP, no FMA contraction so x86 and Arm agree)."""
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
-    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(s) for s in SRCS):
+    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(s) for s in DEPS):
         return LIB
     cmd = ["g++", "-O3", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
            "-o", LIB, *SRCS]

@@ -410,9 +410,7 @@ struct Sim : Base {
     Vf = F(0.8) * diam * diam * diam;  // FluidModel.cpp:255-272
     mf = Vf * rho0;
     visc = (F)P.viscosity;
-    dt = (F)P.time_step;
-    invH = F(1) / dt;
-    invH2 = F(1) / (dt * dt);
+    set_dt((F)P.time_step);
     eps = F(1.0e-5);  // TimeStepDiffDFSPH.h:26
     grav = v3<F>((F)P.gravity[0], (F)P.gravity[1], (F)P.gravity[2]);
     nf = sc->n_fluid;
@@ -501,6 +499,7 @@ struct Sim : Base {
     update_boundary_particles(true);
     update_boundary_volume();
     t = 0; step_count = 0; finished = false;
+    set_dt((F)P.time_step);
     reset_gradient();
     return 0;
   }
@@ -893,6 +892,33 @@ struct Sim : Base {
     }
   }
 
+  void set_dt(F h) {
+    dt = h;
+    invH = F(1) / dt;
+    invH2 = F(1) / (dt * dt);
+  }
+
+  // Simulation::updateTimeStepSizeCFL (Simulation.cpp:541-616)
+  F cfl_time_step(F h) const {
+    F maxVel = F(0.1);
+    const F diameter = F(2.0) * r;
+    for (int64_t i = 0; i < nf; i++) {
+      const F velMag = sqnorm(V3F(v[i] + a[i] * h));
+      if (velMag > maxVel) maxVel = velMag;
+    }
+    for (const auto &B : bodies) {
+      if (!(B.dyn || B.anim)) continue;
+      for (int64_t j = B.start; j < B.start + B.count; j++) {
+        const F velMag = sqnorm(bv[j]);
+        if (velMag > maxVel) maxVel = velMag;
+      }
+    }
+    F hn = (F)P.cfl_factor * F(0.4) * (diameter / std::sqrt(maxVel));
+    hn = std::min(hn, (F)P.cfl_max_time_step);
+    hn = std::max(hn, (F)P.cfl_min_time_step);
+    return hn;
+  }
+
   void one_step() {
     begin_step();
     neighborhood_search();
@@ -949,12 +975,17 @@ struct Sim : Base {
       }
       a[i] = ai;
     }
+    // Simulation::updateTimeStepSize (Simulation.cpp:524-616, called at
+    // TimeStepDiffDFSPH.cpp:583): the new size applies to the pressure solve and the rigid
+    // step; the advection, position update and time advance keep the step's size h_step
+    const F h_step = dt;
+    if (P.cfl_method == 1) set_dt(cfl_time_step(h_step));
 #pragma omp parallel for schedule(static)
-    for (int64_t i = 0; i < nf; i++) v[i] += dt * a[i];  // :588-605
+    for (int64_t i = 0; i < nf; i++) v[i] += h_step * a[i];  // :588-605
     pressure_solve();
 #pragma omp parallel for schedule(static)
-    for (int64_t i = 0; i < nf; i++) x[i] += dt * v[i];  // :613-635
-    t += (R)dt;
+    for (int64_t i = 0; i < nf; i++) x[i] += h_step * v[i];  // :613-635
+    t += (R)h_step;
     // backwardPerStep (:493-524)
     for (auto &B : bodies) {
       if (!B.dyn || B.anim) continue;

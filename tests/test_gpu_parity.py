@@ -189,3 +189,23 @@ def test_surface_tension_akinci2013_matches_oracle(gpu_lib, oracle_lib, precisio
     g2 = make(plain)
     g2.step(steps)
     assert rel(g2.field(_abi.FIELD_V), gpu.field(_abi.FIELD_V)) > 10 * tol
+
+
+def test_cfl_time_stepping_matches_oracle(gpu_lib, oracle_lib):
+    """Adaptive CFL step size (Simulation::updateTimeStepSizeCFL): from 1 ms the size goes to
+    the 5 ms cap while the boundary samples are still at rest, then drops below it once the
+    sphere's 2.2 m/s reaches its samples; GPU (FP64) and oracle agree on the simulated time
+    (the sum of the sizes), the fields and the rigid state within 1e-9."""
+    sc = scn.small_contact_scene(precision=_abi.DFSPH_FP64, cfl_method=1, cfl_factor=0.5, cfl_max_time_step=0.005,
+                                 sphere_v=(2.0, -1.0, 0.0))
+    gpu, ref = make(sc), oracle_lib.Oracle(sc)
+    sizes = []
+    for _ in range(6):
+        st = gpu.step(1)
+        ref.step(1)
+        sizes.append(st["time_step"])
+    assert max(sizes) == sc.params.cfl_max_time_step and min(sizes) < 0.6 * sc.params.cfl_max_time_step
+    assert abs(gpu.time()[0] - ref.time()) <= 1e-12 * ref.time()
+    for f in (_abi.FIELD_X, _abi.FIELD_V, _abi.FIELD_DENSITY):
+        assert rel(gpu.field(f), ref.field(f)) < 1e-9, f
+    assert rel(gpu.rigid_state(1)[0], ref.rigid_state(1)[0]) < 1e-9
