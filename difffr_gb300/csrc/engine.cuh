@@ -241,6 +241,10 @@ class Engine : public EngineBase {
   DBuf<V4<T>> xd_, vd_, x0d_;  // dynamic, body order
   DBuf<int> bodyd_, keyD_, rankD_, orderD_, dynSortedToBody_, bfcount_, bflist_;
   DBuf<double> acc_;
+  DBuf<RedChunk> chunks_;      // per-body reduction chunks
+  DBuf<int2> body_chunks_;     // chunk range of each body
+  DBuf<double> red_part_;      // chunk partial sums
+  int nchunks_ = 0;
   DBuf<T> psi_;
   DBuf<BodyState> bs_;
   // reductions and flags

@@ -243,6 +243,23 @@ Engine<T>::Engine(const dfsph_scene *sc) {
   orderD_.alloc(ND); dynSortedToBody_.alloc(ND); bfcount_.alloc(ND); bflist_.alloc(ND * (size_t)kbf_);
   acc_.alloc(ND * ACC_STRIDE);
   bs_.alloc(std::max(nb_, 1));
+  {  // reduction chunks: RED_CHUNK consecutive samples of one dynamic body each
+    std::vector<RedChunk> ch;
+    std::vector<int2> bc(std::max(nb_, 1), make_int2(0, 0));
+    for (int b = 0; b < nb_; b++) {
+      const BodyState &B = body_init_[b];
+      bc[b].x = (int)ch.size();
+      if (B.dyn)
+        for (int d = 0; d < B.dcount; d += RED_CHUNK) ch.push_back(RedChunk{b, B.dstart + d, std::min(RED_CHUNK, B.dcount - d)});
+      bc[b].y = (int)ch.size();
+    }
+    nchunks_ = (int)ch.size();
+    chunks_.alloc(std::max<size_t>(ch.size(), 1));
+    body_chunks_.alloc(bc.size());
+    red_part_.alloc(std::max<size_t>(ch.size(), 1) * RED_VALUES);
+    if (!ch.empty()) DF_CK(cudaMemcpy(chunks_.p, ch.data(), ch.size() * sizeof(RedChunk), cudaMemcpyHostToDevice));
+    DF_CK(cudaMemcpy(body_chunks_.p, bc.data(), bc.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  }
   DF_CK(cudaMemsetAsync(BR_.p, 0, NB * sizeof(Rec<T>), stream_));
   DF_CK(cudaMemsetAsync(acc_.p, 0, ND * ACC_STRIDE * sizeof(double), stream_));
   if (nd_ > 0) {
@@ -610,7 +627,9 @@ template <class T>
 void Engine<T>::rigid_end() {
   if (nd_ == 0) return;
   pbegin();
-  k_body_reduce<T><<<nb_, RED_VALUES * RED_PARTS, 0, stream_>>>(bs_.p, nb_, xd_.p, acc_.p);
+  if (nchunks_ > 0)
+    k_body_partials<T><<<nchunks_, RED_THREADS, 0, stream_>>>(bs_.p, chunks_.p, xd_.p, acc_.p, red_part_.p);
+  k_body_final<<<nb_, RED_THREADS, 0, stream_>>>(bs_.p, nb_, body_chunks_.p, red_part_.p);
   double *tape_step = nullptr;
   if (P_.enable_gradient) {
     if (tape_len_ >= tape_cap_) grow_tape();
@@ -619,7 +638,7 @@ void Engine<T>::rigid_end() {
   }
   k_rigid_step<<<nb_, 128, 0, stream_>>>(bs_.p, nb_, rc_, tape_step);
   k_boundary_update<T><<<blocks(nd_), 256, 0, stream_>>>(bs_.p, nd_, x0d_.p, bodyd_.p, xd_.p, vd_.p, 1);
-  launched(3);
+  launched(nchunks_ > 0 ? 4 : 3);
   pend(DFSPH_K_RIGID, nd_);
   check_launch();
 }

@@ -306,65 +306,65 @@ static __global__ void __launch_bounds__(256) k_max_speed2(int n, const Rec<T> *
 }
 
 // ------------------------------------------------------------------ per-body reduction
-// One block per body: sums the accumulator rows of its dynamic samples in a fixed
-// order (8 interleaved partials per value, then in order), forms the torque
-// sum (x_j - x_b) x F_j, stores F, T and the net Jacobians, and zeroes the rows
+// Sums the accumulator rows of every dynamic body's samples in a fixed order, forms the
+// torque sum (x_j - x_b) x F_j, stores F, T and the net Jacobians, and zeroes the rows
 // (BoundaryModel_Akinci2012::accumulate_and_reset_gradient, :453-497;
 // BoundaryModel::getForceAndTorque / clearForceAndTorque, BoundaryModel.cpp:38-85).
+// Two stages so that many SMs share the reads: k_body_partials sums each chunk of
+// RED_CHUNK consecutive samples of one body in sample order; k_body_final sums a body's
+// chunk partials in chunk order.
 constexpr int RED_VALUES = 3 + NJAC + 3;  // force, jacobians, torque
-constexpr int RED_PARTS = 8;
+constexpr int RED_CHUNK = 16;
+constexpr int RED_THREADS = 128;
+static_assert(RED_VALUES <= RED_THREADS, "one thread per reduced value");
+struct RedChunk {
+  int body, start, count;
+};
 
 template <class T>
-static __global__ void __launch_bounds__(RED_VALUES * RED_PARTS) k_body_reduce(BodyState *__restrict__ bs, int nbodies,
-                                                                        const V4<T> *__restrict__ xd,
-                                                                        double *__restrict__ acc) {
-  __shared__ double part[RED_VALUES * RED_PARTS];
+static __global__ void __launch_bounds__(RED_THREADS) k_body_partials(const BodyState *__restrict__ bs,
+                                                                      const RedChunk *__restrict__ chunks,
+                                                                      const V4<T> *__restrict__ xd,
+                                                                      double *__restrict__ acc,
+                                                                      double *__restrict__ part) {
+  const RedChunk ch = chunks[blockIdx.x];
+  const BodyState &B = bs[ch.body];
+  const int v = threadIdx.x;
+  if (v < RED_VALUES) {
+    double s = 0.0;
+    if (v < 3 + NJAC) {
+      for (int d = ch.start; d < ch.start + ch.count; d++) s += acc[(size_t)d * ACC_STRIDE + v];
+    } else {
+      const int comp = v - 3 - NJAC;
+      for (int d = ch.start; d < ch.start + ch.count; d++) {
+        const double *row = acc + (size_t)d * ACC_STRIDE;
+        const V4<T> xj = xd[d];
+        const double rx = (double)xj.x - B.x[0], ry = (double)xj.y - B.x[1], rz = (double)xj.z - B.x[2];
+        const double fx = row[0], fy = row[1], fz = row[2];
+        s += comp == 0 ? ry * fz - rz * fy : (comp == 1 ? rz * fx - rx * fz : rx * fy - ry * fx);
+      }
+    }
+    part[(size_t)blockIdx.x * RED_VALUES + v] = s;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < ch.count * ACC_STRIDE; k += blockDim.x) acc[(size_t)ch.start * ACC_STRIDE + k] = 0.0;
+}
+
+static __global__ void __launch_bounds__(RED_THREADS) k_body_final(BodyState *__restrict__ bs, int nbodies,
+                                                                   const int2 *__restrict__ body_chunks,
+                                                                   const double *__restrict__ part) {
   const int b = blockIdx.x;
   if (b >= nbodies) return;
   BodyState &B = bs[b];
   if (!B.dyn) return;
-  const int t = threadIdx.x;
-  const int val = t / RED_PARTS, p = t % RED_PARTS;
-  double s = 0.0;
-  if (val < RED_VALUES) {
-    // the rows d = dstart + p, + RED_PARTS, ... are summed in this order; UNROLL of them
-    // are loaded before their additions so the loads overlap
-    constexpr int UNROLL = 8;
-    const int dend = B.dstart + B.dcount;
-    for (int d0 = B.dstart + p; d0 < dend; d0 += UNROLL * RED_PARTS) {
-      double t[UNROLL];
-#pragma unroll
-      for (int u = 0; u < UNROLL; u++) {
-        const int d = d0 + u * RED_PARTS;
-        t[u] = 0.0;
-        if (d < dend) {
-          const double *row = acc + (size_t)d * ACC_STRIDE;
-          if (val < 3 + NJAC) t[u] = row[val];
-          else {
-            const V4<T> xj = xd[d];
-            const double rx = (double)xj.x - B.x[0], ry = (double)xj.y - B.x[1], rz = (double)xj.z - B.x[2];
-            const double fx = row[0], fy = row[1], fz = row[2];
-            const int comp = val - 3 - NJAC;
-            t[u] = comp == 0 ? ry * fz - rz * fy : (comp == 1 ? rz * fx - rx * fz : rx * fy - ry * fx);
-          }
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < UNROLL; u++)
-        if (d0 + u * RED_PARTS < dend) s += t[u];
-    }
-  }
-  part[t] = s;
-  __syncthreads();
-  if (p == 0 && val < RED_VALUES) {
-    double tot = 0.0;
-    for (int k = 0; k < RED_PARTS; k++) tot += part[val * RED_PARTS + k];
-    if (val < 3) B.F[val] = tot;
-    else if (val < 3 + NJAC) B.nets[val - 3] = tot;
-    else B.T[val - 3 - NJAC] = tot;
-  }
-  __syncthreads();
-  for (int k = t; k < B.dcount * ACC_STRIDE; k += blockDim.x) acc[(size_t)B.dstart * ACC_STRIDE + k] = 0.0;
+  const int v = threadIdx.x;
+  if (v >= RED_VALUES) return;
+  const int2 r = body_chunks[b];
+  double tot = 0.0;
+  for (int c = r.x; c < r.y; c++) tot += part[(size_t)c * RED_VALUES + v];
+  if (v < 3) B.F[v] = tot;
+  else if (v < 3 + NJAC) B.nets[v - 3] = tot;
+  else B.T[v - 3 - NJAC] = tot;
 }
 
 // ------------------------------------------------------------------ chain rule + integration (FP64)
