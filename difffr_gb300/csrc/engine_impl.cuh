@@ -574,7 +574,8 @@ void Engine<T>::solve_impl(bool pressure) {
   const int im = pressure ? PASS_PRESSURE : PASS_DIVERGENCE;
   if (warm) {
     const bool ml = pressure && (ml_record_ || ml_on_);
-    launch_density(wm, kap, false, ml ? F_.p : nullptr);
+    // the divergence warm start's density pass ran inside the list build
+    if (pressure) launch_density(wm, kap, false, ml ? F_.p : nullptr);
     if (pressure && ml_on_) launch_mlp_warmstart(kap);
     launch_pairs(pressure, true, false);
     launch_velocity(nullptr);
@@ -654,11 +655,20 @@ int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
     sort_fluid();
     sort_dynamic();
     if (n_ > 0) {
-      { pbegin(); k_lists_density_factor<T><<<blocks(n_, LIST_THREADS), LIST_THREADS, 0, stream_>>>(fc_, R_[cur_].p, cstartF_.p,
-                                                                 BR_.p, cstartS_.p, nd_ ? cstartD_.p : nullptr, ns_,
-                                                                 flist_.p, fcount_.p, blist_.p, bcount_.p, rho_.p,
-                                                                 alpha_.p, sumgrad_.p, err_.p);
-        launched(); pend(DFSPH_K_LISTS_DENSITY, n_); }
+      {
+        // the divergence solve's warm-start density change is computed by the list build
+        const bool divwarm = P_.enable_divergence_solver && P_.use_divergence_warmstart;
+        pbegin();
+#define DF_LISTS(W)                                                                                                \
+  k_lists_density_factor<T, W><<<blocks(n_, LIST_THREADS), LIST_THREADS, 0, stream_>>>(                            \
+      fc_, R_[cur_].p, cstartF_.p, BR_.p, cstartS_.p, nd_ ? cstartD_.p : nullptr, ns_, flist_.p, fcount_.p, blist_.p, \
+      bcount_.p, rho_.p, alpha_.p, sumgrad_.p, err_.p, Q_.p, rhoAdv_.p, kappaV_[cur_].p)
+        if (divwarm) DF_LISTS(true);
+        else DF_LISTS(false);
+#undef DF_LISTS
+        launched();
+        pend(DFSPH_K_LISTS_DENSITY, n_);
+      }
       if (nd_) {
         pbegin();
         k_bf_lists<T><<<blocks(nd_), 256, 0, stream_>>>(fc_, nd_, xd_.p, R_[cur_].p, cstartF_.p, kbf_, bflist_.p,

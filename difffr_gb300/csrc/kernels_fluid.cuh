@@ -166,20 +166,27 @@ static __device__ __forceinline__ void for_each_row(const Grid<T> &g, const int 
 // Neighbour lists (fluid and boundary), density (TimeStep.cpp:147-200) and the
 // DFSPH factor with sum_grad_p_k (TimeStepDiffDFSPH.cpp:883-962), fused in one pass.
 // Also stores the XSPH weight m_i / rho_i in v[i].w for the viscosity pass.
+// DIVWARM: also the divergence solve's warm start (what k_density_pass does in
+// PASS_DIVERGENCE_WARM, :1698-1788 with :1977-2041): the density change over the same
+// neighbours in the same order, rho_dot = 0 below 20 neighbours, kappaV = 0.5 max(kappaV,
+// -0.5) / h where rho_dot > 0, and Q[i] = (x_i, kappaV) for the warm-start correction.
 constexpr int LIST_THREADS = 256;
-template <class T>
+template <class T, bool DIVWARM>
 static __global__ void __launch_bounds__(LIST_THREADS) k_lists_density_factor(
     FluidConsts<T> c, Rec<T> *__restrict__ R, const int *__restrict__ cstartF,
     const Rec<T> *__restrict__ BR, const int *__restrict__ cstartS, const int *__restrict__ cstartD, int ns,
     int *__restrict__ flist, int *__restrict__ fcount, int *__restrict__ blist, int *__restrict__ bcount,
-    T *__restrict__ rho, T *__restrict__ alpha, V4<T> *__restrict__ sumgrad, int *__restrict__ err) {
+    T *__restrict__ rho, T *__restrict__ alpha, V4<T> *__restrict__ sumgrad, int *__restrict__ err,
+    V4<T> *__restrict__ Q, T *__restrict__ rhoAdv, T *__restrict__ kappaV) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= c.n) return;
-  const V4<T> xi = R[i].x;
+  const Rec<T> ri = ld_rec(R + i);
+  const V4<T> xi = ri.x, vi = ri.v;
   int cx, cy, cz;
   grid_cell(c.grid, xi.x, xi.y, xi.z, cx, cy, cz);
   T dens = c.V * c.kc.w0;
   T sgk = T(0);
+  T delta = T(0);
   V3<T> gpi = {T(0), T(0), T(0)};
   int cnt = 0;
   for_each_row(c.grid, cstartF, cx, cy, cz, [&](int b, int e) {
@@ -202,6 +209,10 @@ static __global__ void __launch_bounds__(LIST_THREADS) k_lists_density_factor(
           const V3<T> gpj = (-c.V) * V3<T>{g * dx, g * dy, g * dz};
           sgk += dot(gpj, gpj);
           gpi = gpi - gpj;
+          if (DIVWARM) {  // the velocity only for accepted neighbours
+            const V4<T> vj = R[j].v;
+            delta += c.V * (g * ((vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz));
+          }
         }
       }
     }
@@ -221,6 +232,10 @@ static __global__ void __launch_bounds__(LIST_THREADS) k_lists_density_factor(
         const T g = KEval<T>::G(d2, c.kc);
         const V3<T> gpj = (-xj.w) * V3<T>{g * dx, g * dy, g * dz};
         gpi = gpi - gpj;
+        if (DIVWARM) {
+          const V4<T> vj = BR[off + j].v;
+          delta += xj.w * (g * ((vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz));
+        }
       }
     }
   };
@@ -234,6 +249,15 @@ static __global__ void __launch_bounds__(LIST_THREADS) k_lists_density_factor(
   sumgrad[i] = V4<T>{-gpi.x, -gpi.y, -gpi.z, T(0)};
   sgk += dot(gpi, gpi);
   alpha[i] = (sgk > c.eps) ? -T(1) / sgk : T(0);
+  if (DIVWARM) {
+    T ra = delta > T(0) ? delta : T(0);
+    if (cnt + bc < 20) ra = T(0);
+    rhoAdv[i] = ra;
+    const T kp = kappaV[i];
+    const T kq = (ra > T(0)) ? T(0.5) * (kp > T(-0.5) ? kp : T(-0.5)) * c.invH : T(0);
+    kappaV[i] = kq;
+    Q[i] = V4<T>{xi.x, xi.y, xi.z, kq};
+  }
 }
 
 // Fluid neighbours of each dynamic boundary sample (body order).
