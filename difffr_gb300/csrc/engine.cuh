@@ -281,6 +281,7 @@ class Engine : public EngineBase {
 
   // trajectory state (host)
   double dt_cur_ = 0.0;  // the time step size (changes under CFL)
+  bool xs_fuse_ = false, xs_done_ = false;  // XSPH advanced by the divergence solve's last pass
   DBuf<unsigned long long> speed2_;  // CFL: max squared speed (bits of a non-negative double)
   double t_ = 0.0;
   int64_t step_count_ = 0;

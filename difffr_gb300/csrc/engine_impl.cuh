@@ -510,14 +510,20 @@ void Engine<T>::launch_density(int mode, T *kappa_io, bool partials, float4 *fea
   const int nbk = blocks(n_ * LPP);
   double *pp = partials ? partials_.p : nullptr;
   pbegin();
-#define DF_DENS(M)                                                                                                \
-  k_density_pass<T, M><<<nbk, 256, 0, stream_>>>(fc_, R_[cur_].p, Q_.p, BR_.p, flist_.p, fcount_.p, blist_.p,           \
-                                                 bcount_.p, rho_.p, alpha_.p, rhoAdv_.p, kappa_io, pp, feat)
+#define DF_DENS(M, XS)                                                                                             \
+  k_density_pass<T, M, XS><<<nbk, 256, 0, stream_>>>(fc_, R_[cur_].p, Q_.p, BR_.p, flist_.p, fcount_.p, blist_.p,       \
+                                                     bcount_.p, rho_.p, alpha_.p, rhoAdv_.p, kappa_io, pp, feat,      \
+                                                     R_[1 - cur_].p)
+  // the divergence solve's checked passes also advance the XSPH phase (see k_density_pass)
+  const bool xs = mode == PASS_DIVERGENCE && partials && xs_fuse_;
   switch (mode) {
-    case PASS_PRESSURE: DF_DENS(PASS_PRESSURE); break;
-    case PASS_DIVERGENCE: DF_DENS(PASS_DIVERGENCE); break;
-    case PASS_PRESSURE_WARM: DF_DENS(PASS_PRESSURE_WARM); break;
-    default: DF_DENS(PASS_DIVERGENCE_WARM); break;
+    case PASS_PRESSURE: DF_DENS(PASS_PRESSURE, false); break;
+    case PASS_DIVERGENCE:
+      if (xs) { DF_DENS(PASS_DIVERGENCE, true); xs_done_ = true; }
+      else DF_DENS(PASS_DIVERGENCE, false);
+      break;
+    case PASS_PRESSURE_WARM: DF_DENS(PASS_PRESSURE_WARM, false); break;
+    default: DF_DENS(PASS_DIVERGENCE_WARM, false); break;
   }
 #undef DF_DENS
   launched();
@@ -677,12 +683,14 @@ int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
         pend(DFSPH_K_BF_LISTS, nd_);
       }
       check_launch();
+      xs_fuse_ = P_.surface_tension_method != 2;
+      xs_done_ = false;
       if (P_.enable_divergence_solver) solve(false);
       else { last_iters_v_ = 0; last_err_v_ = 0.0; }
       const int nv = 1 - cur_;
+      const int scale_kv = (P_.enable_divergence_solver && P_.use_divergence_warmstart) ? 1 : 0;
       pbegin();
-      {
-        const int scale_kv = (P_.enable_divergence_solver && P_.use_divergence_warmstart) ? 1 : 0;
+      if (!xs_done_) {
         if (P_.surface_tension_method == 2) {
           k_normals<T><<<blocks(n_), 256, 0, stream_>>>(fc_, R_[cur_].p, flist_.p, fcount_.p, rho_.p, N_.p);
           k_xsph_advect<T, true><<<blocks(n_ * LPP), 256, 0, stream_>>>(fc_, R_[cur_].p, R_[nv].p, flist_.p,
@@ -694,8 +702,8 @@ int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
                                                                          fcount_.p, kappaV_[cur_].p, scale_kv, nullptr,
                                                                          nullptr, nullptr, nullptr);
         }
+        launched();
       }
-      launched();
       pend(DFSPH_K_XSPH, n_);
       // the advected state lives in the other record buffer: swap the record pair only
       std::swap(R_[cur_].p, R_[nv].p);
@@ -710,7 +718,8 @@ int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
       }
       pbegin();
       k_integrate<T><<<blocks(n_), 256, 0, stream_>>>(fc_, R_[cur_].p, kappa_[cur_].p,
-                                                      P_.use_pressure_warmstart ? 1 : 0, (T)h_step);
+                                                      P_.use_pressure_warmstart ? 1 : 0, (T)h_step,
+                                                      (xs_done_ && scale_kv) ? kappaV_[cur_].p : nullptr, (T)h_step);
       launched();
       pend(DFSPH_K_INTEGRATE, n_);
     } else {

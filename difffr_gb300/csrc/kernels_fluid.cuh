@@ -403,27 +403,40 @@ template <class T> static __device__ __forceinline__ T sub_sum(T v) {
 // velocity correction, and the block partials of the solver residual.
 // Reads R (positions, velocities); writes Q[i] = (x_i, k_i): the next velocity pass
 // gathers position and stiffness of a neighbour with one 16-byte load.
-template <class T, int MODE>
+// XS (divergence passes only): the same neighbour records also give the XSPH viscosity
+// and gravity of the next phase (k_xsph_advect's arithmetic, in its order); the advected
+// records go to R_out. Once the divergence solve's last check passes, R_out holds the
+// state the separate XSPH pass would have produced.
+template <class T, int MODE, bool XS = false>
 static __global__ void __launch_bounds__(256, DFSPH_DENSITY_MIN_BLOCKS) k_density_pass(
     FluidConsts<T> c, const Rec<T> *__restrict__ R, V4<T> *__restrict__ Q, const Rec<T> *__restrict__ BR,
     const int *__restrict__ flist, const int *__restrict__ fcount, const int *__restrict__ blist,
     const int *__restrict__ bcount, const T *__restrict__ rho, const T *__restrict__ alpha, T *__restrict__ rhoAdv,
-    T *__restrict__ kappa_io, double *__restrict__ partials, float4 *__restrict__ feat) {
+    T *__restrict__ kappa_io, double *__restrict__ partials, float4 *__restrict__ feat, Rec<T> *__restrict__ R_out) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = t / LPP, s = t % LPP;
   const bool live = i < c.n;
   double e = 0.0;
   T delta = T(0);
+  T ax = T(0), ay = T(0), az = T(0);
   int nf = 0, nb = 0;
   Rec<T> ri;
   if (live) {
     ri = ld_rec(R + i);
     const V4<T> xi = ri.x, vi4 = ri.v;
+    const T cvis = c.invH * c.visc;
     nf = fcount[i];
     for_neighbors_sub<DFSPH_DENSITY_BATCH, Rec<T>>(nf, flist, c.n, i, s, [&](int j) { return ld_rec(R + j); }, [&](const Rec<T> &d) {
       const T rx = xi.x - d.x.x, ry = xi.y - d.x.y, rz = xi.z - d.x.z;
       const T g = KEval<T>::G(rx * rx + ry * ry + rz * rz, c.kc);
       delta += c.V * (g * ((vi4.x - d.v.x) * rx + (vi4.y - d.v.y) * ry + (vi4.z - d.v.z) * rz));
+      if (XS) {
+        const T w = KEval<T>::W(rx * rx + ry * ry + rz * rz, c.kc);
+        const T f = cvis * d.v.w;
+        ax -= f * (vi4.x - d.v.x) * w;
+        ay -= f * (vi4.y - d.v.y) * w;
+        az -= f * (vi4.z - d.v.z) * w;
+      }
     });
     nb = bcount[i];
     for_neighbors_sub<DFSPH_DENSITY_BATCH, Rec<T>>(nb, blist, c.n, i, s, [&](int j) { return ld_rec(BR + j); }, [&](const Rec<T> &d) {
@@ -465,6 +478,11 @@ static __global__ void __launch_bounds__(256, DFSPH_DENSITY_MIN_BLOCKS) k_densit
       kappa_io[i] = kq;
     }
     Q[i] = V4<T>{ri.x.x, ri.x.y, ri.x.z, kq};
+    if (XS) {
+      const V4<T> vi = ri.v;
+      ax += c.gx; ay += c.gy; az += c.gz;
+      R_out[i] = Rec<T>{ri.x, V4<T>{vi.x + c.dt * ax, vi.y + c.dt * ay, vi.z + c.dt * az, vi.w}};
+    }
   }
   if (partials) block_partial_sum(e, partials);
 }
@@ -604,11 +622,15 @@ static __global__ void __launch_bounds__(256) k_normals(FluidConsts<T> c, const 
 
 // x += h v with the step's initial size h (TimeStepDiffDFSPH.cpp:613-635); kappa *= dt^2
 // with the current size (:752-767) when requested.
+// kappaV *= h_div (the end of the divergence solve, :870-880) when the XSPH pass was
+// fused into the divergence solve's last density pass (kappaV is next read by the next
+// step's warm start).
 template <class T>
 static __global__ void k_integrate(FluidConsts<T> c, Rec<T> *__restrict__ R, T *__restrict__ kappa, int scale_kappa,
-                                   T h) {
+                                   T h, T *__restrict__ kappaV, T h_div) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= c.n) return;
+  if (kappaV) kappaV[i] *= h_div;
   Rec<T> r = R[i];
   r.x.x += h * r.v.x; r.x.y += h * r.v.y; r.x.z += h * r.v.z;
   R[i].x = r.x;
