@@ -186,7 +186,7 @@ class Engine : public EngineBase {
   void counts(int64_t *nf, int64_t *nb) override { *nf = n_; *nb = ns_ + nd_; }
   void neighbors(int which, int64_t *start, int32_t *idx, int64_t *total) override;
   void get_time(double *t, int64_t *sc) override { *t = t_; *sc = step_count_; }
-  void synchronize() override { DF_CK(cudaStreamSynchronize(stream_)); }
+  void synchronize() override { sync_all(); }
   int64_t launches() override { return launches_; }
   void record_event(int slot) override;
   double event_elapsed(int a, int b) override;
@@ -212,6 +212,9 @@ class Engine : public EngineBase {
   int n_ = 0, ns_ = 0, nd_ = 0, nb_ = 0, kbf_ = 128;
   int ncell_ = 0;
   cudaStream_t stream_ = nullptr;
+  cudaStream_t stream2_ = nullptr;  // rigid kernels (overlap the next step's fluid sort)
+  cudaEvent_t ev_fluid_done_ = nullptr, ev_rigid_done_ = nullptr;
+  bool rigid_pending_ = false;
   int64_t launches_ = 0;
 
   // host copies
@@ -304,17 +307,28 @@ class Engine : public EngineBase {
     if (pool_.empty()) { cudaEvent_t e; DF_CK(cudaEventCreate(&e)); return e; }
     cudaEvent_t e = pool_.back(); pool_.pop_back(); return e;
   }
-  void pbegin() {
+  void pbegin(cudaStream_t s = nullptr) {
     if (!prof_on_) return;
     open_ev_ = take_event();
-    DF_CK(cudaEventRecord(open_ev_, stream_));
+    DF_CK(cudaEventRecord(open_ev_, s ? s : stream_));
   }
-  void pend(int k, int64_t units) {
+  void pend(int k, int64_t units, cudaStream_t s = nullptr) {
     if (!prof_on_ || !open_ev_) return;
     cudaEvent_t b = take_event();
-    DF_CK(cudaEventRecord(b, stream_));
+    DF_CK(cudaEventRecord(b, s ? s : stream_));
     pending_.push_back({k, open_ev_, b, units});
     open_ev_ = nullptr;
+  }
+  // the rigid kernels' stream: the main stream waits for them before it touches rigid
+  // data; host synchronisation waits for both
+  void wait_rigid() {
+    if (!rigid_pending_) return;
+    DF_CK(cudaStreamWaitEvent(stream_, ev_rigid_done_, 0));
+    rigid_pending_ = false;
+  }
+  void sync_all() {
+    wait_rigid();
+    DF_CK(cudaStreamSynchronize(stream_));
   }
   void resolve_profile();
   // phase timers (a whole solve); independent of the per-launch pair above

@@ -203,6 +203,9 @@ Engine<T>::Engine(const dfsph_scene *sc) {
   ncell_ = fc_.grid.nx * fc_.grid.ny * fc_.grid.nz;
 
   DF_CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  DF_CK(cudaStreamCreateWithFlags(&stream2_, cudaStreamNonBlocking));
+  DF_CK(cudaEventCreateWithFlags(&ev_fluid_done_, cudaEventDisableTiming));
+  DF_CK(cudaEventCreateWithFlags(&ev_rigid_done_, cudaEventDisableTiming));
   {
     int dev = 0;
     DF_CK(cudaGetDevice(&dev));
@@ -282,7 +285,7 @@ Engine<T>::Engine(const dfsph_scene *sc) {
     sort_points(tmp.p, 1, ns_, k1.p, k2.p, cstartS_.p, k3.p);
     std::vector<int> order(ns_);
     DF_CK(cudaMemcpyAsync(order.data(), k3.p, ns_ * sizeof(int), cudaMemcpyDeviceToHost, stream_));
-    DF_CK(cudaStreamSynchronize(stream_));
+    sync_all();
     std::vector<V4<T>> sorted(ns_);
     static_orig_.resize(ns_);
     for (int s = 0; s < ns_; s++) {
@@ -294,7 +297,7 @@ Engine<T>::Engine(const dfsph_scene *sc) {
     std::vector<Rec<T>> srec(ns_);
     for (int q = 0; q < ns_; q++) srec[q] = Rec<T>{sorted[q], V4<T>{T(0), T(0), T(0), T(0)}};
     DF_CK(cudaMemcpyAsync(BR_.p, srec.data(), ns_ * sizeof(Rec<T>), cudaMemcpyHostToDevice, stream_));
-    DF_CK(cudaStreamSynchronize(stream_));
+    sync_all();
   } else {
     // keep the empty table's scan consistent (all zero)
   }
@@ -307,7 +310,11 @@ Engine<T>::Engine(const dfsph_scene *sc) {
 
 template <class T>
 Engine<T>::~Engine() {
+  if (stream2_) cudaStreamSynchronize(stream2_);
   if (stream_) cudaStreamSynchronize(stream_);
+  if (ev_fluid_done_) cudaEventDestroy(ev_fluid_done_);
+  if (ev_rigid_done_) cudaEventDestroy(ev_rigid_done_);
+  if (stream2_) cudaStreamDestroy(stream2_);
   for (auto &e : ev_) if (e) cudaEventDestroy(e);
   for (auto &r : pending_) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
   for (auto &e : pool_) cudaEventDestroy(e);
@@ -379,7 +386,7 @@ void Engine<T>::upload_fluid_initial() {
     }
     R_init_.alloc(n_);
     DF_CK(cudaMemcpyAsync(R_init_.p, rh.data(), n_ * sizeof(Rec<T>), cudaMemcpyHostToDevice, stream_));
-    DF_CK(cudaStreamSynchronize(stream_));
+    sync_all();
   }
   DF_CK(cudaMemcpyAsync(R_[0].p, R_init_.p, n_ * sizeof(Rec<T>), cudaMemcpyDeviceToDevice, stream_));
   // perm[1] must also be a valid permutation before the first gather
@@ -394,25 +401,25 @@ void Engine<T>::upload_fluid_initial() {
   DF_CK(cudaMemsetAsync(fcount_.p, 0, n_ * sizeof(int), stream_));
   DF_CK(cudaMemsetAsync(bcount_.p, 0, n_ * sizeof(int), stream_));
   check_launch();
-  DF_CK(cudaStreamSynchronize(stream_));
+  sync_all();
 }
 template <class T>
 void Engine<T>::body_state_download(std::vector<BodyState> &out) {
   out.resize(nb_);
   if (nb_ == 0) return;
-  DF_CK(cudaStreamSynchronize(stream_));
+  sync_all();
   DF_CK(cudaMemcpy(out.data(), bs_.p, nb_ * sizeof(BodyState), cudaMemcpyDeviceToHost));
 }
 template <class T>
 void Engine<T>::body_state_upload(const std::vector<BodyState> &in) {
   if (nb_ == 0) return;
   DF_CK(cudaMemcpyAsync(bs_.p, in.data(), nb_ * sizeof(BodyState), cudaMemcpyHostToDevice, stream_));
-  DF_CK(cudaStreamSynchronize(stream_));
+  sync_all();
 }
 
 template <class T>
 void Engine<T>::reset() {
-  DF_CK(cudaStreamSynchronize(stream_));
+  sync_all();
   upload_fluid_initial();
   std::vector<BodyState> bsv = body_init_;  // pose x0/q0, v = omega = 0 (Dynamic3dRigidBody::reset)
   anim_ = body_anim0_;
@@ -430,7 +437,7 @@ void Engine<T>::reset() {
   finished_ = false;
   tape_len_ = 0;
   set_dt(P_.time_step);
-  DF_CK(cudaStreamSynchronize(stream_));
+  sync_all();
 }
 
 template <class T>
@@ -441,7 +448,7 @@ void Engine<T>::reset_gradient() {
   body_state_upload(bsv);
   if (nd_ > 0) DF_CK(cudaMemsetAsync(acc_.p, 0, (size_t)nd_ * ACC_STRIDE * sizeof(double), stream_));
   tape_len_ = 0;
-  DF_CK(cudaStreamSynchronize(stream_));
+  sync_all();
 }
 
 // TimeStepDiffDFSPH::beginStep (:353-430)
@@ -484,7 +491,7 @@ void Engine<T>::begin_step() {
 
 template <class T>
 double Engine<T>::read_residual() {
-  DF_CK(cudaStreamSynchronize(stream_));
+  sync_all();
   const int e = (int)resid_host_[1];
   if (e) check_error_word();
   return resid_host_[0];
@@ -616,13 +623,14 @@ void Engine<T>::solve_impl(bool pressure) {
 
 template <class T>
 void Engine<T>::grow_tape() {
+  wait_rigid();  // earlier steps' tape rows are written on the rigid stream
   const int64_t ncap = std::max<int64_t>(tape_cap_ * 2, 256);
   DBuf<double> nt;
   nt.alloc((size_t)ncap * nb_ * NSTATE * NSTATE);
   if (tape_len_ > 0)
     DF_CK(cudaMemcpyAsync(nt.p, tape_.p, (size_t)tape_len_ * nb_ * NSTATE * NSTATE * sizeof(double),
                           cudaMemcpyDeviceToDevice, stream_));
-  DF_CK(cudaStreamSynchronize(stream_));
+  sync_all();
   std::swap(tape_.p, nt.p);
   std::swap(tape_.n, nt.n);
   tape_cap_ = ncap;
@@ -631,22 +639,29 @@ void Engine<T>::grow_tape() {
 // backwardPerStep's chain rule (:493-524) + velocityTimeStep + positionTimeStep +
 // updateBoundaryParticles, all on the device.
 template <class T>
+// The rigid kernels run on a second stream after the fluid's integration, so that they
+// overlap the next step's fluid sort (which touches no rigid data); every later use of
+// rigid data on the main stream, and every host synchronisation, waits for them.
 void Engine<T>::rigid_end() {
   if (nd_ == 0) return;
-  pbegin();
-  if (nchunks_ > 0)
-    k_body_partials<T><<<nchunks_, RED_THREADS, 0, stream_>>>(bs_.p, chunks_.p, xd_.p, acc_.p, red_part_.p);
-  k_body_final<<<nb_, RED_THREADS, 0, stream_>>>(bs_.p, nb_, body_chunks_.p, red_part_.p);
   double *tape_step = nullptr;
   if (P_.enable_gradient) {
     if (tape_len_ >= tape_cap_) grow_tape();
     tape_step = tape_.p + (size_t)tape_len_ * nb_ * NSTATE * NSTATE;
     tape_len_++;
   }
-  k_rigid_step<<<nb_, 128, 0, stream_>>>(bs_.p, nb_, rc_, tape_step);
-  k_boundary_update<T><<<blocks(nd_), 256, 0, stream_>>>(bs_.p, nd_, x0d_.p, bodyd_.p, xd_.p, vd_.p, 1);
+  DF_CK(cudaEventRecord(ev_fluid_done_, stream_));
+  DF_CK(cudaStreamWaitEvent(stream2_, ev_fluid_done_, 0));
+  pbegin(stream2_);
+  if (nchunks_ > 0)
+    k_body_partials<T><<<nchunks_, RED_THREADS, 0, stream2_>>>(bs_.p, chunks_.p, xd_.p, acc_.p, red_part_.p);
+  k_body_final<<<nb_, RED_THREADS, 0, stream2_>>>(bs_.p, nb_, body_chunks_.p, red_part_.p);
+  k_rigid_step<<<nb_, 128, 0, stream2_>>>(bs_.p, nb_, rc_, tape_step);
+  k_boundary_update<T><<<blocks(nd_), 256, 0, stream2_>>>(bs_.p, nd_, x0d_.p, bodyd_.p, xd_.p, vd_.p, 1);
   launched(nchunks_ > 0 ? 4 : 3);
-  pend(DFSPH_K_RIGID, nd_);
+  pend(DFSPH_K_RIGID, nd_, stream2_);
+  DF_CK(cudaEventRecord(ev_rigid_done_, stream2_));
+  rigid_pending_ = true;
   check_launch();
 }
 
@@ -657,8 +672,9 @@ int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
   int64_t ti = 0, tv = 0;
   for (int s = 0; s < nsteps; s++) {
     const double h_step = dt_cur_;  // the step's initial size (positions, time)
+    sort_fluid();  // overlaps the previous step's rigid kernels
+    wait_rigid();
     begin_step();
-    sort_fluid();
     sort_dynamic();
     if (n_ > 0) {
       {
@@ -733,7 +749,7 @@ int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
     if (last_iters_ >= P_.max_iterations || (P_.enable_divergence_solver && last_iters_v_ >= P_.max_iterations_v))
       rc = DFSPH_ERR_NOT_CONVERGED;
   }
-  DF_CK(cudaStreamSynchronize(stream_));
+  sync_all();
   check_error_word();
   if (st) {
     st->steps_done = nsteps;
@@ -765,7 +781,7 @@ template <class T>
 void Engine<T>::get_rigid_state(int b, double *x, double *q, double *v, double *w) {
   if (b < 0 || b >= nb_) throw DfsphException(DFSPH_ERR_INVALID_ARG, "body index");
   BodyState B;
-  DF_CK(cudaStreamSynchronize(stream_));
+  sync_all();
   DF_CK(cudaMemcpy(&B, bs_.p + b, sizeof(BodyState), cudaMemcpyDeviceToHost));
   for (int k = 0; k < 3; k++) { if (x) x[k] = B.x[k]; if (v) v[k] = B.v[k]; if (w) w[k] = B.w[k]; }
   if (q) for (int k = 0; k < 4; k++) q[k] = B.q[k];
@@ -780,7 +796,7 @@ void Engine<T>::set_rigid_velocity(int b, const double *v, const double *w) {
   if (nd_ > 0) {
     k_boundary_update<T><<<blocks(nd_), 256, 0, stream_>>>(bs_.p, nd_, x0d_.p, bodyd_.p, xd_.p, vd_.p, 1);
     launched();
-    DF_CK(cudaStreamSynchronize(stream_));
+    sync_all();
   }
 }
 template <class T>
@@ -828,11 +844,12 @@ void Engine<T>::backward(const double *dL, double *out) {
     li.alloc(lam.size());
     lo.alloc(lam.size());
     DF_CK(cudaMemcpyAsync(li.p, lam.data(), lam.size() * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    wait_rigid();
     k_backward<<<nb_, 32, 0, stream_>>>(tape_.p, (int)tape_len_, nb_, li.p, lo.p);
     launched();
     check_launch();
     DF_CK(cudaMemcpyAsync(res.data(), lo.p, res.size() * sizeof(double), cudaMemcpyDeviceToHost, stream_));
-    DF_CK(cudaStreamSynchronize(stream_));
+    sync_all();
   } else {
     res = lam;
   }
@@ -842,7 +859,7 @@ void Engine<T>::backward(const double *dL, double *out) {
 
 template <class T>
 void Engine<T>::copy_field(int f, double *dst, int64_t n) {
-  DF_CK(cudaStreamSynchronize(stream_));
+  sync_all();
   const bool bfield = f == DFSPH_FIELD_BOUNDARY_X || f == DFSPH_FIELD_BOUNDARY_V || f == DFSPH_FIELD_BOUNDARY_PSI;
   const int comps = (f == DFSPH_FIELD_X || f == DFSPH_FIELD_V || f == DFSPH_FIELD_SUM_GRAD_P ||
                      f == DFSPH_FIELD_BOUNDARY_X || f == DFSPH_FIELD_BOUNDARY_V) ? 3 : 1;
@@ -896,7 +913,7 @@ void Engine<T>::copy_field(int f, double *dst, int64_t n) {
 
 template <class T>
 void Engine<T>::set_field(int f, const double *src, int64_t n) {
-  DF_CK(cudaStreamSynchronize(stream_));
+  sync_all();
   const int comps = (f == DFSPH_FIELD_X || f == DFSPH_FIELD_V) ? 3 : 1;
   if (!(f == DFSPH_FIELD_X || f == DFSPH_FIELD_V || f == DFSPH_FIELD_KAPPA || f == DFSPH_FIELD_KAPPA_V))
     throw DfsphException(DFSPH_ERR_INVALID_ARG, "field is not settable");
@@ -923,7 +940,7 @@ void Engine<T>::set_field(int f, const double *src, int64_t n) {
 
 template <class T>
 void Engine<T>::neighbors(int which, int64_t *start, int32_t *idx, int64_t *total) {
-  DF_CK(cudaStreamSynchronize(stream_));
+  sync_all();
   if (step_count_ == 0) throw DfsphException(DFSPH_ERR_STATE, "no neighbour search has run yet");
   std::vector<std::vector<int32_t>> rows;
   std::vector<int> perm(std::max(n_, 1));
@@ -1005,7 +1022,7 @@ double Engine<T>::event_elapsed(int a, int b) {
 template <class T>
 void Engine<T>::resolve_profile() {
   if (pending_.empty()) return;
-  DF_CK(cudaStreamSynchronize(stream_));
+  sync_all();
   for (auto &r : pending_) {
     float ms = 0.f;
     DF_CK(cudaEventElapsedTime(&ms, r.a, r.b));
@@ -1050,7 +1067,7 @@ void Engine<T>::set_rigid_state(int b, const double *x, const double *q, const d
   if (nd_ > 0) {
     k_boundary_update<T><<<blocks(nd_), 256, 0, stream_>>>(bs_.p, nd_, x0d_.p, bodyd_.p, xd_.p, vd_.p, 1);
     launched();
-    DF_CK(cudaStreamSynchronize(stream_));
+    sync_all();
   }
 }
 
@@ -1066,7 +1083,7 @@ void Engine<T>::set_gradient_enabled(bool on) {
 
 template <class T>
 int Engine<T>::checkpoint_save() {
-  DF_CK(cudaStreamSynchronize(stream_));
+  sync_all();
   std::unique_ptr<Snap> s(new Snap());
   const size_t N = std::max(n_, 1), ND = std::max(nd_, 1), NBd = std::max(nb_, 1);
   s->R.alloc(N); s->kap.alloc(N); s->kapV.alloc(N); s->perm.alloc(N);
@@ -1078,7 +1095,7 @@ int Engine<T>::checkpoint_save() {
   DF_CK(cudaMemcpyAsync(s->bs.p, bs_.p, NBd * sizeof(BodyState), cudaMemcpyDeviceToDevice, stream_));
   DF_CK(cudaMemcpyAsync(s->xd.p, xd_.p, ND * sizeof(V4<T>), cudaMemcpyDeviceToDevice, stream_));
   DF_CK(cudaMemcpyAsync(s->vd.p, vd_.p, ND * sizeof(V4<T>), cudaMemcpyDeviceToDevice, stream_));
-  DF_CK(cudaStreamSynchronize(stream_));
+  sync_all();
   s->t = t_; s->sc = step_count_; s->finished = finished_; s->anim = anim_; s->dt = dt_cur_;
   for (size_t k = 0; k < snaps_.size(); k++)
     if (!snaps_[k]) { snaps_[k] = std::move(s); return (int)k; }
@@ -1091,7 +1108,7 @@ void Engine<T>::checkpoint_restore(int slot) {
   if (slot < 0 || slot >= (int)snaps_.size() || !snaps_[slot]) throw DfsphException(DFSPH_ERR_INVALID_ARG, "checkpoint slot");
   Snap &s = *snaps_[slot];
   const size_t N = std::max(n_, 1), ND = std::max(nd_, 1), NBd = std::max(nb_, 1);
-  DF_CK(cudaStreamSynchronize(stream_));
+  sync_all();
   DF_CK(cudaMemcpyAsync(R_[cur_].p, s.R.p, N * sizeof(Rec<T>), cudaMemcpyDeviceToDevice, stream_));
   DF_CK(cudaMemcpyAsync(kappa_[cur_].p, s.kap.p, N * sizeof(T), cudaMemcpyDeviceToDevice, stream_));
   DF_CK(cudaMemcpyAsync(kappaV_[cur_].p, s.kapV.p, N * sizeof(T), cudaMemcpyDeviceToDevice, stream_));
@@ -1100,7 +1117,7 @@ void Engine<T>::checkpoint_restore(int slot) {
   DF_CK(cudaMemcpyAsync(xd_.p, s.xd.p, ND * sizeof(V4<T>), cudaMemcpyDeviceToDevice, stream_));
   DF_CK(cudaMemcpyAsync(vd_.p, s.vd.p, ND * sizeof(V4<T>), cudaMemcpyDeviceToDevice, stream_));
   if (nd_ > 0) DF_CK(cudaMemsetAsync(acc_.p, 0, (size_t)nd_ * ACC_STRIDE * sizeof(double), stream_));
-  DF_CK(cudaStreamSynchronize(stream_));
+  sync_all();
   t_ = s.t; step_count_ = s.sc; finished_ = s.finished; anim_ = s.anim;
   set_dt(s.dt);
 }
@@ -1108,7 +1125,7 @@ void Engine<T>::checkpoint_restore(int slot) {
 template <class T>
 void Engine<T>::checkpoint_free(int slot) {
   if (slot < 0 || slot >= (int)snaps_.size() || !snaps_[slot]) throw DfsphException(DFSPH_ERR_INVALID_ARG, "checkpoint slot");
-  DF_CK(cudaStreamSynchronize(stream_));
+  sync_all();
   snaps_[slot].reset();
 }
 
@@ -1124,11 +1141,12 @@ void Engine<T>::adjoint_sweep(const double *lam_in, double *lam_out) {
   li.alloc(m);
   lo.alloc(m);
   DF_CK(cudaMemcpyAsync(li.p, lam_in, (size_t)NSTATE * nb_ * sizeof(double), cudaMemcpyHostToDevice, stream_));
+  wait_rigid();
   k_backward<<<nb_, 32, 0, stream_>>>(tape_.p, (int)tape_len_, nb_, li.p, lo.p);
   launched();
   check_launch();
   DF_CK(cudaMemcpyAsync(lam_out, lo.p, (size_t)NSTATE * nb_ * sizeof(double), cudaMemcpyDeviceToHost, stream_));
-  DF_CK(cudaStreamSynchronize(stream_));
+  sync_all();
 }
 // ----------------------------------------------------------------- learned warm start
 template <class T>
@@ -1192,7 +1210,7 @@ int64_t Engine<T>::ml_capture(float *x, float *y, int64_t cap) {
   k_ml_scatter<<<blocks(n_), 256, 0, stream_>>>(n_, F_.p, kfin_.p, mlflag_.p, cap, x, y);
   launched();
   check_launch();
-  DF_CK(cudaStreamSynchronize(stream_));
+  sync_all();
   return std::min<int64_t>((int64_t)last_scan + last_flag, cap);
 }
 // ----------------------------------------------------------------- time step size
@@ -1226,7 +1244,7 @@ double Engine<T>::cfl_time_step() {
   }
   unsigned long long bits = 0;
   DF_CK(cudaMemcpyAsync(&bits, speed2_.p, sizeof(bits), cudaMemcpyDeviceToHost, stream_));
-  DF_CK(cudaStreamSynchronize(stream_));
+  sync_all();
   double m;
   std::memcpy(&m, &bits, sizeof(m));
   const T maxVel = std::max((T)0.1, (T)m);
