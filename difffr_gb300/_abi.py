@@ -73,6 +73,12 @@ class DfsphParams(ctypes.Structure):
         ("cfl_factor", c_double),
         ("cfl_min_time_step", c_double),
         ("cfl_max_time_step", c_double),
+        ("use_rigid_contact_solver", c_int32),
+        ("use_rigid_gradient_manager", c_int32),
+        ("rigid_contact_gamma", c_double),
+        ("rigid_contact_beta", c_double),
+        ("rigid_contact_support_radius_factor", c_double),
+        ("rigid_contact_friction_coeff", c_double),
     ]
 
 
@@ -212,6 +218,9 @@ def load_library(path: str | None = None):
         "dfsph_get_rigid_mass": ([vp, c_int32, POINTER(c_double), POINTER(c_double)], c_int32),
         "dfsph_get_rigid_grad": ([vp, c_int32, POINTER(c_double)], c_int32),
         "dfsph_get_net_jacobians": ([vp, c_int32, POINTER(c_double)], c_int32),
+        "dfsph_get_manager_grad": ([vp, c_int32, c_int32, POINTER(c_double)], c_int32),
+        "dfsph_get_manager_jacobians": ([vp, c_int32, c_int32, POINTER(c_double)], c_int32),
+        "dfsph_get_contact_count": ([vp, POINTER(c_int64), POINTER(c_int64)], c_int32),
         "dfsph_reset_gradient": ([vp], c_int32),
         "dfsph_backward": ([vp, POINTER(c_double), POINTER(c_double)], c_int32),
         "dfsph_tape_length": ([vp, POINTER(c_int64)], c_int32),
@@ -269,6 +278,7 @@ EXPORTED_SYMBOLS = (
     "dfsph_mlp_create", "dfsph_mlp_destroy", "dfsph_mlp_get_params", "dfsph_mlp_set_params",
     "dfsph_mlp_fit_normalization", "dfsph_mlp_train_step", "dfsph_mlp_gradient", "dfsph_mlp_predict",
     "dfsph_set_warmstart_model", "dfsph_ml_record", "dfsph_ml_capture",
+    "dfsph_get_manager_grad", "dfsph_get_manager_jacobians", "dfsph_get_contact_count",
 )
 KERNEL_CLASSES = ("sort", "lists_density_factor", "bf_lists", "density_pass", "velocity_pass",
                   "xsph_advect", "integrate", "pairs", "rigid", "mlp")

@@ -6,8 +6,10 @@ velocity from ``init_params`` (n_bodies x 6: v0, omega0), resets the simulation,
 omega) as a tensor that autograd differentiates with respect to ``init_params``.
 
 The derivative is the reference's gradient chain (the per-step rigid Jacobian blocks of
-the selected gradient mode, BoundaryModel_Akinci2012::perform_chain_rule), applied in
-reverse over the recorded step matrices. Two schedules:
+the selected gradient mode, BoundaryModel_Akinci2012::perform_chain_rule; with the
+gradient manager on, RigidBodyGradientManager's chain over body pairs, which couples the
+bodies through the contact solver's blocks), applied in reverse over the recorded step
+matrices. Two schedules:
 
 * direct (``checkpoint_every=None``): the forward pass accumulates the pair Jacobians
   and records one 13x13 matrix per body and step; the backward pass is one reverse sweep.
@@ -59,6 +61,9 @@ class DiffDFSPHRollout(torch.autograd.Function):
         sim = ctx.sim
         lam = grad_out.detach().to("cpu", torch.float64).numpy().reshape(sim.n_bodies, 13)
         if ctx.segments:
+            mgr = sim.uses_manager
+            if mgr:  # the manager's v0 and omega0 columns have separate step maps
+                lam = np.stack([lam, lam])
             sim.set_gradient_enabled(True)
             for slot, n in reversed(ctx.segments):
                 sim.checkpoint_restore(slot)
@@ -67,7 +72,7 @@ class DiffDFSPHRollout(torch.autograd.Function):
                 lam = sim.adjoint_sweep(lam)
                 sim.checkpoint_free(slot)
             ctx.segments = []
-            g = lam[:, 7:13]
+            g = np.concatenate([lam[0][:, 7:10], lam[1][:, 10:13]], axis=1) if mgr else lam[:, 7:13]
         else:
             g = sim.backward(lam)
         return torch.as_tensor(np.ascontiguousarray(g), dtype=ctx.dtype, device=ctx.device), None, None, None

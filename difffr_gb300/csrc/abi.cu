@@ -93,6 +93,12 @@ int dfsph_default_params(dfsph_params *p) {
   p->cfl_factor = 0.5;
   p->cfl_min_time_step = 0.0001;
   p->cfl_max_time_step = 0.005;
+  p->use_rigid_contact_solver = 0;
+  p->use_rigid_gradient_manager = 0;
+  p->rigid_contact_gamma = 0.7;
+  p->rigid_contact_beta = 1.0;
+  p->rigid_contact_support_radius_factor = 4.0;
+  p->rigid_contact_friction_coeff = 0.0;
   return DFSPH_OK;
 }
 
@@ -215,6 +221,33 @@ int dfsph_get_net_jacobians(dfsph_ctx *ctx, int32_t body, double out[78]) {
     valid(ctx);
     if (!out) throw DfsphException(DFSPH_ERR_INVALID_ARG, "NULL output");
     ctx->engine->get_net_jacobians(body, out);
+    return DFSPH_OK;
+  });
+}
+
+int dfsph_get_manager_grad(dfsph_ctx *ctx, int32_t body, int32_t body2, double out[78]) {
+  return guard([&] {
+    valid(ctx);
+    if (!out) throw DfsphException(DFSPH_ERR_INVALID_ARG, "NULL output");
+    ctx->engine->get_manager_grad(body, body2, out);
+    return DFSPH_OK;
+  });
+}
+
+int dfsph_get_manager_jacobians(dfsph_ctx *ctx, int32_t body, int32_t body2, double out[78]) {
+  return guard([&] {
+    valid(ctx);
+    if (!out) throw DfsphException(DFSPH_ERR_INVALID_ARG, "NULL output");
+    ctx->engine->get_manager_jacobians(body, body2, out);
+    return DFSPH_OK;
+  });
+}
+
+int dfsph_get_contact_count(dfsph_ctx *ctx, int64_t *n_contact, int64_t *n_active) {
+  return guard([&] {
+    valid(ctx);
+    if (!n_contact || !n_active) throw DfsphException(DFSPH_ERR_INVALID_ARG, "NULL output");
+    ctx->engine->contact_count(n_contact, n_active);
     return DFSPH_OK;
   });
 }

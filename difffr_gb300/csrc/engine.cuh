@@ -17,6 +17,7 @@
 #include "common.cuh"
 #include "kernels_fluid.cuh"
 #include "kernels_rigid.cuh"
+#include "kernels_contact.cuh"
 #include "kernels_mlp.cuh"
 
 namespace dfsph {
@@ -202,6 +203,9 @@ class Engine : public EngineBase {
   void set_warmstart_model(const MlpView *v) override;
   void ml_record(bool on) override;
   int64_t ml_capture(float *x, float *y, int64_t cap) override;
+  void get_manager_grad(int b, int b2, double *out) override;
+  void get_manager_jacobians(int b, int b2, double *out) override;
+  void contact_count(int64_t *nc, int64_t *na) override;
 
  private:
   // configuration
@@ -263,6 +267,7 @@ class Engine : public EngineBase {
     DBuf<int> perm;
     DBuf<BodyState> bs;
     DBuf<V4<T>> xd, vd;
+    DBuf<double> mgrM, mgrS;
     double t = 0, dt = 0;
     int64_t sc = 0;
     bool finished = false;
@@ -278,9 +283,24 @@ class Engine : public EngineBase {
   DBuf<int> mlflag_;
   Scanner mlscan_;
   int num_sms_ = 152;
-  // adjoint tape
+  // adjoint tape: per step nb 13x13 maps (per-body chain) or two 13nb x 13nb maps (manager)
   DBuf<double> tape_;
   int64_t tape_len_ = 0, tape_cap_ = 0;
+  size_t tape_stride() const {
+    return manager_ ? (size_t)2 * NSTATE * nb_ * NSTATE * nb_ : (size_t)nb_ * NSTATE * NSTATE;
+  }
+  // rigid-rigid contact (penalty form) and the gradient manager's multi-body chain
+  bool contact_ = false, manager_ = false;
+  ContactConsts cc_;
+  DBuf<int> bodyS_;            // body of each static sample (sorted order)
+  DBuf<V4<T>> x0S_;            // local coordinates of each static sample (sorted order)
+  DBuf<double> cvol0S_, cdens0S_, cvol0D_, cdens0D_;  // rest volume / density (static sorted, dynamic body order)
+  DBuf<ContactRec> crec_;
+  DBuf<double> cblk_;
+  DBuf<int> clist_, ccount_;
+  DBuf<double> Mc_, mgrM_, mgrS_;  // contact blocks of the step, manager blocks, manager chain state
+  void contact_init();
+  void manager_reset(bool blocks);
 
   // trajectory state (host)
   double dt_cur_ = 0.0;  // the time step size (changes under CFL)

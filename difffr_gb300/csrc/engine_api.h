@@ -63,6 +63,9 @@ class EngineBase {
   virtual void set_warmstart_model(const MlpView *v) = 0;
   virtual void ml_record(bool on) = 0;
   virtual int64_t ml_capture(float *x, float *y, int64_t cap) = 0;
+  virtual void get_manager_grad(int b, int b2, double *out) = 0;
+  virtual void get_manager_jacobians(int b, int b2, double *out) = 0;
+  virtual void contact_count(int64_t *nc, int64_t *na) = 0;
 };
 
 EngineBase *make_engine_fp32(const dfsph_scene *sc);

@@ -111,12 +111,34 @@ Engine<T>::Engine(const dfsph_scene *sc) {
   rc_.gyroscopic = P_.rigid_body_mode == DFSPH_RB_GYROSCOPIC;
   rc_.optimize_rotation = P_.optimize_rotation;
   rc_.enable_gradient = P_.enable_gradient;
+  contact_ = P_.use_rigid_contact_solver != 0;
+  manager_ = P_.use_rigid_gradient_manager != 0;
+  rc_.manager = manager_ ? 1 : 0;
+  rc_.nbodies = nb_;
+  if (contact_) {
+    if (!(P_.rigid_contact_support_radius_factor > 0) || !(P_.rigid_contact_gamma > 0))
+      throw DfsphException(DFSPH_ERR_INVALID_ARG, "rigid contact support radius factor and gamma must be positive");
+    const double sr = P_.rigid_contact_support_radius_factor * P_.particle_radius;
+    const double s3 = sr * sr * sr;
+    cc_.kc.h = sr; cc_.kc.k = 8.0 / (M_PI * s3); cc_.kc.l = 48.0 / (M_PI * s3); cc_.kc.w0 = cc_.kc.k; cc_.kc.invh = 1.0 / sr;
+    const double hh = (double)h, h3d = hh * hh * hh;
+    cc_.kh.h = hh; cc_.kh.k = 8.0 / (M_PI * h3d); cc_.kh.l = 48.0 / (M_PI * h3d); cc_.kh.w0 = cc_.kh.k; cc_.kh.invh = 1.0 / hh;
+    cc_.beta = P_.rigid_contact_beta;
+    cc_.mu = P_.rigid_contact_friction_coeff;
+    cc_.gx = rc_.gx; cc_.gy = rc_.gy; cc_.gz = rc_.gz;
+    cc_.dt = rc_.dt;
+    // the contact blocks are carried forward even with gradients off: the next step's
+    // fluid stage reads them, and a checkpoint must hold them for an exact replay
+    cc_.grad = manager_ ? 1 : 0;
+  }
 
   // ---- bodies (mass model of Dynamic3dRigidBody::determineMassProperties, :184-213)
   std::vector<double> static_world;  // xyz
   std::vector<int> static_orig_unsorted;
   std::vector<double> dyn_local;
   std::vector<int> dyn_body;
+  std::vector<int> bnd_body;       // boundary index -> body
+  std::vector<double> bnd_local;   // boundary index -> local coordinates (as T)
   int boundary_index = 0;
   const double rr = (double)r;
   for (int b = 0; b < nb_; b++) {
@@ -147,6 +169,10 @@ Engine<T>::Engine(const dfsph_scene *sc) {
     body_anim0_.push_back(B.anim);
     init_v_.insert(init_v_.end(), d.init_velocity, d.init_velocity + 3);
     init_w_.insert(init_w_.end(), d.init_angular_velocity, d.init_angular_velocity + 3);
+    for (int s = 0; s < d.n_samples; s++) {
+      bnd_body.push_back(b);
+      for (int k = 0; k < 3; k++) bnd_local.push_back((double)(T)d.samples[3 * s + k]);
+    }
     if (B.dyn) {
       B.dstart = nd_;
       B.dcount = (int)d.n_samples;
@@ -297,15 +323,82 @@ Engine<T>::Engine(const dfsph_scene *sc) {
     std::vector<Rec<T>> srec(ns_);
     for (int q = 0; q < ns_; q++) srec[q] = Rec<T>{sorted[q], V4<T>{T(0), T(0), T(0), T(0)}};
     DF_CK(cudaMemcpyAsync(BR_.p, srec.data(), ns_ * sizeof(Rec<T>), cudaMemcpyHostToDevice, stream_));
+    if (contact_) {
+      std::vector<int> bs_h(ns_);
+      std::vector<V4<T>> x0s_h(ns_);
+      for (int q = 0; q < ns_; q++) {
+        const int o = static_orig_[q];
+        bs_h[q] = bnd_body[o];
+        x0s_h[q] = V4<T>{(T)bnd_local[3 * o], (T)bnd_local[3 * o + 1], (T)bnd_local[3 * o + 2], T(0)};
+      }
+      bodyS_.alloc(ns_); x0S_.alloc(ns_);
+      DF_CK(cudaMemcpyAsync(bodyS_.p, bs_h.data(), ns_ * sizeof(int), cudaMemcpyHostToDevice, stream_));
+      DF_CK(cudaMemcpyAsync(x0S_.p, x0s_h.data(), ns_ * sizeof(V4<T>), cudaMemcpyHostToDevice, stream_));
+    }
     sync_all();
   } else {
     // keep the empty table's scan consistent (all zero)
   }
+  if (contact_) {
+    if (!bodyS_.p) { bodyS_.alloc(1); x0S_.alloc(1); }
+    cvol0S_.alloc(std::max(ns_, 1)); cdens0S_.alloc(std::max(ns_, 1));
+    cvol0D_.alloc(ND); cdens0D_.alloc(ND);
+    crec_.alloc(ND); clist_.alloc(ND);
+    if (manager_) cblk_.alloc(ND * (size_t)CONTACT_BLK);
+  }
+  ccount_.alloc(2 * (size_t)std::max(nb_, 1));
+  DF_CK(cudaMemsetAsync(ccount_.p, 0, 2 * (size_t)std::max(nb_, 1) * sizeof(int), stream_));
+  if (manager_) {
+    const size_t nbb = (size_t)std::max(nb_, 1);
+    Mc_.alloc(nbb * nbb * NJAC);
+    mgrM_.alloc(nbb * nbb * NJAC);
+    mgrS_.alloc((size_t)NSTATE * nbb * 6 * nbb);
+  }
   if (nd_ > 0 && P_.enable_gradient) {
     tape_cap_ = 256;
-    tape_.alloc((size_t)tape_cap_ * nb_ * NSTATE * NSTATE);
+    tape_.alloc((size_t)tape_cap_ * tape_stride());
   }
   reset();
+  if (contact_) contact_init();
+}
+
+// RigidContactSolver::RigidContactSolver (RigidContactSolver.cpp:23-262): rest volume and
+// rest density of every boundary sample, once, from the positions after the first reset.
+template <class T>
+void Engine<T>::contact_init() {
+  if (ns_ + nd_ == 0) return;
+  for (int phase = 0; phase < 2; phase++) {
+    k_contact_rest<T><<<blocks(ns_ + nd_), 256, 0, stream_>>>(
+        cc_, fc_.grid, fc_.h2, ns_, nd_, BR_.p, cstartS_.p, nd_ ? cstartD_.p : nullptr, bodyS_.p,
+        nd_ ? bodyd_.p : nullptr, nd_ ? dynSortedToBody_.p : nullptr, P_.rigid_contact_gamma, phase, cvol0S_.p,
+        cvol0D_.p, cdens0S_.p, cdens0D_.p);
+    launched();
+  }
+  check_launch();
+  sync_all();
+}
+
+// RigidBodyGradientManager::reset (RigidBodyGradientManager.cpp:477-524): identity in the
+// v / omega slots of each body's own columns; with blocks == true also zero blocks (a full
+// reset). The blocks are kept by dfsph_reset_gradient because the next step's fluid stage
+// reads the last contact blocks, so that a segment replayed from a checkpoint maps exactly
+// as it did in the first run.
+template <class T>
+void Engine<T>::manager_reset(bool blocks) {
+  if (!manager_ || nb_ == 0) return;
+  const size_t ncol = 6 * (size_t)nb_, nrow = (size_t)NSTATE * nb_;
+  std::vector<double> S(nrow * ncol, 0.0);
+  for (int a = 0; a < nb_; a++)
+    for (int j = 0; j < 3; j++) {
+      S[((size_t)NSTATE * a + 7 + j) * ncol + 6 * a + j] = 1.0;
+      S[((size_t)NSTATE * a + 10 + j) * ncol + 6 * a + 3 + j] = 1.0;
+    }
+  DF_CK(cudaMemcpyAsync(mgrS_.p, S.data(), S.size() * sizeof(double), cudaMemcpyHostToDevice, stream_));
+  if (blocks) {
+    DF_CK(cudaMemsetAsync(mgrM_.p, 0, (size_t)nb_ * nb_ * NJAC * sizeof(double), stream_));
+    DF_CK(cudaMemsetAsync(Mc_.p, 0, (size_t)nb_ * nb_ * NJAC * sizeof(double), stream_));
+  }
+  sync_all();
 }
 
 template <class T>
@@ -437,6 +530,7 @@ void Engine<T>::reset() {
   finished_ = false;
   tape_len_ = 0;
   set_dt(P_.time_step);
+  manager_reset(true);
   sync_all();
 }
 
@@ -448,6 +542,7 @@ void Engine<T>::reset_gradient() {
   body_state_upload(bsv);
   if (nd_ > 0) DF_CK(cudaMemsetAsync(acc_.p, 0, (size_t)nd_ * ACC_STRIDE * sizeof(double), stream_));
   tape_len_ = 0;
+  manager_reset(false);
   sync_all();
 }
 
@@ -626,9 +721,9 @@ void Engine<T>::grow_tape() {
   wait_rigid();  // earlier steps' tape rows are written on the rigid stream
   const int64_t ncap = std::max<int64_t>(tape_cap_ * 2, 256);
   DBuf<double> nt;
-  nt.alloc((size_t)ncap * nb_ * NSTATE * NSTATE);
+  nt.alloc((size_t)ncap * tape_stride());
   if (tape_len_ > 0)
-    DF_CK(cudaMemcpyAsync(nt.p, tape_.p, (size_t)tape_len_ * nb_ * NSTATE * NSTATE * sizeof(double),
+    DF_CK(cudaMemcpyAsync(nt.p, tape_.p, (size_t)tape_len_ * tape_stride() * sizeof(double),
                           cudaMemcpyDeviceToDevice, stream_));
   sync_all();
   std::swap(tape_.p, nt.p);
@@ -647,18 +742,44 @@ void Engine<T>::rigid_end() {
   double *tape_step = nullptr;
   if (P_.enable_gradient) {
     if (tape_len_ >= tape_cap_) grow_tape();
-    tape_step = tape_.p + (size_t)tape_len_ * nb_ * NSTATE * NSTATE;
+    tape_step = tape_.p + (size_t)tape_len_ * tape_stride();
     tape_len_++;
   }
+  const bool mgr_chain = manager_ && P_.enable_gradient;
+  const bool mgr_blocks = manager_ && contact_;
   DF_CK(cudaEventRecord(ev_fluid_done_, stream_));
   DF_CK(cudaStreamWaitEvent(stream2_, ev_fluid_done_, 0));
   pbegin(stream2_);
-  if (nchunks_ > 0)
+  int nl = 0;
+  if (nchunks_ > 0) {
     k_body_partials<T><<<nchunks_, RED_THREADS, 0, stream2_>>>(bs_.p, chunks_.p, xd_.p, acc_.p, red_part_.p);
+    nl++;
+  }
   k_body_final<<<nb_, RED_THREADS, 0, stream2_>>>(bs_.p, nb_, body_chunks_.p, red_part_.p);
-  k_rigid_step<<<nb_, 128, 0, stream2_>>>(bs_.p, nb_, rc_, tape_step);
+  nl++;
+  ContactStep cs{nullptr, nullptr, nullptr, ccount_.p, nullptr};
+  if (contact_) {
+    cc_.dt = rc_.dt;
+    cc_.grad = manager_ ? 1 : 0;
+    // samples of the dynamic bodies against every boundary sample; the dynamic cell table
+    // is this step's (the samples have not moved since sort_dynamic)
+    k_contact_samples<T><<<blocks(nd_, 128), 128, 0, stream2_>>>(
+        cc_, fc_.grid, fc_.h2, ns_, nd_, bs_.p, BR_.p, cstartS_.p, cstartD_.p, bodyS_.p, x0S_.p, bodyd_.p,
+        dynSortedToBody_.p, xd_.p, x0d_.p, cvol0S_.p, cvol0D_.p, cdens0D_.p, crec_.p, cc_.grad ? cblk_.p : nullptr);
+    nl++;
+    cs.rec = crec_.p;
+    cs.list = clist_.p;
+    if (mgr_blocks) { cs.blk = cblk_.p; cs.Mc = Mc_.p; }
+  }
+  k_rigid_step<<<nb_, 128, 0, stream2_>>>(bs_.p, nb_, rc_, manager_ ? nullptr : tape_step, cs);
+  nl++;
+  if (mgr_chain || mgr_blocks) {
+    MgrConsts mc{rc_.dt, nb_, rc_.gyroscopic, n_ > 0 ? 1 : 0, contact_ ? 1 : 0, 1, mgr_chain ? 1 : 0};
+    k_manager_chain<<<1, 256, 0, stream2_>>>(bs_.p, mc, mgrM_.p, Mc_.p, mgrS_.p, mgr_chain ? tape_step : nullptr);
+    nl++;
+  }
   k_boundary_update<T><<<blocks(nd_), 256, 0, stream2_>>>(bs_.p, nd_, x0d_.p, bodyd_.p, xd_.p, vd_.p, 1);
-  launched(nchunks_ > 0 ? 4 : 3);
+  launched(nl + 1);
   pend(DFSPH_K_RIGID, nd_, stream2_);
   DF_CK(cudaEventRecord(ev_rigid_done_, stream2_));
   rigid_pending_ = true;
@@ -838,6 +959,19 @@ void Engine<T>::get_net_jacobians(int b, double *out) {
 template <class T>
 void Engine<T>::backward(const double *dL, double *out) {
   if (!dL || !out) throw DfsphException(DFSPH_ERR_INVALID_ARG, "NULL buffer");
+  if (manager_) {
+    // two sweeps (v0 and omega0 columns) from the same dL_dstate
+    const size_t n = (size_t)NSTATE * nb_;
+    std::vector<double> lam(2 * n), res(2 * n);
+    for (size_t k = 0; k < n; k++) lam[k] = lam[n + k] = dL[k];
+    adjoint_sweep(lam.data(), res.data());
+    for (int b = 0; b < nb_; b++)
+      for (int k = 0; k < 3; k++) {
+        out[6 * b + k] = res[(size_t)NSTATE * b + 7 + k];
+        out[6 * b + 3 + k] = res[n + (size_t)NSTATE * b + 10 + k];
+      }
+    return;
+  }
   std::vector<double> lam(dL, dL + (size_t)NSTATE * nb_), res((size_t)NSTATE * nb_);
   if (tape_len_ > 0 && nb_ > 0) {
     DBuf<double> li, lo;
@@ -1077,7 +1211,7 @@ void Engine<T>::set_gradient_enabled(bool on) {
   rc_.enable_gradient = P_.enable_gradient;
   if (on && nd_ > 0 && tape_cap_ == 0) {
     tape_cap_ = 256;
-    tape_.alloc((size_t)tape_cap_ * nb_ * NSTATE * NSTATE);
+    tape_.alloc((size_t)tape_cap_ * tape_stride());
   }
 }
 
@@ -1095,6 +1229,11 @@ int Engine<T>::checkpoint_save() {
   DF_CK(cudaMemcpyAsync(s->bs.p, bs_.p, NBd * sizeof(BodyState), cudaMemcpyDeviceToDevice, stream_));
   DF_CK(cudaMemcpyAsync(s->xd.p, xd_.p, ND * sizeof(V4<T>), cudaMemcpyDeviceToDevice, stream_));
   DF_CK(cudaMemcpyAsync(s->vd.p, vd_.p, ND * sizeof(V4<T>), cudaMemcpyDeviceToDevice, stream_));
+  if (manager_) {
+    s->mgrM.alloc(mgrM_.n); s->mgrS.alloc(mgrS_.n);
+    DF_CK(cudaMemcpyAsync(s->mgrM.p, mgrM_.p, mgrM_.n * sizeof(double), cudaMemcpyDeviceToDevice, stream_));
+    DF_CK(cudaMemcpyAsync(s->mgrS.p, mgrS_.p, mgrS_.n * sizeof(double), cudaMemcpyDeviceToDevice, stream_));
+  }
   sync_all();
   s->t = t_; s->sc = step_count_; s->finished = finished_; s->anim = anim_; s->dt = dt_cur_;
   for (size_t k = 0; k < snaps_.size(); k++)
@@ -1116,6 +1255,10 @@ void Engine<T>::checkpoint_restore(int slot) {
   DF_CK(cudaMemcpyAsync(bs_.p, s.bs.p, NBd * sizeof(BodyState), cudaMemcpyDeviceToDevice, stream_));
   DF_CK(cudaMemcpyAsync(xd_.p, s.xd.p, ND * sizeof(V4<T>), cudaMemcpyDeviceToDevice, stream_));
   DF_CK(cudaMemcpyAsync(vd_.p, s.vd.p, ND * sizeof(V4<T>), cudaMemcpyDeviceToDevice, stream_));
+  if (manager_) {
+    DF_CK(cudaMemcpyAsync(mgrM_.p, s.mgrM.p, mgrM_.n * sizeof(double), cudaMemcpyDeviceToDevice, stream_));
+    DF_CK(cudaMemcpyAsync(mgrS_.p, s.mgrS.p, mgrS_.n * sizeof(double), cudaMemcpyDeviceToDevice, stream_));
+  }
   if (nd_ > 0) DF_CK(cudaMemsetAsync(acc_.p, 0, (size_t)nd_ * ACC_STRIDE * sizeof(double), stream_));
   sync_all();
   t_ = s.t; step_count_ = s.sc; finished_ = s.finished; anim_ = s.anim;
@@ -1132,6 +1275,24 @@ void Engine<T>::checkpoint_free(int slot) {
 template <class T>
 void Engine<T>::adjoint_sweep(const double *lam_in, double *lam_out) {
   if (!lam_in || !lam_out) throw DfsphException(DFSPH_ERR_INVALID_ARG, "NULL buffer");
+  if (manager_) {
+    const size_t n2 = 2 * (size_t)NSTATE * nb_;
+    if (tape_len_ == 0 || nb_ == 0) {
+      for (size_t k = 0; k < n2; k++) lam_out[k] = lam_in[k];
+      return;
+    }
+    DBuf<double> li, lo;
+    li.alloc(n2);
+    lo.alloc(n2);
+    DF_CK(cudaMemcpyAsync(li.p, lam_in, n2 * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    wait_rigid();
+    k_backward_mgr<<<1, 256, 0, stream_>>>(tape_.p, (int)tape_len_, NSTATE * nb_, li.p, lo.p);
+    launched();
+    check_launch();
+    DF_CK(cudaMemcpyAsync(lam_out, lo.p, n2 * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    sync_all();
+    return;
+  }
   const size_t m = (size_t)NSTATE * std::max(nb_, 1);
   if (tape_len_ == 0 || nb_ == 0) {
     for (size_t k = 0; k < (size_t)NSTATE * nb_; k++) lam_out[k] = lam_in[k];
@@ -1148,6 +1309,42 @@ void Engine<T>::adjoint_sweep(const double *lam_in, double *lam_out) {
   DF_CK(cudaMemcpyAsync(lam_out, lo.p, (size_t)NSTATE * nb_ * sizeof(double), cudaMemcpyDeviceToHost, stream_));
   sync_all();
 }
+template <class T>
+void Engine<T>::get_manager_grad(int b, int b2, double *out) {
+  if (!manager_) throw DfsphException(DFSPH_ERR_UNSUPPORTED, "the gradient manager is off (use_rigid_gradient_manager)");
+  if (b < 0 || b >= nb_ || b2 < 0 || b2 >= nb_) throw DfsphException(DFSPH_ERR_INVALID_ARG, "body index");
+  sync_all();
+  const size_t ncol = 6 * (size_t)nb_;
+  std::vector<double> rows((size_t)NSTATE * ncol);
+  DF_CK(cudaMemcpy(rows.data(), mgrS_.p + (size_t)NSTATE * b * ncol, rows.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  // x_v0 x_w0 (3x3), q_v0 q_w0 (4x3), v_v0 v_w0, w_v0 w_w0 (3x3): rows of one component
+  // group, columns v0 (0..2) or omega0 (3..5) of body b2
+  double *o = out;
+  const int groups[4][2] = {{0, 3}, {3, 4}, {7, 3}, {10, 3}};
+  for (auto &g : groups)
+    for (int half = 0; half < 2; half++)
+      for (int r = 0; r < g[1]; r++)
+        for (int j = 0; j < 3; j++) *o++ = rows[(size_t)(g[0] + r) * ncol + 6 * b2 + 3 * half + j];
+}
+
+template <class T>
+void Engine<T>::get_manager_jacobians(int b, int b2, double *out) {
+  if (!manager_) throw DfsphException(DFSPH_ERR_UNSUPPORTED, "the gradient manager is off (use_rigid_gradient_manager)");
+  if (b < 0 || b >= nb_ || b2 < 0 || b2 >= nb_) throw DfsphException(DFSPH_ERR_INVALID_ARG, "body index");
+  sync_all();
+  DF_CK(cudaMemcpy(out, mgrM_.p + ((size_t)b * nb_ + b2) * NJAC, NJAC * sizeof(double), cudaMemcpyDeviceToHost));
+}
+
+template <class T>
+void Engine<T>::contact_count(int64_t *nc, int64_t *na) {
+  sync_all();
+  *nc = 0; *na = 0;
+  if (!contact_ || nb_ == 0) return;
+  std::vector<int> c(2 * (size_t)nb_);
+  DF_CK(cudaMemcpy(c.data(), ccount_.p, c.size() * sizeof(int), cudaMemcpyDeviceToHost));
+  for (int b = 0; b < nb_; b++) { *nc += c[2 * b]; *na += c[2 * b + 1]; }
+}
+
 // ----------------------------------------------------------------- learned warm start
 template <class T>
 void Engine<T>::ml_buffers() {
@@ -1229,6 +1426,7 @@ void Engine<T>::set_dt(double h) {
   pcP_.cTrunc = P_.truncate_gradient_coeff ? (T)(unsigned int)cg2 : cg2;
   pcD_.cTrunc = P_.truncate_gradient_coeff ? (T)(unsigned int)cg1 : cg1;
   rc_.dt = (double)fc_.dt;
+  cc_.dt = rc_.dt;
 }
 
 // Simulation::updateTimeStepSizeCFL (Simulation.cpp:541-616): max(0.1, |v + h a|^2 over the

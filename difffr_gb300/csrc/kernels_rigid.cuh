@@ -24,6 +24,9 @@ struct BodyState {
   double F[3], T[3];      // net fluid force / torque of the last step (BoundaryModel::getForce/getTorque)
   double nets[NJAC];      // per-step net Jacobians (grad_net_force_to_* / grad_net_torque_to_*)
   double G[NSTATE * 6];   // forward-mode chain state: rows x q v omega, columns v0 (3) omega0 (3)
+  // the last velocity step's angular velocity before and after it, and the rotation and
+  // world inertia before the position step (the gradient manager's stages read these)
+  double wpre[3], wmid[3], qpre[4], Ipre[9], Iipre[9];
   int dyn, anim, dstart, dcount;  // dynamic samples [dstart, dstart + dcount) in body order
   int chain_ran;          // 1 if the last step applied the chain rule
   int pad_;
@@ -32,6 +35,8 @@ struct BodyState {
 struct RigidConsts {
   double dt, gx, gy, gz;
   int gradient_mode, gyroscopic, optimize_rotation, enable_gradient;
+  int manager;  // the gradient manager's multi-body chain replaces the per-body chain
+  int nbodies;
 };
 
 // ------------------------------------------------------------------ small matrices (T)
@@ -504,12 +509,45 @@ static __device__ void grad_RqTp_d(const double *q, const double *p, double *out
   grad_RqTp<double>(q[0], q[1], q[2], q[3], V3<double>{p[0], p[1], p[2]}, out);
 }
 
+// Rigid contact of one sample of a dynamic body (kernels_contact.cuh writes these).
+constexpr int CONTACT_BLK = 2 * NJAC;  // per force-carrying sample: own-body blocks, other-body blocks
+struct ContactRec {
+  double f[3], tau[3];  // penalty + friction force and r x f on the sample's body
+  int flag;             // 0: no neighbour of another body, 1: contact without force, 2: force
+  int RR;               // the other body the cross blocks refer to (the last in point-set order)
+};
+struct ContactStep {
+  const ContactRec *rec;  // per dynamic sample (body order), or null without the contact solver
+  const double *blk;      // per dynamic sample CONTACT_BLK Jacobian terms, or null
+  int *list;              // scratch: each body's force-carrying samples in order
+  int *counts;            // per body: samples in contact, samples with a force
+  double *Mc;             // [body][body][NJAC] contact blocks of this step, or null
+};
+
+// exclusive prefix over the block's threads (blockDim.x a multiple of 32, at most 1024)
+static __device__ __forceinline__ int block_exclusive_scan(int v, int *warp_tot, int &total) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int inc = v;
+  for (int o = 1; o < 32; o <<= 1) { const int u = __shfl_up_sync(0xffffffffu, inc, o); if (lane >= o) inc += u; }
+  __syncthreads();
+  if (lane == 31) warp_tot[w] = inc;
+  __syncthreads();
+  int before = 0;
+  total = 0;
+  for (int k = 0; k < nw; k++) { if (k < w) before += warp_tot[k]; total += warp_tot[k]; }
+  return before + inc - v;
+}
+
 // One block (128 threads) per body: chain rule -> step matrix A (13x13, appended to the
 // tape), G <- A G; then RigidBody3dBoundarySimulator::velocityTimeStep (forces,
 // gyroscopic torque, gravity; :278-320) and positionTimeStep -> animate (:322-344,
-// Dynamic3dRigidBody.h:113-154, 215-235).
+// Dynamic3dRigidBody.h:113-154, 215-235). With the contact solver the velocity step is
+// gravity, then each force-carrying contact sample's force and torque in sample order, then
+// updateBoundaryForces once per boundary model (RigidBody3dBoundarySimulator.cpp:284-298,
+// RigidContactSolver.cpp:347-362); every addForce / addTorque moves the velocities at once and
+// every gyroscopic addTorque adds (I w) x w (Dynamic3dRigidBody.h:113-142).
 static __global__ void __launch_bounds__(128) k_rigid_step(BodyState *__restrict__ bs, int nbodies, RigidConsts rc,
-                                                    double *__restrict__ tape_step) {
+                                                    double *__restrict__ tape_step, ContactStep cs) {
   __shared__ ChainCoef C;
   __shared__ double A[NSTATE * NSTATE];
   __shared__ double Gold[NSTATE * 6];
@@ -527,7 +565,7 @@ static __global__ void __launch_bounds__(128) k_rigid_step(BodyState *__restrict
   }
   __syncthreads();
   BodyState &B = sB;
-  const bool chain = B.dyn && !B.anim && rc.enable_gradient;
+  const bool chain = B.dyn && !B.anim && rc.enable_gradient && !rc.manager;
   if (t == 0) B.chain_ran = chain ? 1 : 0;
   if (chain) {
     if (t == 0) {
@@ -592,21 +630,61 @@ static __global__ void __launch_bounds__(128) k_rigid_step(BodyState *__restrict
     for (int k = t; k < NSTATE * NSTATE; k += blockDim.x)
       tape_step[(size_t)b * NSTATE * NSTATE + k] = (k / NSTATE == k % NSTATE) ? 1.0 : 0.0;
   }
+  // the body's force-carrying contact samples, in sample order
+  __shared__ int warp_tot[32];
+  __shared__ int s_con, s_act;
+  const bool contact = cs.rec != nullptr && B.dyn;
+  if (t == 0) { s_con = 0; s_act = 0; }
+  __syncthreads();
+  if (contact) {
+    for (int base = 0; base < B.dcount; base += blockDim.x) {
+      const int i = base + t;
+      const int flag = i < B.dcount ? cs.rec[B.dstart + i].flag : 0;
+      int tot;
+      const int pos = block_exclusive_scan(flag == 2 ? 1 : 0, warp_tot, tot);
+      if (flag == 2) cs.list[B.dstart + s_act + pos] = B.dstart + i;
+      const int ncon = __syncthreads_count(flag >= 1);
+      if (t == 0) { s_act += tot; s_con += ncon; }
+      __syncthreads();
+    }
+  }
+  if (t == 0 && cs.counts) { cs.counts[2 * b] = s_con; cs.counts[2 * b + 1] = s_act; }
   if (t == 0 && B.dyn) {
     const double dt = rc.dt;
-    if (!B.anim) {
-      for (int k = 0; k < 3; k++) B.v[k] += B.invMass * B.F[k] * dt;
+    for (int k = 0; k < 3; k++) { B.wpre[k] = B.w[k]; }
+    for (int k = 0; k < 4; k++) B.qpre[k] = B.q[k];
+    for (int k = 0; k < 9; k++) { B.Ipre[k] = B.I[k]; B.Iipre[k] = B.Iinv[k]; }
+    auto add_force = [&](const double *f) { for (int k = 0; k < 3; k++) B.v[k] += B.invMass * f[k] * dt; };
+    auto add_torque = [&](const double *tq) {
       double d[3], L[3], cr[3];
       if (rc.gyroscopic) {
         mv3(B.I, B.w, L);
         cross3(L, B.w, cr);
-        for (int k = 0; k < 3; k++) cr[k] += B.T[k];
-      } else for (int k = 0; k < 3; k++) cr[k] = B.T[k];
+        for (int k = 0; k < 3; k++) cr[k] += tq[k];
+      } else for (int k = 0; k < 3; k++) cr[k] = tq[k];
       mv3(B.Iinv, cr, d);
       for (int k = 0; k < 3; k++) B.w[k] += d[k] * dt;
-      const double gm[3] = {rc.gx * B.mass, rc.gy * B.mass, rc.gz * B.mass};
-      for (int k = 0; k < 3; k++) B.v[k] += B.invMass * gm[k] * dt;
+    };
+    const double gm[3] = {rc.gx * B.mass, rc.gy * B.mass, rc.gz * B.mass};
+    if (cs.rec) {
+      add_force(gm);
+      for (int k = 0; k < s_act; k++) {
+        const ContactRec &cr = cs.rec[cs.list[B.dstart + k]];
+        add_force(cr.f);
+        add_torque(cr.tau);
+      }
+      const double zero[3] = {0.0, 0.0, 0.0};
+      if (!B.anim)
+        for (int rep = 0; rep < rc.nbodies; rep++) {
+          add_force(rep == 0 ? B.F : zero);
+          add_torque(rep == 0 ? B.T : zero);
+        }
+    } else if (!B.anim) {
+      add_force(B.F);
+      add_torque(B.T);
+      add_force(gm);
     }
+    for (int k = 0; k < 3; k++) B.wmid[k] = B.w[k];
     for (int k = 0; k < 3; k++) B.x[k] += B.v[k] * dt;
     const double wq[4] = {0.0, B.w[0], B.w[1], B.w[2]};
     double dq[4];
@@ -623,6 +701,21 @@ static __global__ void __launch_bounds__(128) k_rigid_step(BodyState *__restrict
     for (int i = 0; i < 3; i++)
       for (int j = 0; j < 3; j++) B.I[3 * i + j] = RI[3 * i] * RT[j] + RI[3 * i + 1] * RT[3 + j] + RI[3 * i + 2] * RT[6 + j];
     inv3<double>(B.I, B.Iinv);
+  }
+  // the contact solver's Jacobian blocks of this body, summed in sample order
+  if (cs.Mc) {
+    const int nb = rc.nbodies;
+    for (int e = t; e < nb * NJAC; e += blockDim.x) {
+      const int c = e / NJAC, k = e % NJAC;
+      double acc = 0.0;
+      if (contact)
+        for (int m = 0; m < s_act; m++) {
+          const int smp = cs.list[B.dstart + m];
+          if (c == b) acc += cs.blk[(size_t)smp * CONTACT_BLK + k];
+          else if (cs.rec[smp].RR == c) acc += cs.blk[(size_t)smp * CONTACT_BLK + NJAC + k];
+        }
+      cs.Mc[((size_t)b * nb + c) * NJAC + k] = acc;
+    }
   }
   __syncthreads();
   {

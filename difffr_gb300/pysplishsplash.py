@@ -173,25 +173,40 @@ class BoundaryModelAkinci2012:
         return RigidBodyObject(self._base, self._i)
 
 
-def _nets(base, R):
-    o = base._sim.net_jacobians(R)
+def _split_nets(o):
     return {"Fv": o[0:9].reshape(3, 3), "Fx": o[9:18].reshape(3, 3), "Fw": o[18:27].reshape(3, 3),
             "Fq": o[27:39].reshape(3, 4), "Tw": o[39:48].reshape(3, 3), "Tv": o[48:57].reshape(3, 3),
             "Tx": o[57:66].reshape(3, 3), "Tq": o[66:78].reshape(3, 4)}
 
 
+def _nets(base, R):
+    return _split_nets(base._sim.net_jacobians(R))
+
+
 class RigidBodyGradientManager:
-    """RigidBodyGradientManager accessors (SimulationModule.cpp:406-415). Without the
-    rigid contact solver the manager's blocks are diagonal (BoundaryModel_Akinci2012.cpp:
-    952-967): [R][RR] is body R's own chain state when R == RR and zero otherwise."""
+    """RigidBodyGradientManager accessors (SimulationModule.cpp:406-415). With
+    useRigidGradientManager the library runs the manager's own chain over body pairs
+    (RigidBodyGradientManager.cpp:96-468), coupled through the rigid contact solver's blocks,
+    and [R][RR] is that chain's state. Without it the manager is not stepped in the reference
+    either; these accessors then return body R's own chain state on the diagonal and zero
+    elsewhere."""
 
     def __init__(self, base):
         self._base = base
 
     def _blk(self, R, RR, key, shape):
+        sim = self._base._sim
+        if sim.uses_manager:
+            return sim.manager_grad_blocks(R, RR)[key]
         if R != RR:
             return np.zeros(shape)
-        return self._base._sim.rigid_grad_blocks(R)[key]
+        return sim.rigid_grad_blocks(R)[key]
+
+    def _jac(self, R, RR, key):
+        sim = self._base._sim
+        if sim.uses_manager:
+            return _split_nets(sim.manager_jacobians(R, RR))[key]
+        return _nets(self._base, R)[key] if R == RR else np.zeros((3, 4) if key in ("Fq", "Tq") else (3, 3))
 
     def get_grad_x_to_v0(self, R, RR):
         return self._blk(R, RR, "x_v0", (3, 3))
@@ -205,11 +220,41 @@ class RigidBodyGradientManager:
     def get_grad_q_to_omega0(self, R, RR):
         return self._blk(R, RR, "q_w0", (4, 3))
 
+    def get_grad_v_to_v0(self, R, RR):
+        return self._blk(R, RR, "v_v0", (3, 3))
+
+    def get_grad_v_to_omega0(self, R, RR):
+        return self._blk(R, RR, "v_w0", (3, 3))
+
+    def get_grad_omega_to_v0(self, R, RR):
+        return self._blk(R, RR, "w_v0", (3, 3))
+
+    def get_grad_omega_to_omega0(self, R, RR):
+        return self._blk(R, RR, "w_w0", (3, 3))
+
     def get_grad_net_force_to_vn(self, R, RR):
-        return _nets(self._base, R)["Fv"] if R == RR else np.zeros((3, 3))
+        return self._jac(R, RR, "Fv")
+
+    def get_grad_net_force_to_xn(self, R, RR):
+        return self._jac(R, RR, "Fx")
+
+    def get_grad_net_force_to_omega_n(self, R, RR):
+        return self._jac(R, RR, "Fw")
+
+    def get_grad_net_force_to_qn(self, R, RR):
+        return self._jac(R, RR, "Fq")
+
+    def get_grad_net_torque_to_vn(self, R, RR):
+        return self._jac(R, RR, "Tv")
+
+    def get_grad_net_torque_to_xn(self, R, RR):
+        return self._jac(R, RR, "Tx")
 
     def get_grad_net_torque_to_omega_n(self, R, RR):
-        return _nets(self._base, R)["Tw"] if R == RR else np.zeros((3, 3))
+        return self._jac(R, RR, "Tw")
+
+    def get_grad_net_torque_to_qn(self, R, RR):
+        return self._jac(R, RR, "Tq")
 
     def reset(self):
         self._base._sim.reset_gradient()
@@ -312,6 +357,30 @@ class TimeStepDiffDFSPH:
         return int(np.unique(row[hit]).size)
 
 
+class RigidContactSolver:
+    """BoundarySimulator::getRigidContactSolver() (SimulationModule.cpp:383-397): the
+    penalty-form contact solver runs inside each step; reset() has nothing to clear between
+    trajectories beyond what SimulatorBase.reset() restores, and the last step's contact
+    counts are exposed for inspection."""
+
+    def __init__(self, base):
+        self._base = base
+
+    def reset(self):
+        pass
+
+    def num_contacts(self):
+        return self._base._sim.contact_count()[0]
+
+
+class _BoundarySimulator:
+    def __init__(self, base):
+        self._base = base
+
+    def getRigidContactSolver(self):
+        return RigidContactSolver(self._base) if self._base._scene.params.use_rigid_contact_solver else None
+
+
 class Simulation:
     """Simulation::getCurrent() and the accessors the scripts use
     (SimulationModule.cpp:95-211)."""
@@ -345,7 +414,10 @@ class Simulation:
         self._base._set_param(gradient_mode=int(m))
 
     def useRigidGradientManager(self):
-        return bool(getattr(self._base._scene, "use_rigid_gradient_manager", False))
+        return bool(self._base._scene.params.use_rigid_gradient_manager)
+
+    def useRigidContactSolver(self):
+        return bool(self._base._scene.params.use_rigid_contact_solver)
 
     def getParticleRadius(self):
         return self._base._scene.params.particle_radius
@@ -460,6 +532,9 @@ class _SimulatorBase:
 
     def getRigidBodyGradientManager(self):
         return RigidBodyGradientManager(self)
+
+    def getBoundarySimulator(self):
+        return _BoundarySimulator(self)
 
     def getOutputPath(self):
         return self._output

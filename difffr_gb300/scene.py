@@ -58,6 +58,12 @@ class Params:
     cfl_factor: float = 0.5
     cfl_min_time_step: float = 0.0001
     cfl_max_time_step: float = 0.005
+    use_rigid_contact_solver: int = 0
+    use_rigid_gradient_manager: int = 0
+    rigid_contact_gamma: float = 0.7
+    rigid_contact_beta: float = 1.0
+    rigid_contact_support_radius_factor: float = 4.0
+    rigid_contact_friction_coeff: float = 0.0
 
 
 @dataclass
@@ -283,6 +289,40 @@ def small_contact_scene(n=(12, 10, 12), r=0.025, seed=0, precision=_abi.DFSPH_FP
     pair terms are active from the first step (used by parity tests)."""
     return tank_sphere(n=n, r=r, sphere_radius=sphere_radius, drop_gap=drop_gap, seed=seed, precision=precision,
                        steps=20, **kw)
+
+
+def two_sphere_contact(n=(20, 6, 10), r=0.025, seed=0, precision=_abi.DFSPH_FP64, sphere_radius=0.1,
+                       gap=0.02, speed=0.5, beta=20000.0, friction=0.0, release=False, uat=0.0, **kw):
+    """Two dynamic spheres, half immersed in a shallow tank, moving towards each other along
+    x with seeded spins; they start `gap` apart (surface to surface), so their boundary samples
+    are within one support radius and the rigid contact solver acts from the first step. The
+    gradient manager is on (the reference's two-ball billiards setup: useRigidContactSolver,
+    useRigidGradientManager, rigidContactBeta)."""
+    rng = np.random.default_rng(seed)
+    sp = 2.0 * r
+    fx = fluid_lattice(n, sp, (sp, sp, sp), r, rng)
+    box = ((n[0] + 1) * sp, (n[1] + 8) * sp, (n[2] + 1) * sp)
+    walls = box_surface((0.0, 0.0, 0.0), box, sp)
+    top = sp + (n[1] - 1) * sp
+    cz = 0.5 * box[2]
+    cx0 = 0.5 * box[0] - sphere_radius - 0.5 * gap
+    cx1 = 0.5 * box[0] + sphere_radius + 0.5 * gap
+    for cx in (cx0, cx1):  # no fluid inside the spheres
+        fx = fx[np.linalg.norm(fx - np.array([cx, top, cz]), axis=1) > sphere_radius + r]
+    rng2 = np.random.default_rng(seed + 5000)
+    bodies = [Body(samples=walls, density=1000.0)]
+    for cx, sgn in ((cx0, 1.0), (cx1, -1.0)):
+        w = tuple(rng2.uniform(-1.0, 1.0, 3))
+        c = (cx, top, cz)
+        bodies.append(Body(samples=sphere_surface(sphere_radius, sp), translation=c, density=500.0,
+                           is_dynamic=True, init_velocity=(sgn * speed, 0.0, 0.0), init_angular_velocity=w,
+                           target_x=c))
+    kw.setdefault("time_step", 0.001)
+    params = Params(fluid_precision=precision, particle_radius=r, use_rigid_contact_solver=1,
+                    use_rigid_gradient_manager=1, rigid_contact_beta=beta, rigid_contact_friction_coeff=friction,
+                    release_rigid_body_mode=int(release), uniform_accelerate_rb_time=uat, **kw)
+    return Scene(params=params, fluid_x=fx, fluid_v=np.zeros_like(fx), bodies=bodies,
+                 name=f"two_sphere_contact_{fx.shape[0]}", steps=40)
 
 
 CONFIGS = {0: config0, 1: config1, 2: config2, 4: config4}

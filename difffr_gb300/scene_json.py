@@ -36,6 +36,10 @@ CONFIG_KEYS = {
     "surfaceTensionBoundary": "surface_tension_boundary", "viscosity": "viscosity",
     "cflMethod": "cfl_method", "cflFactor": "cfl_factor", "cflMinTimeStepSize": "cfl_min_time_step",
     "cflMaxTimeStepSize": "cfl_max_time_step",
+    "useRigidContactSolver": "use_rigid_contact_solver", "useRigidGradientManager": "use_rigid_gradient_manager",
+    "rigidContactGamma": "rigid_contact_gamma", "rigidContactBeta": "rigid_contact_beta",
+    "rigidContactSupportRadiusFactor": "rigid_contact_support_radius_factor",
+    "rigidContactFrictionCoeff": "rigid_contact_friction_coeff",
 }
 
 
@@ -154,5 +158,4 @@ def load_scene(path_or_dict, precision=0, seed=0):
         bodies[-1].target_angle_in_degree = tuple(b.get("targetAngleInDegree", [0, 0, 0]))
     sc = scn.Scene(params=params, fluid_x=fx, fluid_v=fv, bodies=bodies,
                    name=os.path.basename(str(path_or_dict)))
-    sc.use_rigid_gradient_manager = bool(cfg.get("useRigidGradientManager", False))
     return sc

@@ -16,6 +16,16 @@ from . import _abi
 from ._abi import check, dptr
 
 
+def grad_blocks(g):
+    """The 78 chain-state numbers (dfsph_get_rigid_grad layout) as named blocks."""
+    return {
+        "x_v0": g[0:9].reshape(3, 3), "x_w0": g[9:18].reshape(3, 3),
+        "q_v0": g[18:30].reshape(4, 3), "q_w0": g[30:42].reshape(4, 3),
+        "v_v0": g[42:51].reshape(3, 3), "v_w0": g[51:60].reshape(3, 3),
+        "w_v0": g[60:69].reshape(3, 3), "w_w0": g[69:78].reshape(3, 3),
+    }
+
+
 class DiffDFSPH:
     def __init__(self, scene, lib_path=None):
         self.lib = _abi.load_library(lib_path)
@@ -145,13 +155,33 @@ class DiffDFSPH:
         return o
 
     def rigid_grad_blocks(self, b):
-        g = self.rigid_grad(b)
-        return {
-            "x_v0": g[0:9].reshape(3, 3), "x_w0": g[9:18].reshape(3, 3),
-            "q_v0": g[18:30].reshape(4, 3), "q_w0": g[30:42].reshape(4, 3),
-            "v_v0": g[42:51].reshape(3, 3), "v_w0": g[51:60].reshape(3, 3),
-            "w_v0": g[60:69].reshape(3, 3), "w_w0": g[69:78].reshape(3, 3),
-        }
+        return grad_blocks(self.rigid_grad(b))
+
+    @property
+    def uses_manager(self):
+        return bool(self.scene.params.use_rigid_gradient_manager)
+
+    def manager_grad(self, b, b2):
+        """The gradient manager's chain state [b][b2] (78 doubles, dfsph_get_rigid_grad layout):
+        derivatives of body b's state with respect to body b2's initial (v, omega)."""
+        o = np.zeros(78)
+        check(self.lib, self.lib.dfsph_get_manager_grad(self.h, int(b), int(b2), dptr(o)))
+        return o
+
+    def manager_grad_blocks(self, b, b2):
+        return grad_blocks(self.manager_grad(b, b2))
+
+    def manager_jacobians(self, b, b2):
+        """The manager's force / torque blocks [b][b2] (dfsph_get_net_jacobians layout)."""
+        o = np.zeros(78)
+        check(self.lib, self.lib.dfsph_get_manager_jacobians(self.h, int(b), int(b2), dptr(o)))
+        return o
+
+    def contact_count(self):
+        """(samples of dynamic bodies in contact, samples that carried a penalty force) of the last step."""
+        nc, na = c_int64(), c_int64()
+        check(self.lib, self.lib.dfsph_get_contact_count(self.h, byref(nc), byref(na)))
+        return nc.value, na.value
 
     def net_jacobians(self, b):
         o = np.zeros(78)
@@ -218,8 +248,11 @@ class DiffDFSPH:
         check(self.lib, self.lib.dfsph_checkpoint_free(self.h, int(slot)))
 
     def adjoint_sweep(self, lam):
-        """Full 13-component adjoints (n_bodies, 13) pulled back over the recorded steps."""
-        g = np.ascontiguousarray(lam, dtype=np.float64).reshape(self.n_bodies, 13)
+        """Full 13-component adjoints (n_bodies, 13) pulled back over the recorded steps. With
+        the gradient manager the v0 and omega0 columns have separate maps: lam is then
+        (2, n_bodies, 13), the v0 sweep's adjoint and the omega0 sweep's."""
+        shape = (2, self.n_bodies, 13) if self.uses_manager else (self.n_bodies, 13)
+        g = np.ascontiguousarray(lam, dtype=np.float64).reshape(shape)
         out = np.zeros_like(g)
         check(self.lib, self.lib.dfsph_adjoint_sweep(self.h, dptr(g), dptr(out)))
         return out

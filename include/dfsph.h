@@ -98,6 +98,16 @@ typedef struct dfsph_params {
   double  cfl_factor;                  /* "cflFactor", default 0.5 */
   double  cfl_min_time_step;           /* "cflMinTimeStepSize", default 0.0001 */
   double  cfl_max_time_step;           /* "cflMaxTimeStepSize", default 0.005 */
+  /* Rigid-rigid contact (InterlinkedSPH RigidContactSolver, penalty form,
+     RigidContactSolver.cpp:307-555, RigidBody3dBoundarySimulator.cpp:278-320; scene keys of SceneLoader.cpp:54-71) */
+  int32_t use_rigid_contact_solver;    /* "useRigidContactSolver", default 0 */
+  int32_t use_rigid_gradient_manager;  /* "useRigidGradientManager": the multi-body chain of
+                                          RigidBodyGradientManager.cpp:96-468 instead of the
+                                          per-body chain; default 0 */
+  double  rigid_contact_gamma;         /* "rigidContactGamma", default 0.7 */
+  double  rigid_contact_beta;          /* "rigidContactBeta" (penalty stiffness), default 1.0 */
+  double  rigid_contact_support_radius_factor; /* "rigidContactSupportRadiusFactor", default 4.0 */
+  double  rigid_contact_friction_coeff; /* "rigidContactFrictionCoeff", default 0.0 */
 } dfsph_params;
 
 /*
@@ -232,8 +242,29 @@ int dfsph_get_rigid_grad(dfsph_ctx *ctx, int32_t body, double out[78]);
    out[78] = F_v F_x F_w (3x3 each) F_q (3x4) T_w T_v T_x (3x3 each) T_q (3x4). */
 int dfsph_get_net_jacobians(dfsph_ctx *ctx, int32_t body, double out[78]);
 
+/* Multi-body chain state of the gradient manager (use_rigid_gradient_manager):
+   RigidBodyGradientManager get_grad_x_to_v0(R, RR), get_grad_x_to_omega0, get_grad_q_to_v0,
+   get_grad_q_to_omega0 and the v / omega blocks (SimulationModule.cpp:406-415) — the
+   derivative of body R's state with respect to body RR's initial (v, omega). out[78] in the
+   layout of dfsph_get_rigid_grad. DFSPH_ERR_UNSUPPORTED when the manager is off. */
+int dfsph_get_manager_grad(dfsph_ctx *ctx, int32_t body, int32_t body2, double out[78]);
+
+/* The manager's current force / torque Jacobian blocks [R][RR] (get_grad_net_force_to_vn(R, RR),
+   get_grad_net_torque_to_omega_n(R, RR), ...): the fluid's blocks on the diagonal after a fluid
+   step, overwritten by the contact solver's blocks for every dynamic pair when it runs
+   (RigidContactSolver.cpp:1341-1369). out[78] in the layout of dfsph_get_net_jacobians. */
+int dfsph_get_manager_jacobians(dfsph_ctx *ctx, int32_t body, int32_t body2, double out[78]);
+
+/* Rigid contact of the last step: samples of dynamic bodies with a boundary neighbour of
+   another body (num_contacts, RigidContactSolver.cpp:307-345) and, of those, the samples whose
+   contact density exceeded their rest density and so carried a penalty force. */
+int dfsph_get_contact_count(dfsph_ctx *ctx, int64_t *n_contact, int64_t *n_active);
+
 /* Replaces TimeStepDiffDFSPH::reset_gradient (DiffDFSPHModule.cpp:91): chain state to
-   identity/zero and the recorded per-step adjoint tape cleared. */
+   identity/zero and the recorded per-step adjoint tape cleared. With the gradient manager
+   on, its chain state is reset too (RigidBodyGradientManager::reset); its Jacobian blocks
+   stay, because the next step's fluid stage reads the last contact blocks (dfsph_reset
+   clears them). */
 int dfsph_reset_gradient(dfsph_ctx *ctx);
 
 /* Reverse-mode adjoint over the per-step chain matrices recorded since the last
@@ -241,7 +272,8 @@ int dfsph_reset_gradient(dfsph_ctx *ctx);
    (dL/dx[3], dL/dq[4] (w,x,y,z), dL/dv[3], dL/domega[3]) for the current state;
    dL_dinit receives 6 doubles per body (dL/dv0[3], dL/domega0[3]). Equal to
    contracting dL_dstate with the forward-mode chain state. No reference counterpart:
-   the reference only propagates forward-mode tangents. */
+   the reference only propagates forward-mode tangents. With the gradient manager on the
+   step maps couple the bodies, and dL_dinit of body RR collects every body's dL_dstate. */
 int dfsph_backward(dfsph_ctx *ctx, const double *dL_dstate, double *dL_dinit);
 int dfsph_tape_length(dfsph_ctx *ctx, int64_t *n_steps);
 
@@ -284,7 +316,11 @@ int dfsph_checkpoint_free(dfsph_ctx *ctx, int32_t slot);
 
 /* Reverse sweep of the recorded step matrices on full 13-component adjoints: lam_out =
    A_1^T ... A_N^T lam_in, per body (x, q, v, omega). Lets a caller chain the adjoint across
-   recomputed segments; dfsph_backward is this sweep followed by taking the (v, omega) part. */
+   recomputed segments; dfsph_backward is this sweep followed by taking the (v, omega) part.
+   With the gradient manager on, the maps of the v0 columns and of the omega0 columns differ
+   (RigidBodyGradientManager.cpp:196-205 drops the q term of the v0 columns), so lam_in and
+   lam_out hold 26 doubles per body: 13 per body for the v0 sweep, then 13 per body for the
+   omega0 sweep. */
 int dfsph_adjoint_sweep(dfsph_ctx *ctx, const double *lam_in, double *lam_out);
 
 /* Synchronises the context's stream (for timing from the caller). */

@@ -57,6 +57,9 @@ def lib():
             getattr(L, n).argtypes = [c_void_p, c_int, dp, dp]
         for n in ("orc_get_rigid_grad", "orc_get_net_jacobians"):
             getattr(L, n).argtypes = [c_void_p, c_int, dp]
+        for n in ("orc_get_manager_grad", "orc_get_manager_jacobians"):
+            getattr(L, n).argtypes = [c_void_p, c_int, c_int, dp]
+        L.orc_get_contact_count.argtypes = [c_void_p, POINTER(c_int64), POINTER(c_int64)]
         L.orc_get_neighbors.argtypes = [c_void_p, c_int, POINTER(c_int64), POINTER(c_int32), POINTER(c_int64)]
         L.orc_reset.argtypes = [c_void_p]
         L.orc_reset_gradient.argtypes = [c_void_p]
@@ -77,6 +80,16 @@ def lib():
 
 def _p(a):
     return a.ctypes.data_as(POINTER(c_double))
+
+
+def grad_blocks(g):
+    """The 78 chain-state numbers (dfsph_get_rigid_grad layout) as named blocks."""
+    return {
+        "x_v0": g[0:9].reshape(3, 3), "x_w0": g[9:18].reshape(3, 3),
+        "q_v0": g[18:30].reshape(4, 3), "q_w0": g[30:42].reshape(4, 3),
+        "v_v0": g[42:51].reshape(3, 3), "v_w0": g[51:60].reshape(3, 3),
+        "w_v0": g[60:69].reshape(3, 3), "w_w0": g[69:78].reshape(3, 3),
+    }
 
 
 class Oracle:
@@ -146,13 +159,22 @@ class Oracle:
         return o
 
     def rigid_grad_blocks(self, b):
-        g = self.rigid_grad(b)
-        return {
-            "x_v0": g[0:9].reshape(3, 3), "x_w0": g[9:18].reshape(3, 3),
-            "q_v0": g[18:30].reshape(4, 3), "q_w0": g[30:42].reshape(4, 3),
-            "v_v0": g[42:51].reshape(3, 3), "v_w0": g[51:60].reshape(3, 3),
-            "w_v0": g[60:69].reshape(3, 3), "w_w0": g[69:78].reshape(3, 3),
-        }
+        return grad_blocks(self.rigid_grad(b))
+
+    def manager_grad(self, b, b2):
+        o = np.zeros(78)
+        assert self.L.orc_get_manager_grad(self.h, b, b2, _p(o)) == 0
+        return o
+
+    def manager_jacobians(self, b, b2):
+        o = np.zeros(78)
+        assert self.L.orc_get_manager_jacobians(self.h, b, b2, _p(o)) == 0
+        return o
+
+    def contact_count(self):
+        nc, na = c_int64(), c_int64()
+        assert self.L.orc_get_contact_count(self.h, ctypes.byref(nc), ctypes.byref(na)) == 0
+        return nc.value, na.value
 
     def net_jacobians(self, b):
         o = np.zeros(78)

@@ -350,6 +350,9 @@ struct Base {
   virtual int reset_gradient() = 0;
   virtual int counts(int64_t *nf, int64_t *nb) = 0;
   virtual double time() = 0;
+  virtual int mgr_grad(int b, int b2, double *out) = 0;
+  virtual int mgr_jac(int b, int b2, double *out) = 0;
+  virtual int contact_count(int64_t *nc, int64_t *na) = 0;
 };
 
 template <class F, class R>
@@ -389,6 +392,19 @@ struct Sim : Base {
     M43R Gq_v, Gq_w, partial_qn_w;
   };
   std::vector<Body> bodies;
+  // RigidContactSolver (InterlinkedSPH/RigidContactSolver.h:140-224): per boundary sample rest
+  // volume and rest density from its own body, the contact kernel with the contact support
+  // radius, and the last step's contact counts
+  Cubic<R> KCt, KHr;
+  std::vector<R> cvol0, cdens0;
+  int64_t n_contact = 0, n_active = 0;
+  // RigidBodyGradientManager (RigidBodyGradientManager.h:20-93): Jacobian blocks [R][RR]
+  // (the contact solver's of this step in mgrMc) and the chain state [R][RR]
+  struct MgrBlk { M3R Fv, Fx, Fw, Tw, Tv, Tx; M34R Fq, Tq; };
+  struct MgrState { M3R Gx_v, Gx_w, Gv_v, Gv_w, Gw_v, Gw_w; M43R Gq_v, Gq_w; };
+  std::vector<MgrBlk> mgrM, mgrMc;
+  std::vector<MgrState> mgrS;
+  std::vector<M3R> mFv0, mFw0, mTv0, mTw0;  // grad_net_{force,torque}_to_{v0,omega0}[R][RR]
   std::vector<int64_t> ffS, fbS, bfS;
   std::vector<int32_t> ff, fb, bf;
   R t = 0;
@@ -453,7 +469,36 @@ struct Sim : Base {
       bodies.push_back(B);
     }
     bx.assign(nbp, V3F::zero()); bv.assign(nbp, V3F::zero()); psi.assign(nbp, 0);
+    const size_t nb2 = bodies.size() * bodies.size();
+    mgrM.resize(nb2); mgrMc.resize(nb2); mgrS.resize(nb2);
+    mFv0.resize(nb2); mFw0.resize(nb2); mTv0.resize(nb2); mTw0.resize(nb2);
     reset();
+    if (P.use_rigid_contact_solver) init_contact();
+  }
+
+  // RigidContactSolver::RigidContactSolver (RigidContactSolver.cpp:23-262): every boundary
+  // sample's rest volume gamma / (W0 + sum over its own body's neighbours of W) and rest
+  // density, with the contact kernel of support factor * r, from the samples' world positions
+  // once (own-body distances do not change as the bodies move).
+  void init_contact() {
+    KCt.set((R)P.rigid_contact_support_radius_factor * (R)P.particle_radius);
+    KHr.set((R)h);
+    std::vector<int64_t> S; std::vector<int32_t> I;
+    neighbor_search(bx, bx, h, true, S, I);
+    cvol0.assign(nbp, R(0)); cdens0.assign(nbp, R(0));
+    const R gamma = (R)P.rigid_contact_gamma;
+    for (int64_t j = 0; j < nbp; j++) {
+      R sumW = KCt.w0;
+      for (int64_t s = S[j]; s < S[j + 1]; s++)
+        if (bbody[I[s]] == bbody[j]) sumW += KCt.W(V3R(bx[j].template cast<R>() - bx[I[s]].template cast<R>()));
+      cvol0[j] = gamma / sumW;
+    }
+    for (int64_t j = 0; j < nbp; j++) {
+      R d = cvol0[j] * KCt.w0;
+      for (int64_t s = S[j]; s < S[j + 1]; s++)
+        if (bbody[I[s]] == bbody[j]) d += cvol0[I[s]] * KCt.W(V3R(bx[j].template cast<R>() - bx[I[s]].template cast<R>()));
+      cdens0[j] = d;
+    }
   }
 
   void update_inertia(Body &B) {  // Dynamic3dRigidBody.h:215-219
@@ -501,6 +546,7 @@ struct Sim : Base {
     t = 0; step_count = 0; finished = false;
     set_dt((F)P.time_step);
     reset_gradient();
+    clear_manager_blocks();
     return 0;
   }
   int reset_gradient() override {  // BoundaryModel_Akinci2012::reset_gradient (:61-108)
@@ -514,7 +560,26 @@ struct Sim : Base {
       B.Gq_w = M43R::zero(); B.partial_qn_w = M43R::zero(); B.Gq_v = M43R::zero();
       B.Gx_v = M3R::zero(); B.Gx_w = M3R::zero();
     }
+    // RigidBodyGradientManager::reset (RigidBodyGradientManager.cpp:477-524) of the chain
+    // state; the blocks are cleared by reset() only (the GPU library keeps them across
+    // dfsph_reset_gradient so that checkpointed replays map as the first run did)
+    const int nb = (int)bodies.size();
+    for (int a = 0; a < nb; a++)
+      for (int c = 0; c < nb; c++) {
+        MgrState &S = mgrS[a * nb + c];
+        S.Gx_v = S.Gx_w = S.Gv_w = S.Gw_v = M3R::zero();
+        S.Gq_v = S.Gq_w = M43R::zero();
+        S.Gv_v = S.Gw_w = (a == c) ? M3R::eye() : M3R::zero();
+        mFv0[a * nb + c] = mFw0[a * nb + c] = mTv0[a * nb + c] = mTw0[a * nb + c] = M3R::zero();
+      }
     return 0;
+  }
+  void clear_manager_blocks() {
+    for (size_t k = 0; k < mgrM.size(); k++) {
+      MgrBlk &M = mgrM[k];
+      M.Fv = M.Fx = M.Fw = M.Tw = M.Tv = M.Tx = M3R::zero(); M.Fq = M.Tq = M34R::zero();
+      mgrMc[k] = M;
+    }
   }
 
   // BoundaryModel::addForce (BoundaryModel.h:46-58)
@@ -858,6 +923,218 @@ struct Sim : Base {
     }
   }
 
+  // Dynamic3dRigidBody::addForce / addTorque (Dynamic3dRigidBody.h:113-142): each call moves
+  // the body's velocities at once; in the gyroscopic mode every addTorque adds (I w) x w with
+  // the angular velocity of that moment.
+  void add_force_now(Body &B, const V3R &f) { B.v += B.invMass * f * (R)dt; }
+  void add_torque_now(Body &B, const V3R &tq) {
+    if (P.rigid_body_mode == DFSPH_RB_GYROSCOPIC) {
+      const V3R L = B.I * B.w;
+      B.w += B.Iinv * (cross(L, B.w) + tq) * (R)dt;
+    } else B.w += B.Iinv * tq * (R)dt;
+  }
+  static V3R normalized_or_self(const V3R &a) {  // Eigen 3.4 MatrixBase::normalized()
+    const R z = sqnorm(a);
+    return z > R(0) ? V3R(a / std::sqrt(z)) : a;
+  }
+  // RigidContactSolver::beforePenaltyInitialize + solveRigidContactPenalty
+  // (RigidContactSolver.cpp:307-345, 419-555), for the samples of dynamic bodies (a static
+  // body's force moves nothing and the manager skips its blocks). Neighbours over all boundary
+  // point sets within h; the contact density uses the contact kernel, its gradient the
+  // simulation's kernel (sim->gradW, :456-460).
+  void contact_forces(bool grad) {
+    const int nb = (int)bodies.size();
+    for (auto &M : mgrMc) { M.Fv = M.Fx = M.Fw = M.Tw = M.Tv = M.Tx = M3R::zero(); M.Fq = M.Tq = M34R::zero(); }
+    n_contact = n_active = 0;
+    std::vector<char> mask(nbp, 0);
+    for (auto &B : bodies) if (B.dyn) for (int64_t j = B.start; j < B.start + B.count; j++) mask[j] = 1;
+    std::vector<int64_t> S; std::vector<int32_t> I;
+    neighbor_search(bx, bx, h, true, S, I, &mask);
+    auto svel = [&](int64_t k) -> V3R {  // vel[R][r] (:313-316): the bodies' velocities after gravity
+      const Body &C = bodies[bbody[k]];
+      if (!(C.dyn || C.anim)) return V3R::zero();
+      return V3R(C.v + cross(C.w, V3R(bx[k].template cast<R>() - C.x)));
+    };
+    const R beta = (R)P.rigid_contact_beta, mu = (R)P.rigid_contact_friction_coeff;
+    for (int b = 0; b < nb; b++) {
+      Body &B = bodies[b];
+      if (!B.dyn) continue;
+      for (int64_t j = B.start; j < B.start + B.count; j++) {
+        bool has = false;
+        for (int64_t s = S[j]; s < S[j + 1]; s++) if (bbody[I[s]] != b) has = true;
+        if (!has) continue;
+        n_contact++;
+        const V3R xr = bx[j].template cast<R>();
+        const V3R rr = xr - B.x;
+        const V3R r0 = bx0[j].template cast<R>();
+        R dens = cvol0[j] * KCt.w0;
+        V3R sum_x = V3R::zero(), sum_vk = V3R::zero(), avg_rk = V3R::zero(), gdx = V3R::zero();
+        V4<R> gdq = V4<R>::zero(), gdqk = V4<R>::zero();
+        R sum_w = 0;
+        int RR = b;
+        const M34R GqB = grad_Rqp_to_q(B.q, r0);
+        for (int64_t s = S[j]; s < S[j + 1]; s++) {
+          const int64_t k = I[s];
+          const V3R xk = bx[k].template cast<R>();
+          const V3R d = xr - xk;
+          const R w = KCt.W(d);
+          dens += cvol0[k] * w;
+          if (bbody[k] == b) { sum_x += xk * w; sum_w += w; }
+          else {
+            RR = bbody[k];
+            const Body &C = bodies[RR];
+            sum_vk += svel(k) * w;
+            avg_rk += V3R(xk - C.x) * w;
+            const V3R gw = KHr.gradW(d);
+            gdx += cvol0[k] * gw;
+            gdq += (cvol0[k] * gw.T_() * GqB).T_();
+            gdqk += (cvol0[k] * gw.T_() * R(-1) * grad_Rqp_to_q(C.q, V3R(bx0[k].template cast<R>()))).T_();
+          }
+        }
+        const R ratio = dens / cdens0[j];
+        if (!(ratio > R(1))) continue;
+        n_active++;
+        const V3R normal = xr - sum_x / sum_w;
+        const V3R vrel = svel(j) - sum_vk / sum_w;
+        avg_rk = avg_rk / sum_w;
+        const V3R Fn = -beta * std::max(ratio - R(1), R(0)) * normal;
+        const V3R u = normalized_or_self(vrel);
+        const V3R Ff = -mu * norm(Fn) * u;
+        const V3R f = Fn + Ff;
+        add_force_now(B, f);
+        add_torque_now(B, cross(rr, f));
+        if (!grad) continue;
+        const V3R gFn_d = -beta * normal;
+        const M3R gFn_x = gFn_d * gdx.T_();
+        const M34R gFn_q = gFn_d * gdq.T_();
+        const M34R gFn_qk = gFn_d * gdqk.T_();
+        const V3R gFf_d = ((-mu * u) * Fn.T_() / norm(Fn)) * gFn_d;
+        const M3R gFf_vr = (-mu * norm(Fn) / norm(vrel)) * (M3R::eye() - u * u.T_());
+        const M3R gFf_w = gFf_vr * skew(rr).T_();
+        const M3R gFf_wk = -gFf_vr * skew(avg_rk).T_();
+        const M3R gFf_x = gFf_d * gdx.T_();
+        const M34R gFf_q = gFf_d * gdq.T_();
+        const M34R gFf_qk = gFf_d * gdqk.T_();
+        MgrBlk &D = mgrMc[b * nb + b];
+        const M3R gf_x = gFn_x + gFf_x;
+        D.Fx += gf_x;
+        D.Tx += skew(rr) * gf_x;
+        const M34R gf_q = gFn_q + gFf_q;
+        D.Fq += gf_q;
+        D.Tq += skew(rr) * gf_q + skew(f).T_() * GqB;
+        D.Fv += gFf_vr;
+        D.Fw += gFf_w;
+        if (RR != b) {
+          MgrBlk &X = mgrMc[b * nb + RR];
+          X.Fv += -gFf_vr;
+          X.Fw += gFf_wk;
+          X.Fx += -gf_x;
+          X.Tx += -skew(rr) * gf_x;
+          const M34R gf_qk = gFn_qk + gFf_qk;
+          X.Fq += gf_qk;
+          X.Tq += skew(rr) * gf_qk;
+        }
+      }
+    }
+  }
+
+  // ---- RigidBodyGradientManager (RigidBodyGradientManager.cpp:96-468)
+  // perform_force_and_torque_chain_rule (:96-156) and its _Rigid form (:158-290), which adds
+  // the x and q terms; its v0 columns lose the q term to a statement that ends early (:196-205).
+  void mgr_force_chain(bool rigid) {
+    const int nb = (int)bodies.size();
+    for (int a = 0; a < nb; a++)
+      for (int c = 0; c < nb; c++) mFv0[a * nb + c] = mFw0[a * nb + c] = mTv0[a * nb + c] = mTw0[a * nb + c] = M3R::zero();
+    for (int a = 0; a < nb; a++) {
+      if (!bodies[a].dyn) continue;
+      for (int c = 0; c < nb; c++) {
+        if (!bodies[c].dyn) continue;
+        for (int k = 0; k < nb; k++) {
+          if (!bodies[k].dyn) continue;
+          const MgrBlk &M = mgrM[a * nb + k];
+          const MgrState &S = mgrS[k * nb + c];
+          if (!rigid) {
+            mFv0[a * nb + c] += M.Fv * S.Gv_v + M.Fw * S.Gw_v;
+            mTv0[a * nb + c] += M.Tv * S.Gv_v + M.Tw * S.Gw_v;
+            mFw0[a * nb + c] += M.Fv * S.Gv_w + M.Fw * S.Gw_w;
+            mTw0[a * nb + c] += M.Tv * S.Gv_w + M.Tw * S.Gw_w;
+          } else {
+            mFv0[a * nb + c] += M.Fv * S.Gv_v + M.Fw * S.Gw_v + M.Fx * S.Gx_v;
+            mTv0[a * nb + c] += M.Tv * S.Gv_v + M.Tw * S.Gw_v + M.Tx * S.Gx_v;
+            mFw0[a * nb + c] += M.Fv * S.Gv_w + M.Fw * S.Gw_w + M.Fx * S.Gx_w + M.Fq * S.Gq_w;
+            mTw0[a * nb + c] += M.Tv * S.Gv_w + M.Tw * S.Gw_w + M.Tx * S.Gx_w + M.Tq * S.Gq_w;
+          }
+        }
+      }
+    }
+  }
+  // perform_velocity_chain_rule (:292-393); F and T are the fluid force and torque still held by
+  // the boundary model (zero once updateBoundaryForces has cleared them)
+  void mgr_velocity_chain(bool fluid_ft) {
+    const int nb = (int)bodies.size();
+    const bool gyro = P.rigid_body_mode == DFSPH_RB_GYROSCOPIC;
+    const R dt_ = (R)dt;
+    for (int a = 0; a < nb; a++) {
+      Body &B = bodies[a];
+      if (!B.dyn) continue;
+      const M3R &inertia = B.I, &inv_inertia = B.Iinv;
+      const V3R om = B.w;
+      V3R force = V3R::zero(), torque = V3R::zero();
+      if (fluid_ft) force_and_torque(B, force, torque);
+      for (int c = 0; c < nb; c++) {
+        if (!bodies[c].dyn) continue;
+        MgrState &S = mgrS[a * nb + c];
+        S.Gv_v = S.Gv_v + dt_ * B.invMass * mFv0[a * nb + c];
+        S.Gv_w = S.Gv_w + dt_ * B.invMass * mFw0[a * nb + c];
+        V3R temp_v;
+        M3R gTau_w0, gTau_v0;
+        if (gyro) {
+          temp_v = cross(V3R(inertia * om), om) + torque;
+          const M3R gL_w0 = skew(V3R(inertia * om)) * S.Gw_w + skew(om).T_() * (inertia * S.Gw_w + grad_inertia_v(B, om, S.Gq_w));
+          const M3R gL_v0 = skew(V3R(inertia * om)) * S.Gw_v + skew(om).T_() * (inertia * S.Gw_v + grad_inertia_v(B, om, S.Gq_v));
+          gTau_w0 = gL_w0 + mTw0[a * nb + c];
+          gTau_v0 = gL_v0 + mTv0[a * nb + c];
+        } else {
+          temp_v = torque;
+          gTau_w0 = mTw0[a * nb + c];
+          gTau_v0 = mTv0[a * nb + c];
+        }
+        const M3R gII_w0 = inv_inertia * grad_inertia_v(B, V3R(inv_inertia * temp_v), S.Gq_w);
+        const M3R gII_v0 = inv_inertia * grad_inertia_v(B, V3R(inv_inertia * temp_v), S.Gq_v);
+        S.Gw_w = S.Gw_w + dt_ * (gII_w0 + B.Iinv * gTau_w0);
+        S.Gw_v = S.Gw_v + dt_ * (gII_v0 + B.Iinv * gTau_v0);
+      }
+    }
+  }
+  // perform_position_and_rotation_chain_rule (:395-453), with the angular velocity the
+  // velocity step left and the rotation before the position step
+  void mgr_position_rotation() {
+    const int nb = (int)bodies.size();
+    const R dt_ = (R)dt;
+    for (int a = 0; a < nb; a++) {
+      const Body &B = bodies[a];
+      if (!B.dyn) continue;
+      const QR q = B.q;
+      const QR p = {R(0), B.w[0], B.w[1], B.w[2]};
+      QR nq = q;
+      const QR pq = p * nq;
+      nq.w += dt_ * R(0.5) * pq.w; nq.x += dt_ * R(0.5) * pq.x; nq.y += dt_ * R(0.5) * pq.y; nq.z += dt_ * R(0.5) * pq.z;
+      QR nqn = nq; nqn.normalize();
+      const V4<R> nv = nqn.vec4();
+      const M4<R> Gpq = grad_p_q_product_to_q(p);
+      const M43R Gpw = grad_omega_q_product_to_omega(q);
+      const M4<R> Gn = (M4<R>::eye() - nv * nv.T_()) / nq.norm();
+      for (int c = 0; c < nb; c++) {
+        if (!bodies[c].dyn) continue;
+        MgrState &S = mgrS[a * nb + c];
+        S.Gx_v += dt_ * S.Gv_v;
+        S.Gx_w += dt_ * S.Gv_w;
+        S.Gq_v = Gn * (S.Gq_v + dt_ / R(2) * (Gpw * S.Gw_v + Gpq * S.Gq_v));
+        S.Gq_w = Gn * (S.Gq_w + dt_ / R(2) * (Gpw * S.Gw_w + Gpq * S.Gq_w));
+      }
+    }
+  }
+
   void neighborhood_search() {
     neighbor_search(x, x, h, true, ffS, ff);
     neighbor_search(x, bx, h, false, fbS, fb);
@@ -986,28 +1263,72 @@ struct Sim : Base {
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < nf; i++) x[i] += h_step * v[i];  // :613-635
     t += (R)h_step;
-    // backwardPerStep (:493-524)
-    for (auto &B : bodies) {
+    // backwardPerStep (:493-524): the per-body chain, or with the gradient manager the body's
+    // net blocks become the manager's diagonal blocks (BoundaryModel_Akinci2012.cpp:952-967)
+    const bool mgr = P.use_rigid_gradient_manager != 0;
+    const int nbod = (int)bodies.size();
+    for (int b = 0; b < nbod; b++) {
+      Body &B = bodies[b];
       if (!B.dyn || B.anim) continue;
       accumulate_and_reset(B);
-      chain_rule(B);
+      if (mgr) {
+        MgrBlk &M = mgrM[b * nbod + b];
+        M.Fv = B.nFv; M.Fx = B.nFx; M.Fw = B.nFw; M.Fq = B.nFq;
+        M.Tv = B.nTv; M.Tx = B.nTx; M.Tw = B.nTw; M.Tq = B.nTq;
+      } else chain_rule(B);
     }
     // endStep (:432-490)
     finished = t >= (R)P.target_time + (R)P.uniform_accelerate_rb_time;
-    // RigidBody3dBoundarySimulator::velocityTimeStep (:278-320) + BoundarySimulator::updateBoundaryForces
-    for (auto &B : bodies) {
-      if (!B.dyn) continue;
-      if (!B.anim) {
-        V3R Fo, To;
-        force_and_torque(B, Fo, To);
-        B.v += B.invMass * Fo * (R)dt;  // Dynamic3dRigidBody::addForce (:113-124)
-        if (P.rigid_body_mode == DFSPH_RB_GYROSCOPIC) {  // addTorque (:125-142)
-          const V3R L = B.I * B.w;
-          B.w += B.Iinv * (cross(L, B.w) + To) * (R)dt;
-        } else B.w += B.Iinv * To * (R)dt;
+    // SimulatorBase::timeStep (SimulatorBase.cpp:999-1016): the manager's fluid stage, the
+    // boundary simulator's velocity step, the manager's rigid stage, the position step
+    if (mgr && nf > 0) { mgr_force_chain(false); mgr_velocity_chain(true); }
+    if (P.use_rigid_contact_solver) {
+      // RigidBody3dBoundarySimulator::velocityTimeStep with the contact solver (:284-298):
+      // gravity on every dynamic body, the penalty forces, then updateBoundaryForces once per
+      // boundary model (RigidContactSolver.cpp:355-358); after the first call the fluid force
+      // is cleared, but each later addTorque(0) still adds the gyroscopic term
+      for (auto &B : bodies) if (B.dyn) add_force_now(B, V3R(grav.template cast<R>() * B.mass));
+      contact_forces(mgr);
+      for (int rep = 0; rep < nbod; rep++)
+        for (auto &B : bodies) {
+          if (!B.dyn) continue;
+          if (!B.anim) {
+            V3R Fo, To;
+            force_and_torque(B, Fo, To);
+            add_force_now(B, Fo);
+            add_torque_now(B, To);
+          }
+          if (rep == 0)
+            for (int th = 0; th < nthreads; th++) { B.fbak[th] = B.fth[th]; B.tbak[th] = B.tth[th]; }
+          for (int th = 0; th < nthreads; th++) { B.fth[th] = V3R::zero(); B.tth[th] = V3R::zero(); }
+        }
+    } else {
+      // RigidBody3dBoundarySimulator::velocityTimeStep (:278-320) + BoundarySimulator::updateBoundaryForces
+      for (auto &B : bodies) {
+        if (!B.dyn) continue;
+        if (!B.anim) {
+          V3R Fo, To;
+          force_and_torque(B, Fo, To);
+          B.v += B.invMass * Fo * (R)dt;  // Dynamic3dRigidBody::addForce (:113-124)
+          if (P.rigid_body_mode == DFSPH_RB_GYROSCOPIC) {  // addTorque (:125-142)
+            const V3R L = B.I * B.w;
+            B.w += B.Iinv * (cross(L, B.w) + To) * (R)dt;
+          } else B.w += B.Iinv * To * (R)dt;
+        }
+        for (int th = 0; th < nthreads; th++) { B.fbak[th] = B.fth[th]; B.tbak[th] = B.tth[th]; B.fth[th] = V3R::zero(); B.tth[th] = V3R::zero(); }
+        if (!B.anim) B.v += B.invMass * (grav.template cast<R>() * B.mass) * (R)dt;  // addGravity (:230-235)
       }
-      for (int th = 0; th < nthreads; th++) { B.fbak[th] = B.fth[th]; B.tbak[th] = B.tth[th]; B.fth[th] = V3R::zero(); B.tth[th] = V3R::zero(); }
-      if (!B.anim) B.v += B.invMass * (grav.template cast<R>() * B.mass) * (R)dt;  // addGravity (:230-235)
+    }
+    if (mgr) {
+      if (P.use_rigid_contact_solver) {
+        // RigidContactSolver::update_rigid_body_gradient_manager (:1341-1369): every dynamic pair
+        for (int a = 0; a < nbod; a++)
+          for (int c = 0; c < nbod; c++)
+            if (bodies[a].dyn && bodies[c].dyn) mgrM[a * nbod + c] = mgrMc[a * nbod + c];
+        mgr_force_chain(true);
+        mgr_velocity_chain(false);
+      }
+      mgr_position_rotation();
     }
     // positionTimeStep (:322-344) -> Dynamic3dRigidBody::animate (:143-154)
     for (auto &B : bodies) {
@@ -1135,6 +1456,25 @@ struct Sim : Base {
     return 0;
   }
   int counts(int64_t *a_, int64_t *b_) override { *a_ = nf; *b_ = nbp; return 0; }
+  int mgr_grad(int b, int b2, double *out) override {
+    const int nb = (int)bodies.size();
+    if (b < 0 || b >= nb || b2 < 0 || b2 >= nb) return DFSPH_ERR_INVALID_ARG;
+    const MgrState &S = mgrS[b * nb + b2];
+    double *o = out;
+    o = put(o, S.Gx_v); o = put(o, S.Gx_w); o = put(o, S.Gq_v); o = put(o, S.Gq_w);
+    o = put(o, S.Gv_v); o = put(o, S.Gv_w); o = put(o, S.Gw_v); o = put(o, S.Gw_w);
+    return 0;
+  }
+  int mgr_jac(int b, int b2, double *out) override {
+    const int nb = (int)bodies.size();
+    if (b < 0 || b >= nb || b2 < 0 || b2 >= nb) return DFSPH_ERR_INVALID_ARG;
+    const MgrBlk &M = mgrM[b * nb + b2];
+    double *o = out;
+    o = put(o, M.Fv); o = put(o, M.Fx); o = put(o, M.Fw); o = put(o, M.Fq);
+    o = put(o, M.Tw); o = put(o, M.Tv); o = put(o, M.Tx); o = put(o, M.Tq);
+    return 0;
+  }
+  int contact_count(int64_t *nc, int64_t *na) override { *nc = n_contact; *na = n_active; return 0; }
   double time() override { return (double)t; }
 };
 
@@ -1167,6 +1507,9 @@ int orc_reset(void *s) { return ((orc::Base *)s)->reset(); }
 int orc_reset_gradient(void *s) { return ((orc::Base *)s)->reset_gradient(); }
 int orc_num_particles(void *s, int64_t *nf, int64_t *nb) { return ((orc::Base *)s)->counts(nf, nb); }
 double orc_get_time(void *s) { return ((orc::Base *)s)->time(); }
+int orc_get_manager_grad(void *s, int b, int b2, double *o) { return ((orc::Base *)s)->mgr_grad(b, b2, o); }
+int orc_get_manager_jacobians(void *s, int b, int b2, double *o) { return ((orc::Base *)s)->mgr_jac(b, b2, o); }
+int orc_get_contact_count(void *s, int64_t *nc, int64_t *na) { return ((orc::Base *)s)->contact_count(nc, na); }
 
 // Kernel probes for the golden-vector pin (double precision kernel with support h).
 void orc_kernel_eval(double h, int n, const double *r, double *W, double *gradW, double *gradGradW) {

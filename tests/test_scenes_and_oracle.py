@@ -274,3 +274,69 @@ def test_reference_state_file_reads():
     assert d["position"].shape == (87374, 3) and d["velocity"].shape == (87374, 3)
     assert {"id", "kappa", "kappa_v"} <= set(d)
     assert np.all(np.isfinite(d["position"])) and np.abs(d["position"]).max() < 2.0
+
+
+@pytest.mark.skipif(not os.path.isdir("/root/reference/experiments"), reason="reference checkout not present")
+def test_reference_contact_scene_loads():
+    """The reference's two-ball billiards scene turns on the rigid contact solver and the
+    gradient manager (its Configuration keys reach dfsph_params)."""
+    base = "/root/reference/experiments/rigid_body_trajectory_optimization/scene"
+    sc = load_scene(os.path.join(base, "billiards-on-water-2balls.json"))
+    p = sc.params
+    assert p.use_rigid_contact_solver == 1 and p.use_rigid_gradient_manager == 1
+    assert p.rigid_contact_beta == 20000.0 and p.release_rigid_body_mode == 1
+    assert [b.is_dynamic for b in sc.bodies] == [False, True, True]
+
+
+def test_scene_json_contact_keys():
+    cfg = {"Configuration": {"particleRadius": 0.02, "useRigidContactSolver": True, "useRigidGradientManager": True,
+                             "rigidContactBeta": 500.0, "rigidContactGamma": 0.6,
+                             "rigidContactSupportRadiusFactor": 3.5, "rigidContactFrictionCoeff": 0.1},
+           "FluidBlocks": [{"start": [0, 0, 0], "end": [0.2, 0.2, 0.2]}]}
+    p = load_scene(cfg).params
+    assert (p.use_rigid_contact_solver, p.use_rigid_gradient_manager) == (1, 1)
+    assert (p.rigid_contact_beta, p.rigid_contact_gamma) == (500.0, 0.6)
+    assert (p.rigid_contact_support_radius_factor, p.rigid_contact_friction_coeff) == (3.5, 0.1)
+    d = load_scene({"Configuration": {}, "FluidBlocks": []}).params
+    assert (d.use_rigid_contact_solver, d.rigid_contact_gamma, d.rigid_contact_beta) == (0, 0.7, 1.0)
+    assert d.rigid_contact_support_radius_factor == 4.0 and d.rigid_contact_friction_coeff == 0.0
+
+
+def test_oracle_contact_penalty_and_manager_blocks():
+    """Oracle restatement of the penalty contact (RigidContactSolver.cpp:307-555) and the
+    manager chain (RigidBodyGradientManager.cpp:96-468): the spheres, pushed together, are
+    driven apart; the samples in contact carry forces; the cross blocks [R][RR] and the
+    cross chain state are non-zero and finite."""
+    import oracle
+    sc = scn.two_sphere_contact(speed=0.5)
+    o = oracle.Oracle(sc, mode=oracle.MODE_F64)
+    o.step(1)
+    nc, na = o.contact_count()
+    assert 0 < na <= nc
+    o.step(2)
+    assert o.rigid_state(1)[2][0] < 0.0 < o.rigid_state(2)[2][0]
+    Fx12 = o.manager_jacobians(1, 2)[9:18]
+    assert np.linalg.norm(Fx12) > 0 and np.all(np.isfinite(o.manager_jacobians(2, 1)))
+    g21 = o.manager_grad(2, 1)
+    assert np.linalg.norm(g21) > 0 and np.all(np.isfinite(g21))
+    # without contact the cross terms stay exactly zero
+    far = scn.two_sphere_contact(gap=0.3, speed=0.0)  # clear of each other and of the walls
+    o2 = oracle.Oracle(far, mode=oracle.MODE_F64)
+    o2.step(3)
+    assert o2.contact_count() == (0, 0)
+    assert np.all(o2.manager_grad(2, 1) == 0.0) and np.all(o2.manager_jacobians(1, 2) == 0.0)
+
+
+def test_oracle_manager_reset_gradient_keeps_blocks():
+    """reset_gradient restarts the manager's chain state but keeps its blocks (the next
+    step's fluid stage reads the last contact blocks); reset clears both."""
+    import oracle
+    o = oracle.Oracle(scn.two_sphere_contact(), mode=oracle.MODE_F64)
+    o.step(3)
+    jac = o.manager_jacobians(1, 2).copy()
+    o.reset_gradient()
+    assert np.array_equal(o.manager_jacobians(1, 2), jac)
+    g = oracle.grad_blocks(o.manager_grad(1, 1))
+    assert np.array_equal(g["v_v0"], np.eye(3)) and not g["x_v0"].any()
+    o.reset()
+    assert not o.manager_jacobians(1, 2).any()
