@@ -77,7 +77,7 @@ def pool_adjoint(steps=1000, every=50, eps=1e-4, fd=True):
         loss = _loss_torch(out, body, x_t, q_t)
         loss.backward()
         res[f"{name}_s"] = time.perf_counter() - t0
-        grads[name] = (out.detach().numpy(), p.grad.numpy()[body].copy(), float(loss))
+        grads[name] = (out.detach().numpy(), p.grad.numpy()[body].copy(), float(loss.detach()))
     (oc, gc, lc), (od, gd, ld) = grads["checkpointed"], grads["direct"]
     res["forward_identical"] = bool(np.array_equal(oc, od))
     res["max_rel_grad_diff_checkpointed_vs_direct"] = float(np.max(np.abs(gc - gd)) / max(np.max(np.abs(gd)), 1e-300))
