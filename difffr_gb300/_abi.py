@@ -79,6 +79,7 @@ class DfsphParams(ctypes.Structure):
         ("rigid_contact_beta", c_double),
         ("rigid_contact_support_radius_factor", c_double),
         ("rigid_contact_friction_coeff", c_double),
+        ("viscosity_boundary", c_double),
     ]
 
 

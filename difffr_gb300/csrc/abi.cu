@@ -99,6 +99,7 @@ int dfsph_default_params(dfsph_params *p) {
   p->rigid_contact_beta = 1.0;
   p->rigid_contact_support_radius_factor = 4.0;
   p->rigid_contact_friction_coeff = 0.0;
+  p->viscosity_boundary = 0.0;
   return DFSPH_OK;
 }
 

@@ -90,6 +90,7 @@ Engine<T>::Engine(const dfsph_scene *sc) {
   if (P_.cfl_method == 1 && !(P_.cfl_min_time_step > 0 && P_.cfl_max_time_step >= P_.cfl_min_time_step))
     throw DfsphException(DFSPH_ERR_INVALID_ARG, "CFL time step bounds");
   fc_.visc = (T)P_.viscosity;
+  fc_.visc_b = (T)P_.viscosity_boundary;
   {  // Akinci2013 surface tension constants (SPHKernels.h:446-452, 516-520)
     const double hs = 4.0 * P_.particle_radius;
     fc_.st_k = (T)P_.surface_tension;
@@ -820,7 +821,7 @@ int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
         pend(DFSPH_K_BF_LISTS, nd_);
       }
       check_launch();
-      xs_fuse_ = P_.surface_tension_method != 2;
+      xs_fuse_ = P_.surface_tension_method != 2 && P_.viscosity_boundary == 0.0;
       xs_done_ = false;
       if (P_.enable_divergence_solver) solve(false);
       else { last_iters_v_ = 0; last_err_v_ = 0.0; }
@@ -832,14 +833,20 @@ int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
           k_normals<T><<<blocks(n_), 256, 0, stream_>>>(fc_, R_[cur_].p, flist_.p, fcount_.p, rho_.p, N_.p);
           k_xsph_advect<T, true><<<blocks(n_ * LPP), 256, 0, stream_>>>(fc_, R_[cur_].p, R_[nv].p, flist_.p,
                                                                         fcount_.p, kappaV_[cur_].p, scale_kv, N_.p,
-                                                                        BR_.p, blist_.p, bcount_.p);
+                                                                        BR_.p, blist_.p, bcount_.p, rho_.p);
           launched();
         } else {
           k_xsph_advect<T, false><<<blocks(n_ * LPP), 256, 0, stream_>>>(fc_, R_[cur_].p, R_[nv].p, flist_.p,
                                                                          fcount_.p, kappaV_[cur_].p, scale_kv, nullptr,
-                                                                         nullptr, nullptr, nullptr);
+                                                                         BR_.p, blist_.p, bcount_.p, rho_.p);
         }
         launched();
+        if (P_.viscosity_boundary != 0.0 && nd_ > 0) {
+          // the bodies' reaction, from the velocities before the XSPH update (still in R_[cur_])
+          k_visc_boundary_force<T><<<blocks(nd_), 256, 0, stream_>>>(fc_, nd_, xd_.p, vd_.p, R_[cur_].p, rho_.p,
+                                                                     bflist_.p, bfcount_.p, acc_.p);
+          launched();
+        }
       }
       pend(DFSPH_K_XSPH, n_);
       // the advected state lives in the other record buffer: swap the record pair only

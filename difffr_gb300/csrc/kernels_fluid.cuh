@@ -32,6 +32,7 @@ struct FluidConsts {
   int kf, kb;  // list capacities
   // Akinci2013 surface tension: coefficients, cohesion kernel k and c, adhesion kernel k
   T st_k, st_kb, coh_k, coh_c, adh_k;
+  T visc_b;  // XSPH coefficient against boundary samples (viscosityBoundary)
 };
 
 // |r|^2 summed as Eigen's squaredNorm sums a 3-vector (float: x^2 + (y^2 + z^2); double:
@@ -538,13 +539,16 @@ static __global__ void __launch_bounds__(256, DFSPH_VELOCITY_MIN_BLOCKS) k_veloc
 // ST: Akinci2013 surface tension first (SurfaceTension_Akinci2013.cpp:60-148; it runs before
 // the viscosity, Simulation.cpp:618-631): cohesion and curvature over fluid neighbours with
 // K_ij = 2 rho0 / (rho_i + rho_j), adhesion over boundary neighbours; N[j] = (n_j, rho_j).
+// With visc_b != 0 the boundary term of Viscosity_XSPH::step (:72-82):
+// a_i += -(1/h) visc_b (rho0 psi_j / rho_i) (v_i - v_j) W_ij over boundary neighbours (the
+// bodies' reaction is summed per sample by k_visc_boundary_force).
 template <class T, bool ST>
 static __global__ void __launch_bounds__(256, DFSPH_XSPH_MIN_BLOCKS) k_xsph_advect(FluidConsts<T> c, const Rec<T> *__restrict__ R,
                                                             Rec<T> *__restrict__ R_out, const int *__restrict__ flist,
                                                             const int *__restrict__ fcount, T *__restrict__ kappaV,
                                                             int scale_kappaV, const V4<T> *__restrict__ N,
                                                             const Rec<T> *__restrict__ BR, const int *__restrict__ blist,
-                                                            const int *__restrict__ bcount) {
+                                                            const int *__restrict__ bcount, const T *__restrict__ rho) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = t / LPP, s = t % LPP;
   const bool live = i < c.n;
@@ -591,6 +595,19 @@ static __global__ void __launch_bounds__(256, DFSPH_XSPH_MIN_BLOCKS) k_xsph_adve
       ay -= f * (vi.y - d.v.y) * w;
       az -= f * (vi.z - d.v.z) * w;
     });
+    if (c.visc_b != T(0)) {
+      const T fb = -c.invH * c.visc_b;
+      const T rho_i = rho[i];
+      for_neighbors_sub<DFSPH_XSPH_BATCH, Rec<T>>(bcount[i], blist, c.n, i, s, [&](int j) { return ld_rec(BR + j); },
+                                                  [&](const Rec<T> &d) {
+        const T rx = xi.x - d.x.x, ry = xi.y - d.x.y, rz = xi.z - d.x.z;
+        const T w = KEval<T>::W(rx * rx + ry * ry + rz * rz, c.kc);
+        const T f = fb * (c.rho0 * d.x.w / rho_i);
+        ax += f * (vi.x - d.v.x) * w;
+        ay += f * (vi.y - d.v.y) * w;
+        az += f * (vi.z - d.v.z) * w;
+      });
+    }
   }
   ax = sub_sum(ax); ay = sub_sum(ay); az = sub_sum(az);
   if (live && s == 0) {

@@ -315,6 +315,34 @@ static __global__ void __launch_bounds__(256) k_max_speed2(int n, const Rec<T> *
 // torque sum (x_j - x_b) x F_j, stores F, T and the net Jacobians, and zeroes the rows
 // (BoundaryModel_Akinci2012::accumulate_and_reset_gradient, :453-497;
 // BoundaryModel::getForceAndTorque / clearForceAndTorque, BoundaryModel.cpp:38-85).
+// The bodies' reaction to the boundary XSPH term (Viscosity_XSPH.cpp:72-82:
+// bm->addForce(x_j, -m_i a_ij)), summed per dynamic sample over its fluid neighbours in
+// list order from the velocities before the XSPH update, into the sample's force row.
+template <class T>
+static __global__ void k_visc_boundary_force(FluidConsts<T> c, int nd, const V4<T> *__restrict__ xd,
+                                             const V4<T> *__restrict__ vd, const Rec<T> *__restrict__ R,
+                                             const T *__restrict__ rho, const int *__restrict__ bflist,
+                                             const int *__restrict__ bfcount, double *__restrict__ acc) {
+  const int d = blockIdx.x * blockDim.x + threadIdx.x;
+  if (d >= nd) return;
+  const V4<T> xj = xd[d], vj = vd[d];
+  const T fb = -c.invH * c.visc_b;
+  T f[3] = {T(0), T(0), T(0)};
+  const int cnt = bfcount[d];
+  for (int k = 0; k < cnt; k++) {
+    const int i = bflist[(size_t)k * nd + d];
+    const Rec<T> ri = R[i];
+    const T rx = ri.x.x - xj.x, ry = ri.x.y - xj.y, rz = ri.x.z - xj.z;
+    const T w = KEval<T>::W(rx * rx + ry * ry + rz * rz, c.kc);
+    const T s = fb * (c.rho0 * xj.w / rho[i]);
+    f[0] -= c.m * (s * (ri.v.x - vj.x) * w);
+    f[1] -= c.m * (s * (ri.v.y - vj.y) * w);
+    f[2] -= c.m * (s * (ri.v.z - vj.z) * w);
+  }
+  double *row = acc + (size_t)d * ACC_STRIDE;
+  for (int k = 0; k < 3; k++) row[ACC_FORCE + k] += (double)f[k];
+}
+
 // Two stages so that many SMs share the reads: k_body_partials sums each chunk of
 // RED_CHUNK consecutive samples of one body in sample order; k_body_final sums a body's
 // chunk partials in chunk order.

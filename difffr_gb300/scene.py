@@ -64,6 +64,7 @@ class Params:
     rigid_contact_beta: float = 1.0
     rigid_contact_support_radius_factor: float = 4.0
     rigid_contact_friction_coeff: float = 0.0
+    viscosity_boundary: float = 0.0
 
 
 @dataclass

@@ -39,7 +39,7 @@ CONFIG_KEYS = {
     "useRigidContactSolver": "use_rigid_contact_solver", "useRigidGradientManager": "use_rigid_gradient_manager",
     "rigidContactGamma": "rigid_contact_gamma", "rigidContactBeta": "rigid_contact_beta",
     "rigidContactSupportRadiusFactor": "rigid_contact_support_radius_factor",
-    "rigidContactFrictionCoeff": "rigid_contact_friction_coeff",
+    "rigidContactFrictionCoeff": "rigid_contact_friction_coeff", "viscosityBoundary": "viscosity_boundary",
 }
 
 
@@ -100,7 +100,8 @@ def load_scene(path_or_dict, precision=0, seed=0):
     cfg = dict(data.get("Configuration", {}))
     # fluid material keys ("Materials" entries, SceneLoader.cpp) apply to the one fluid
     for mat in data.get("Materials", []):
-        for k in ("surfaceTensionMethod", "surfaceTension", "surfaceTensionBoundary", "viscosity"):
+        for k in ("surfaceTensionMethod", "surfaceTension", "surfaceTensionBoundary", "viscosity",
+                  "viscosityBoundary"):
             if k in mat:
                 cfg[k] = mat[k]
     kw = {}

@@ -108,6 +108,9 @@ typedef struct dfsph_params {
   double  rigid_contact_beta;          /* "rigidContactBeta" (penalty stiffness), default 1.0 */
   double  rigid_contact_support_radius_factor; /* "rigidContactSupportRadiusFactor", default 4.0 */
   double  rigid_contact_friction_coeff; /* "rigidContactFrictionCoeff", default 0.0 */
+  double  viscosity_boundary;          /* XSPH coefficient against boundary samples, with the
+                                          reaction on dynamic bodies (Viscosity_XSPH.cpp:72-82);
+                                          material "viscosityBoundary", default 0 */
 } dfsph_params;
 
 /*

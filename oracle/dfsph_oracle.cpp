@@ -1250,6 +1250,16 @@ struct Sim : Base {
         const int j = ff[s];
         ai -= invH * visc * (mf / rho[j]) * (v[i] - v[j]) * K.W(x[i] - x[j]);
       }
+      // boundary term and the bodies' reaction (Viscosity_XSPH.cpp:72-82)
+      if (P.viscosity_boundary != 0.0) {
+        const F vb = (F)P.viscosity_boundary;
+        for (int64_t s = fbS[i]; s < fbS[i + 1]; s++) {
+          const int j = fb[s];
+          const V3F aa = -invH * vb * (rho0 * psi[j] / rho[i]) * (v[i] - bv[j]) * K.W(x[i] - bx[j]);
+          ai += aa;
+          add_force(bbody[j], bx[j], V3F(-mf * aa));
+        }
+      }
       a[i] = ai;
     }
     // Simulation::updateTimeStepSize (Simulation.cpp:524-616, called at

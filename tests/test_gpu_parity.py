@@ -191,6 +191,28 @@ def test_surface_tension_akinci2013_matches_oracle(gpu_lib, oracle_lib, precisio
     assert rel(g2.field(_abi.FIELD_V), gpu.field(_abi.FIELD_V)) > 10 * tol
 
 
+@pytest.mark.parametrize("precision", [_abi.DFSPH_FP64, _abi.DFSPH_FP32])
+def test_boundary_viscosity_matches_oracle(gpu_lib, oracle_lib, precision):
+    """XSPH viscosity against the boundary samples with the bodies' reaction
+    (Viscosity_XSPH.cpp:72-82, viscosityBoundary 0.5), against the oracle: fields, the
+    rigid state and the body's fluid force within 1e-9 (FP64) or 1e-4 (FP32) after 6 steps;
+    the term changes both the flow and the force on the sphere."""
+    sc = scn.small_contact_scene(precision=precision, viscosity_boundary=0.5, sphere_v=(1.0, -0.5, 0.0))
+    gpu, ref = make(sc), oracle_lib.Oracle(sc)
+    gpu.step(6)
+    ref.step(6)
+    tol = 1e-9 if precision == _abi.DFSPH_FP64 else 1e-4
+    for f in (_abi.FIELD_X, _abi.FIELD_DENSITY, _abi.FIELD_V):
+        assert rel(gpu.field(f), ref.field(f)) < tol, f
+    for a, b in zip(gpu.rigid_state(1), ref.rigid_state(1)):
+        assert rel(a, b) < tol
+    assert rel(gpu.rigid_force(1)[0], ref.rigid_force(1)[0]) < 10 * tol
+    plain = make(scn.small_contact_scene(precision=precision, sphere_v=(1.0, -0.5, 0.0)))
+    plain.step(6)
+    assert rel(plain.field(_abi.FIELD_V), gpu.field(_abi.FIELD_V)) > 10 * tol
+    assert rel(plain.rigid_force(1)[0], gpu.rigid_force(1)[0]) > 10 * tol
+
+
 def test_cfl_time_stepping_matches_oracle(gpu_lib, oracle_lib):
     """Adaptive CFL step size (Simulation::updateTimeStepSizeCFL): from 1 ms the size goes to
     the 5 ms cap while the boundary samples are still at rest, then drops below it once the
