@@ -554,11 +554,15 @@ class _SimulatorBase:
     def getValueFloat(self, key):
         return self._values.get(key, 0.0)
 
+    def _moving_bodies(self):
+        return [k for k, b in enumerate(self._scene.bodies) if b.is_dynamic or b.is_animated]
+
     def saveState(self, path=""):
         """Snapshot of the full state kept on the device; returns a handle string usable
-        with loadStateWithRigidExisted. When `path` is given, the fluid particles (position,
-        velocity, kappa, kappa_v, id) are also written there as
-        state_<time>_particle_Fluid.bgeo, the reference's state-export file."""
+        with loadStateWithRigidExisted. When `path` is given, the reference's state-export
+        files are written there too (SimulatorBase::saveState): the fluid particles
+        (position, velocity, kappa, kappa_v, id) as state_<n>_particle_Fluid.bgeo and the
+        dynamic and animated bodies' records as state_<n>_dynamicRB.bin, n the step count."""
         from . import _abi
         slot = self._sim.checkpoint_save()
         name = os.path.join(path or self._output, f"state_{slot}")
@@ -566,21 +570,40 @@ class _SimulatorBase:
         self._saved[name + ".bin"] = slot
         if path:
             from .partio_bgeo import write_bgeo
+            from .state_bin import write_dynamic_rb
             os.makedirs(path, exist_ok=True)
-            t = self._sim.time()[0]
-            fn = os.path.join(path, f"state_{t:.6f}_particle_Fluid.bgeo")
+            prefix = os.path.join(path, f"state_{self._sim.time()[1]}")
+            fn = prefix + "_particle_Fluid.bgeo"
             write_bgeo(fn, self._sim.field(_abi.FIELD_X), velocity=self._sim.field(_abi.FIELD_V),
                        kappa=self._sim.field(_abi.FIELD_KAPPA), kappa_v=self._sim.field(_abi.FIELD_KAPPA_V),
                        id=np.arange(self._sim.n_fluid, dtype=np.int32))
-            self._saved[fn] = slot
+            real = np.float64 if self._scene.params.fluid_precision == _abi.DFSPH_FP64 else np.float32
+            write_dynamic_rb(prefix + "_dynamicRB.bin", [self._sim.rigid_state(b) for b in self._moving_bodies()],
+                             real=real)
         return name
 
     def loadStateWithRigidExisted(self, name):
-        """Restores a state saved in this session; a .bgeo file from elsewhere sets the fluid's
-        positions and velocities (and kappa fields when present) and keeps the rigid bodies."""
+        """Restores a state saved in this session. From files: a state .bin (the reference's
+        state_<n>.bin or state_<n>_dynamicRB.bin) sets the dynamic and animated bodies' pose
+        and velocities from its rigid records and the fluid from the state_<n>_particle_Fluid.bgeo
+        beside it when present; a .bgeo file sets the fluid's positions and velocities (and
+        kappa fields when present) and keeps the rigid bodies."""
         from . import _abi
         if name in self._saved:
             self._sim.checkpoint_restore(self._saved[name])
+            return
+        if name.endswith(".bin"):
+            from .state_bin import read_rigid_records
+            moving = self._moving_bodies()
+            recs, _ = read_rigid_records(name, len(moving))
+            for b, (x, q, v, w) in zip(moving, recs):
+                self._sim.set_rigid_state(b, x, q, v, w)
+            stem = name[:-4]
+            if stem.endswith("_dynamicRB"):
+                stem = stem[: -len("_dynamicRB")]
+            fluid = stem + "_particle_Fluid.bgeo"
+            if os.path.exists(fluid):
+                self.loadStateWithRigidExisted(fluid)
             return
         from .partio_bgeo import read_bgeo
         st = read_bgeo(name)

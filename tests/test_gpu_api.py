@@ -197,6 +197,7 @@ def test_pysplishsplash_state_files(gpu_lib, tmp_path):
     assert len(files) == 1
     x1 = base._sim.positions().copy()
     v1 = base._sim.velocities().copy()
+    rigid1 = [np.asarray(a).copy() for a in base._sim.rigid_state(1)]
     base.cleanup()
     # a fresh simulator of the same scene takes the fluid from the file
     other = Exec.SimulatorBase()
@@ -207,3 +208,15 @@ def test_pysplishsplash_state_files(gpu_lib, tmp_path):
     assert np.allclose(other._sim.positions(), x1, atol=1e-6)
     assert np.allclose(other._sim.velocities(), v1, atol=1e-6)
     other.cleanup()
+    # the rigid records (state_<n>_dynamicRB.bin) set the body's pose and velocities, and the
+    # fluid file beside them is read too
+    rb = glob.glob(str(tmp_path / "state_*_dynamicRB.bin"))
+    assert len(rb) == 1
+    third = Exec.SimulatorBase()
+    third.init(scene=sc)
+    third.initSimulation()
+    third.loadStateWithRigidExisted(rb[0])
+    for a, b in zip(third._sim.rigid_state(1), rigid1):
+        assert np.allclose(a, b, rtol=1e-6, atol=1e-6)
+    assert np.allclose(third._sim.positions(), x1, atol=1e-6)
+    third.cleanup()

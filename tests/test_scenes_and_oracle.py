@@ -340,3 +340,43 @@ def test_oracle_manager_reset_gradient_keeps_blocks():
     assert np.array_equal(g["v_v0"], np.eye(3)) and not g["x_v0"].any()
     o.reset()
     assert not o.manager_jacobians(1, 2).any()
+
+
+@pytest.mark.parametrize("real", [np.float32, np.float64])
+def test_state_bin_rigid_records_round_trip(tmp_path, real):
+    """state_<n>_dynamicRB.bin (SimulatorBase.cpp:1985-2000): raw (x, q as x y z w, v, omega)
+    per moving body; read back from the end of the file with the scalar type detected."""
+    from difffr_gb300.state_bin import read_rigid_records, write_dynamic_rb
+    rng = np.random.default_rng(0)
+    recs = []
+    for _ in range(3):
+        q = rng.normal(size=4)
+        recs.append((rng.normal(size=3), q / np.linalg.norm(q), rng.normal(size=3), rng.normal(size=3)))
+    f = tmp_path / "state_7_dynamicRB.bin"
+    write_dynamic_rb(str(f), recs, real=real)
+    assert f.stat().st_size == 3 * 13 * np.dtype(real).itemsize
+    got, dt = read_rigid_records(str(f), 3)
+    assert dt == np.dtype(real)
+    tol = 1e-6 if real == np.float32 else 0.0
+    for a, b in zip(got, recs):
+        for u, w in zip(a, b):
+            np.testing.assert_allclose(u, w, atol=tol, rtol=tol)
+    # a main state file: arbitrary header bytes, then the same records
+    g = tmp_path / "state_7.bin"
+    g.write_bytes(b"\x20\x00\x00\x00" + bytes(range(200)) + f.read_bytes())
+    got2, _ = read_rigid_records(str(g), 3)
+    np.testing.assert_array_equal(got2[1][0], got[1][0])
+
+
+@pytest.mark.skipif(not os.path.isdir("/root/reference/experiments"), reason="reference checkout not present")
+def test_reference_state_file_rigid_records():
+    """The reference's billiards state (state/billiards/state_17.bin, two moving balls):
+    float records with unit quaternions at the end of the file."""
+    from difffr_gb300.state_bin import read_rigid_records
+    f = "/root/reference/experiments/rigid_body_trajectory_optimization/state/billiards/state_17.bin"
+    recs, dt = read_rigid_records(f, 2)
+    assert dt == np.dtype(np.float32)
+    np.testing.assert_allclose(recs[0][0], [-0.95, 0.7864, 0.0], atol=1e-4)
+    np.testing.assert_allclose(recs[1][0], [-0.1, 0.4316, -0.0001], atol=1e-4)
+    for x, q, v, w in recs:
+        assert abs(np.linalg.norm(q) - 1.0) < 1e-6
