@@ -60,7 +60,7 @@ def _quat_matrix(q):
                      [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
 
 
-def _body_samples(b, base_dir, r):
+def _body_samples(b, base_dir, r, seed=0):
     sp = 2.0 * r
     scale = np.asarray(b.get("scale", [1.0, 1.0, 1.0]), dtype=np.float64)
     pf = b.get("particleFile", "")
@@ -72,7 +72,8 @@ def _body_samples(b, base_dir, r):
     gpath = gf if os.path.isabs(gf) else os.path.join(base_dir, gf)
     if gf.lower().endswith(".obj") and os.path.exists(gpath):
         from .mesh_sampling import sample_obj
-        return sample_obj(gpath, scale, r)
+        # "samplingMode" (SceneLoader.cpp:147-148): 0 Poisson disk (the default), 1 regular triangle
+        return sample_obj(gpath, scale, r, mode=int(b.get("samplingMode", 0)), seed=seed)
     g = os.path.basename(gf).lower()
     if "box" in g:
         half = 0.5 * scale
@@ -148,10 +149,10 @@ def load_scene(path_or_dict, precision=0, seed=0):
     fx = np.vstack(fluid) if fluid else np.zeros((0, 3))
     fv = np.vstack(fvel) if fluid else np.zeros((0, 3))
     bodies = []
-    for b in data.get("RigidBodies", []):
+    for k, b in enumerate(data.get("RigidBodies", [])):
         q = quat_from_axis_angle(b.get("rotationAxis", [1, 0, 0]), float(b.get("rotationAngle", 0.0)))
         bodies.append(scn.Body(
-            samples=_body_samples(b, base_dir, r), translation=tuple(b.get("translation", [0, 0, 0])), rotation=q,
+            samples=_body_samples(b, base_dir, r, seed=seed + 101 * k), translation=tuple(b.get("translation", [0, 0, 0])), rotation=q,
             density=float(b.get("density", 1000.0)), is_dynamic=bool(b.get("isDynamic", False)),
             is_animated=bool(b.get("isAnimated", False)), init_velocity=tuple(b.get("initVelocity", [0, 0, 0])),
             init_angular_velocity=tuple(b.get("initAngularVelocity", [0, 0, 0])),

@@ -380,3 +380,34 @@ def test_reference_state_file_rigid_records():
     np.testing.assert_allclose(recs[1][0], [-0.1, 0.4316, -0.0001], atol=1e-4)
     for x, q, v, w in recs:
         assert abs(np.linalg.norm(q) - 1.0) < 1e-6
+
+
+def test_poisson_disk_sampling_flat_and_cube(tmp_path):
+    """Poisson-disk surface sampling (PoissonDiskSampling.cpp, minimum distance r): on a flat
+    square every pair of samples is at least r apart and the density is that of a maximal
+    Poisson-disk set (0.5-0.8 samples per r^2); on a cube all samples lie on the faces; the
+    sampling is deterministic for a seed; the scene loader uses it by default (samplingMode 0)
+    and the regular triangle pattern for samplingMode 1."""
+    from scipy.spatial import cKDTree
+    from difffr_gb300.mesh_sampling import poisson_disk_samples
+    r = 0.02
+    v = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0]], dtype=np.float64)
+    f = np.array([[0, 1, 2], [0, 2, 3]])
+    s = poisson_disk_samples(v, f, r, seed=1)
+    d, _ = cKDTree(s).query(s, k=2)
+    assert d[:, 1].min() >= r
+    assert 0.5 < s.shape[0] * r * r < 0.8
+    assert np.all(np.abs(s[:, 2]) < 1e-12) and s[:, :2].min() >= 0 and s[:, :2].max() <= 1
+    assert np.array_equal(s, poisson_disk_samples(v, f, r, seed=1))
+    path = tmp_path / "UnitBox.obj"
+    _write_cube_obj(path)
+    body = {"geometryFile": "UnitBox.obj", "scale": [1, 1, 1], "isDynamic": True}
+    cfg = {"Configuration": {"particleRadius": 0.02}, "RigidBodies": [body], "FluidBlocks": []}
+    (tmp_path / "a.json").write_text(json.dumps(cfg))
+    pd = load_scene(str(tmp_path / "a.json")).bodies[0].samples
+    assert np.allclose(np.max(np.abs(pd), axis=1), 0.5)
+    assert 0.5 < pd.shape[0] * 0.02 ** 2 / 6.0 < 0.8
+    body["samplingMode"] = 1
+    (tmp_path / "b.json").write_text(json.dumps(cfg))
+    rt = load_scene(str(tmp_path / "b.json")).bodies[0].samples
+    assert rt.shape[0] != pd.shape[0]
