@@ -189,6 +189,10 @@ static __global__ void __launch_bounds__(LIST_THREADS) k_lists_density_factor(
   T sgk = T(0);
   T delta = T(0);
   V3<T> gpi = {T(0), T(0), T(0)};
+  // Two phases, so that the kernel arithmetic runs once per neighbour: the lane's candidate
+  // scan only appends accepted indices (about one candidate in eight is accepted, so a
+  // fused accept branch would be taken by some lane of the warp nearly every iteration),
+  // then the lane walks its own list in order. Same neighbours, same order, same formulas.
   int cnt = 0;
   for_each_row(c.grid, cstartF, cx, cy, cz, [&](int b, int e) {
     for (int j0 = b; j0 < e; j0 += 4) {
@@ -201,49 +205,67 @@ static __global__ void __launch_bounds__(LIST_THREADS) k_lists_density_factor(
         const int j = j0 + u;
         if (j >= e || j == i) continue;
         const T dx = xi.x - xs[u].x, dy = xi.y - xs[u].y, dz = xi.z - xs[u].z;
-        const T d2 = dist2_rn(dx, dy, dz);
-        if (d2 < c.h2) {
+        if (dist2_rn(dx, dy, dz) < c.h2) {
           if (cnt < c.kf) flist[(size_t)cnt * c.n + i] = j;
           cnt++;
-          dens += c.V * KEval<T>::W(d2, c.kc);
-          const T g = KEval<T>::G(d2, c.kc);
-          const V3<T> gpj = (-c.V) * V3<T>{g * dx, g * dy, g * dz};
-          sgk += dot(gpj, gpj);
-          gpi = gpi - gpj;
-          if (DIVWARM) {  // the velocity only for accepted neighbours
-            const V4<T> vj = R[j].v;
-            delta += c.V * (g * ((vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz));
-          }
         }
       }
     }
   });
   if (cnt > c.kf) { atomicOr(err, ERR_FLUID_LIST_OVERFLOW); cnt = c.kf; }
   fcount[i] = cnt;
+  for (int k0 = 0; k0 < cnt; k0 += 4) {
+    int js[4];
+    V4<T> xs[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) js[u] = (k0 + u < cnt) ? flist[(size_t)(k0 + u) * c.n + i] : i;
+#pragma unroll
+    for (int u = 0; u < 4; u++) xs[u] = R[js[u]].x;
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      if (k0 + u >= cnt) break;
+      const T dx = xi.x - xs[u].x, dy = xi.y - xs[u].y, dz = xi.z - xs[u].z;
+      const T d2 = dist2_rn(dx, dy, dz);
+      dens += c.V * KEval<T>::W(d2, c.kc);
+      const T g = KEval<T>::G(d2, c.kc);
+      const V3<T> gpj = (-c.V) * V3<T>{g * dx, g * dy, g * dz};
+      sgk += dot(gpj, gpj);
+      gpi = gpi - gpj;
+      if (DIVWARM) {
+        const V4<T> vj = R[js[u]].v;
+        delta += c.V * (g * ((vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz));
+      }
+    }
+  }
   int bc = 0;
-  auto visit_boundary = [&](int b, int e, int off) {
+  auto scan_boundary = [&](int b, int e, int off) {
     for (int j = b; j < e; j++) {
       const V4<T> xj = BR[off + j].x;
       const T dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
-      const T d2 = dist2_rn(dx, dy, dz);
-      if (d2 < c.h2) {
+      if (dist2_rn(dx, dy, dz) < c.h2) {
         if (bc < c.kb) blist[(size_t)bc * c.n + i] = off + j;
         bc++;
-        dens += xj.w * KEval<T>::W(d2, c.kc);
-        const T g = KEval<T>::G(d2, c.kc);
-        const V3<T> gpj = (-xj.w) * V3<T>{g * dx, g * dy, g * dz};
-        gpi = gpi - gpj;
-        if (DIVWARM) {
-          const V4<T> vj = BR[off + j].v;
-          delta += xj.w * (g * ((vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz));
-        }
       }
     }
   };
-  for_each_row(c.grid, cstartS, cx, cy, cz, [&](int b, int e) { visit_boundary(b, e, 0); });
-  if (cstartD) for_each_row(c.grid, cstartD, cx, cy, cz, [&](int b, int e) { visit_boundary(b, e, ns); });
+  for_each_row(c.grid, cstartS, cx, cy, cz, [&](int b, int e) { scan_boundary(b, e, 0); });
+  if (cstartD) for_each_row(c.grid, cstartD, cx, cy, cz, [&](int b, int e) { scan_boundary(b, e, ns); });
   if (bc > c.kb) { atomicOr(err, ERR_BOUNDARY_LIST_OVERFLOW); bc = c.kb; }
   bcount[i] = bc;
+  for (int k = 0; k < bc; k++) {
+    const int j = blist[(size_t)k * c.n + i];
+    const V4<T> xj = BR[j].x;
+    const T dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+    const T d2 = dist2_rn(dx, dy, dz);
+    dens += xj.w * KEval<T>::W(d2, c.kc);
+    const T g = KEval<T>::G(d2, c.kc);
+    const V3<T> gpj = (-xj.w) * V3<T>{g * dx, g * dy, g * dz};
+    gpi = gpi - gpj;
+    if (DIVWARM) {
+      const V4<T> vj = BR[j].v;
+      delta += xj.w * (g * ((vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz));
+    }
+  }
   const T rh = dens * c.rho0;
   rho[i] = rh;
   R[i].v.w = c.m / rh;
