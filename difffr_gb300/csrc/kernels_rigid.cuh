@@ -677,30 +677,46 @@ static __global__ void __launch_bounds__(128) k_rigid_step(BodyState *__restrict
     }
   }
   if (t == 0 && cs.counts) { cs.counts[2 * b] = s_con; cs.counts[2 * b + 1] = s_act; }
+  const double dt = rc.dt;
+  auto add_force = [&](const double *f) { for (int k = 0; k < 3; k++) B.v[k] += B.invMass * f[k] * dt; };
+  auto add_torque = [&](const double *tq) {
+    double d[3], L[3], cr[3];
+    if (rc.gyroscopic) {
+      mv3(B.I, B.w, L);
+      cross3(L, B.w, cr);
+      for (int k = 0; k < 3; k++) cr[k] += tq[k];
+    } else for (int k = 0; k < 3; k++) cr[k] = tq[k];
+    mv3(B.Iinv, cr, d);
+    for (int k = 0; k < 3; k++) B.w[k] += d[k] * dt;
+  };
   if (t == 0 && B.dyn) {
-    const double dt = rc.dt;
     for (int k = 0; k < 3; k++) { B.wpre[k] = B.w[k]; }
     for (int k = 0; k < 4; k++) B.qpre[k] = B.q[k];
     for (int k = 0; k < 9; k++) { B.Ipre[k] = B.I[k]; B.Iipre[k] = B.Iinv[k]; }
-    auto add_force = [&](const double *f) { for (int k = 0; k < 3; k++) B.v[k] += B.invMass * f[k] * dt; };
-    auto add_torque = [&](const double *tq) {
-      double d[3], L[3], cr[3];
-      if (rc.gyroscopic) {
-        mv3(B.I, B.w, L);
-        cross3(L, B.w, cr);
-        for (int k = 0; k < 3; k++) cr[k] += tq[k];
-      } else for (int k = 0; k < 3; k++) cr[k] = tq[k];
-      mv3(B.Iinv, cr, d);
-      for (int k = 0; k < 3; k++) B.w[k] += d[k] * dt;
-    };
-    const double gm[3] = {rc.gx * B.mass, rc.gy * B.mass, rc.gz * B.mass};
     if (cs.rec) {
+      const double gm[3] = {rc.gx * B.mass, rc.gy * B.mass, rc.gz * B.mass};
       add_force(gm);
-      for (int k = 0; k < s_act; k++) {
-        const ContactRec &cr = cs.rec[cs.list[B.dstart + k]];
-        add_force(cr.f);
-        add_torque(cr.tau);
+    }
+  }
+  if (contact) {
+    // the force-carrying samples' forces and torques, in sample order; staged in shared
+    // memory by all threads so that the sequential part reads no global memory
+    constexpr int CH = 256;
+    __shared__ double sft[CH][6];
+    for (int base = 0; base < s_act; base += CH) {
+      const int m = min(CH, s_act - base);
+      for (int k = t; k < m; k += blockDim.x) {
+        const ContactRec &cr = cs.rec[cs.list[B.dstart + base + k]];
+        for (int e = 0; e < 3; e++) { sft[k][e] = cr.f[e]; sft[k][3 + e] = cr.tau[e]; }
       }
+      __syncthreads();
+      if (t == 0)
+        for (int k = 0; k < m; k++) { add_force(sft[k]); add_torque(sft[k] + 3); }
+      __syncthreads();
+    }
+  }
+  if (t == 0 && B.dyn) {
+    if (cs.rec) {
       const double zero[3] = {0.0, 0.0, 0.0};
       if (!B.anim)
         for (int rep = 0; rep < rc.nbodies; rep++) {
@@ -708,6 +724,7 @@ static __global__ void __launch_bounds__(128) k_rigid_step(BodyState *__restrict
           add_torque(rep == 0 ? B.T : zero);
         }
     } else if (!B.anim) {
+      const double gm[3] = {rc.gx * B.mass, rc.gy * B.mass, rc.gz * B.mass};
       add_force(B.F);
       add_torque(B.T);
       add_force(gm);

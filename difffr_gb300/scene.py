@@ -326,4 +326,21 @@ def two_sphere_contact(n=(20, 6, 10), r=0.025, seed=0, precision=_abi.DFSPH_FP64
                  name=f"two_sphere_contact_{fx.shape[0]}", steps=40)
 
 
+def sphere_on_floor(r=0.0125, precision=_abi.DFSPH_FP64, radius=0.8, gap=0.01, beta=5000.0, **kw):
+    """A large dynamic sphere resting `gap` above the floor of an empty container: several
+    hundred of its samples are in contact with the floor's at once (no fluid)."""
+    sp = 2.0 * r
+    box = (2.0 * radius + 0.4, 2.0 * radius + 0.4, 2.0 * radius + 0.4)
+    walls = box_surface((0.0, 0.0, 0.0), box, sp)
+    c = (0.5 * box[0], radius + gap, 0.5 * box[2])
+    bodies = [Body(samples=walls, density=1000.0),
+              Body(samples=sphere_surface(radius, sp), translation=c, density=800.0, is_dynamic=True,
+                   init_velocity=(0.1, 0.0, 0.0), init_angular_velocity=(0.0, 0.3, 0.2))]
+    kw.setdefault("time_step", 0.001)
+    params = Params(fluid_precision=precision, particle_radius=r, use_rigid_contact_solver=1,
+                    use_rigid_gradient_manager=1, rigid_contact_beta=beta, **kw)
+    return Scene(params=params, fluid_x=np.zeros((0, 3)), fluid_v=np.zeros((0, 3)), bodies=bodies,
+                 name="sphere_on_floor", steps=20)
+
+
 CONFIGS = {0: config0, 1: config1, 2: config2, 4: config4}

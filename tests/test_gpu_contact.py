@@ -148,3 +148,19 @@ def test_manager_checkpointed_rollout_equals_direct():
     np.testing.assert_array_equal(finals[0], finals[1])
     assert _rel(grads[1], grads[0]) < 1e-12
     assert np.abs(grads[0][1, :3]).max() > 0.0
+
+
+def test_many_contact_samples_without_fluid_matches_oracle():
+    """A large sphere on the floor of an empty container: several hundred force-carrying
+    samples on one body (the sequential application is staged in chunks), no fluid stage in
+    the manager chain; rigid state and the manager's chain state against the oracle."""
+    sc = scn.sphere_on_floor()
+    g, o = DiffDFSPH(sc), oracle.Oracle(sc, mode=oracle.MODE_F64)
+    for _ in range(10):
+        g.step(1)
+        o.step(1)
+        assert g.contact_count() == o.contact_count()
+        for a, c in zip(g.rigid_state(1), o.rigid_state(1)):
+            np.testing.assert_allclose(a, c, rtol=1e-8, atol=1e-10)
+    assert g.contact_count()[1] > 256
+    assert _rel(g.manager_grad(1, 1), o.manager_grad(1, 1)) < 1e-6
