@@ -257,6 +257,8 @@ class Engine : public EngineBase {
   // reductions and flags
   DBuf<double> partials_, resid_;
   double *resid_host_ = nullptr;  // pinned, mapped
+  int *err_host_ = nullptr;        // pinned: the error word, copied at the end of each step call
+  BodyState *hbs_pin_ = nullptr;   // pinned: the body states, copied at the end of each step call
   double *resid_host_dev_ = nullptr;
   DBuf<int> err_;
   Scanner scan_;
@@ -366,7 +368,14 @@ class Engine : public EngineBase {
   }
 
   int blocks(int n, int t = 256) const { return (n + t - 1) / t; }
-  void launched(int k = 1) { launches_ += k; }
+  void launched(int k = 1) { launches_ += k; dev_epoch_++; }
+  // host copy of the body states, refreshed when anything was launched or uploaded since
+  int64_t dev_epoch_ = 0, hbs_epoch_ = -1;
+  std::vector<BodyState> hbs_;
+  const BodyState &host_body(int b) {
+    if (hbs_epoch_ != dev_epoch_) { body_state_download(hbs_); hbs_epoch_ = dev_epoch_; }
+    return hbs_[b];
+  }
   void check_launch() { DF_CK(cudaGetLastError()); }
 
   void sort_fluid();
@@ -390,6 +399,7 @@ class Engine : public EngineBase {
   void body_state_download(std::vector<BodyState> &out);
   void body_state_upload(const std::vector<BodyState> &in);
   void check_error_word();
+  void raise_error_word(int e);
 };
 
 }  // namespace dfsph

@@ -262,6 +262,8 @@ Engine<T>::Engine(const dfsph_scene *sc) {
   resid_.alloc(4);
   err_.alloc(1);
   DF_CK(cudaHostAlloc((void **)&resid_host_, 4 * sizeof(double), cudaHostAllocMapped));
+  DF_CK(cudaHostAlloc((void **)&err_host_, sizeof(int), cudaHostAllocDefault));
+  DF_CK(cudaHostAlloc((void **)&hbs_pin_, std::max(nb_, 1) * sizeof(BodyState), cudaHostAllocDefault));
   DF_CK(cudaHostGetDevicePointer((void **)&resid_host_dev_, resid_host_, 0));
   DF_CK(cudaMemsetAsync(err_.p, 0, sizeof(int), stream_));
 
@@ -413,6 +415,8 @@ Engine<T>::~Engine() {
   for (auto &r : pending_) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
   for (auto &e : pool_) cudaEventDestroy(e);
   if (resid_host_) cudaFreeHost(resid_host_);
+  if (err_host_) cudaFreeHost(err_host_);
+  if (hbs_pin_) cudaFreeHost(hbs_pin_);
   if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -507,6 +511,7 @@ void Engine<T>::body_state_download(std::vector<BodyState> &out) {
 template <class T>
 void Engine<T>::body_state_upload(const std::vector<BodyState> &in) {
   if (nb_ == 0) return;
+  dev_epoch_++;
   DF_CK(cudaMemcpyAsync(bs_.p, in.data(), nb_ * sizeof(BodyState), cudaMemcpyHostToDevice, stream_));
   sync_all();
 }
@@ -597,6 +602,11 @@ template <class T>
 void Engine<T>::check_error_word() {
   int e = 0;
   DF_CK(cudaMemcpy(&e, err_.p, sizeof(int), cudaMemcpyDeviceToHost));
+  raise_error_word(e);
+}
+
+template <class T>
+void Engine<T>::raise_error_word(int e) {
   if (e) {
     std::string m = "device error word:";
     if (e & ERR_FLUID_LIST_OVERFLOW) m += " fluid neighbour list overflow (raise max_fluid_neighbors);";
@@ -756,8 +766,6 @@ void Engine<T>::rigid_end() {
     k_body_partials<T><<<nchunks_, RED_THREADS, 0, stream2_>>>(bs_.p, chunks_.p, xd_.p, acc_.p, red_part_.p);
     nl++;
   }
-  k_body_final<<<nb_, RED_THREADS, 0, stream2_>>>(bs_.p, nb_, body_chunks_.p, red_part_.p);
-  nl++;
   ContactStep cs{nullptr, nullptr, nullptr, ccount_.p, nullptr};
   if (contact_) {
     cc_.dt = rc_.dt;
@@ -772,15 +780,15 @@ void Engine<T>::rigid_end() {
     cs.list = clist_.p;
     if (mgr_blocks) { cs.blk = cblk_.p; cs.Mc = Mc_.p; }
   }
-  k_rigid_step<<<nb_, 128, 0, stream2_>>>(bs_.p, nb_, rc_, manager_ ? nullptr : tape_step, cs);
+  k_rigid_step<T><<<nb_, 128, 0, stream2_>>>(bs_.p, nb_, rc_, manager_ ? nullptr : tape_step, cs, body_chunks_.p,
+                                             red_part_.p, x0d_.p, xd_.p, vd_.p);
   nl++;
   if (mgr_chain || mgr_blocks) {
     MgrConsts mc{rc_.dt, nb_, rc_.gyroscopic, n_ > 0 ? 1 : 0, contact_ ? 1 : 0, 1, mgr_chain ? 1 : 0};
     k_manager_chain<<<1, 256, 0, stream2_>>>(bs_.p, mc, mgrM_.p, Mc_.p, mgrS_.p, mgr_chain ? tape_step : nullptr);
     nl++;
   }
-  k_boundary_update<T><<<blocks(nd_), 256, 0, stream2_>>>(bs_.p, nd_, x0d_.p, bodyd_.p, xd_.p, vd_.p, 1);
-  launched(nl + 1);
+  launched(nl);
   pend(DFSPH_K_RIGID, nd_, stream2_);
   DF_CK(cudaEventRecord(ev_rigid_done_, stream2_));
   rigid_pending_ = true;
@@ -790,6 +798,7 @@ void Engine<T>::rigid_end() {
 template <class T>
 int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
   if (nsteps < 0) throw DfsphException(DFSPH_ERR_INVALID_ARG, "nsteps < 0");
+  dev_epoch_++;
   int rc = DFSPH_OK;
   int64_t ti = 0, tv = 0;
   for (int s = 0; s < nsteps; s++) {
@@ -877,8 +886,16 @@ int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
     if (last_iters_ >= P_.max_iterations || (P_.enable_divergence_solver && last_iters_v_ >= P_.max_iterations_v))
       rc = DFSPH_ERR_NOT_CONVERGED;
   }
+  // the error word and the body states come back with the step's final synchronisation
+  // (the host mirror of the bodies is then current without another round trip)
+  wait_rigid();
+  if (nb_ > 0)
+    DF_CK(cudaMemcpyAsync(hbs_pin_, bs_.p, nb_ * sizeof(BodyState), cudaMemcpyDeviceToHost, stream_));
+  DF_CK(cudaMemcpyAsync(err_host_, err_.p, sizeof(int), cudaMemcpyDeviceToHost, stream_));
   sync_all();
-  check_error_word();
+  hbs_.assign(hbs_pin_, hbs_pin_ + nb_);
+  hbs_epoch_ = dev_epoch_;
+  raise_error_word(*err_host_);
   if (st) {
     st->steps_done = nsteps;
     st->pressure_iterations = last_iters_;
@@ -908,9 +925,7 @@ void Engine<T>::get_rigid_init(int b, double *v, double *w) {
 template <class T>
 void Engine<T>::get_rigid_state(int b, double *x, double *q, double *v, double *w) {
   if (b < 0 || b >= nb_) throw DfsphException(DFSPH_ERR_INVALID_ARG, "body index");
-  BodyState B;
-  sync_all();
-  DF_CK(cudaMemcpy(&B, bs_.p + b, sizeof(BodyState), cudaMemcpyDeviceToHost));
+  const BodyState &B = host_body(b);
   for (int k = 0; k < 3; k++) { if (x) x[k] = B.x[k]; if (v) v[k] = B.v[k]; if (w) w[k] = B.w[k]; }
   if (q) for (int k = 0; k < 4; k++) q[k] = B.q[k];
 }
@@ -930,24 +945,20 @@ void Engine<T>::set_rigid_velocity(int b, const double *v, const double *w) {
 template <class T>
 void Engine<T>::get_rigid_force(int b, double *F, double *Tq) {
   if (b < 0 || b >= nb_) throw DfsphException(DFSPH_ERR_INVALID_ARG, "body index");
-  std::vector<BodyState> bsv;
-  body_state_download(bsv);
-  for (int k = 0; k < 3; k++) { F[k] = bsv[b].F[k]; Tq[k] = bsv[b].T[k]; }
+  const BodyState &B = host_body(b);
+  for (int k = 0; k < 3; k++) { F[k] = B.F[k]; Tq[k] = B.T[k]; }
 }
 template <class T>
 void Engine<T>::get_rigid_mass(int b, double *m, double *I) {
   if (b < 0 || b >= nb_) throw DfsphException(DFSPH_ERR_INVALID_ARG, "body index");
-  std::vector<BodyState> bsv;
-  body_state_download(bsv);
-  *m = bsv[b].mass;
-  for (int k = 0; k < 9; k++) I[k] = bsv[b].I[k];
+  const BodyState &B = host_body(b);
+  *m = B.mass;
+  for (int k = 0; k < 9; k++) I[k] = B.I[k];
 }
 template <class T>
 void Engine<T>::get_rigid_grad(int b, double *out) {
   if (b < 0 || b >= nb_) throw DfsphException(DFSPH_ERR_INVALID_ARG, "body index");
-  std::vector<BodyState> bsv;
-  body_state_download(bsv);
-  const double *G = bsv[b].G;
+  const double *G = host_body(b).G;
   double *o = out;
   // x_v0 x_w0 q_v0 q_w0 v_v0 v_w0 w_v0 w_w0
   const int r0[4] = {0, 3, 7, 10}, nr[4] = {3, 4, 3, 3};
@@ -959,9 +970,8 @@ void Engine<T>::get_rigid_grad(int b, double *out) {
 template <class T>
 void Engine<T>::get_net_jacobians(int b, double *out) {
   if (b < 0 || b >= nb_) throw DfsphException(DFSPH_ERR_INVALID_ARG, "body index");
-  std::vector<BodyState> bsv;
-  body_state_download(bsv);
-  for (int k = 0; k < NJAC; k++) out[k] = bsv[b].nets[k];
+  const BodyState &B = host_body(b);
+  for (int k = 0; k < NJAC; k++) out[k] = B.nets[k];
 }
 template <class T>
 void Engine<T>::backward(const double *dL, double *out) {
@@ -1259,6 +1269,7 @@ void Engine<T>::checkpoint_restore(int slot) {
   DF_CK(cudaMemcpyAsync(kappa_[cur_].p, s.kap.p, N * sizeof(T), cudaMemcpyDeviceToDevice, stream_));
   DF_CK(cudaMemcpyAsync(kappaV_[cur_].p, s.kapV.p, N * sizeof(T), cudaMemcpyDeviceToDevice, stream_));
   DF_CK(cudaMemcpyAsync(perm_[cur_].p, s.perm.p, N * sizeof(int), cudaMemcpyDeviceToDevice, stream_));
+  dev_epoch_++;
   DF_CK(cudaMemcpyAsync(bs_.p, s.bs.p, NBd * sizeof(BodyState), cudaMemcpyDeviceToDevice, stream_));
   DF_CK(cudaMemcpyAsync(xd_.p, s.xd.p, ND * sizeof(V4<T>), cudaMemcpyDeviceToDevice, stream_));
   DF_CK(cudaMemcpyAsync(vd_.p, s.vd.p, ND * sizeof(V4<T>), cudaMemcpyDeviceToDevice, stream_));

@@ -344,8 +344,8 @@ static __global__ void k_visc_boundary_force(FluidConsts<T> c, int nd, const V4<
 }
 
 // Two stages so that many SMs share the reads: k_body_partials sums each chunk of
-// RED_CHUNK consecutive samples of one body in sample order; k_body_final sums a body's
-// chunk partials in chunk order.
+// RED_CHUNK consecutive samples of one body in sample order; k_rigid_step then sums a
+// body's chunk partials in chunk order.
 constexpr int RED_VALUES = 3 + NJAC + 3;  // force, jacobians, torque
 constexpr int RED_CHUNK = 16;
 constexpr int RED_THREADS = 128;
@@ -383,22 +383,6 @@ static __global__ void __launch_bounds__(RED_THREADS) k_body_partials(const Body
   for (int k = threadIdx.x; k < ch.count * ACC_STRIDE; k += blockDim.x) acc[(size_t)ch.start * ACC_STRIDE + k] = 0.0;
 }
 
-static __global__ void __launch_bounds__(RED_THREADS) k_body_final(BodyState *__restrict__ bs, int nbodies,
-                                                                   const int2 *__restrict__ body_chunks,
-                                                                   const double *__restrict__ part) {
-  const int b = blockIdx.x;
-  if (b >= nbodies) return;
-  BodyState &B = bs[b];
-  if (!B.dyn) return;
-  const int v = threadIdx.x;
-  if (v >= RED_VALUES) return;
-  const int2 r = body_chunks[b];
-  double tot = 0.0;
-  for (int c = r.x; c < r.y; c++) tot += part[(size_t)c * RED_VALUES + v];
-  if (v < 3) B.F[v] = tot;
-  else if (v < 3 + NJAC) B.nets[v - 3] = tot;
-  else B.T[v - 3 - NJAC] = tot;
-}
 
 // ------------------------------------------------------------------ chain rule + integration (FP64)
 static __device__ __forceinline__ void q_mul(const double *a, const double *b, double *o) {  // Hamilton, (w,x,y,z)
@@ -537,6 +521,27 @@ static __device__ void grad_RqTp_d(const double *q, const double *p, double *out
   grad_RqTp<double>(q[0], q[1], q[2], q[3], V3<double>{p[0], p[1], p[2]}, out);
 }
 
+// SimulatorBase::updateBoundaryParticles (SimulatorBase.cpp:1827-1857) for dynamic
+// samples: x_j = R(q) x0_j + x_b, v_j = omega x (x_j - x_b) + v_b, in FP64 then stored in T.
+template <class T>
+static __device__ __forceinline__ void sample_update(const BodyState &B, int d, const V4<T> *__restrict__ x0d,
+                                                     V4<T> *__restrict__ xd, V4<T> *__restrict__ vd) {
+  const V4<T> p0 = x0d[d];
+  // Quaternion rotation v + w (2 u x v) + u x (2 u x v)
+  const double u[3] = {B.q[1], B.q[2], B.q[3]}, pv[3] = {(double)p0.x, (double)p0.y, (double)p0.z};
+  double uv[3], uuv[3];
+  cross3(u, pv, uv);
+  for (int k = 0; k < 3; k++) uv[k] += uv[k];
+  cross3(u, uv, uuv);
+  double pw[3];
+  for (int k = 0; k < 3; k++) pw[k] = pv[k] + B.q[0] * uv[k] + uuv[k] + B.x[k];
+  const T xs[3] = {(T)pw[0], (T)pw[1], (T)pw[2]};
+  xd[d] = V4<T>{xs[0], xs[1], xs[2], xd[d].w};
+  double rr[3] = {(double)xs[0] - B.x[0], (double)xs[1] - B.x[1], (double)xs[2] - B.x[2]}, vv[3];
+  cross3(B.w, rr, vv);
+  vd[d] = (B.dyn || B.anim) ? V4<T>{(T)(vv[0] + B.v[0]), (T)(vv[1] + B.v[1]), (T)(vv[2] + B.v[2]), T(0)}
+                            : V4<T>{T(0), T(0), T(0), T(0)};
+}
 // Rigid contact of one sample of a dynamic body (kernels_contact.cuh writes these).
 constexpr int CONTACT_BLK = 2 * NJAC;  // per force-carrying sample: own-body blocks, other-body blocks
 struct ContactRec {
@@ -574,8 +579,16 @@ static __device__ __forceinline__ int block_exclusive_scan(int v, int *warp_tot,
 // updateBoundaryForces once per boundary model (RigidBody3dBoundarySimulator.cpp:284-298,
 // RigidContactSolver.cpp:347-362); every addForce / addTorque moves the velocities at once and
 // every gyroscopic addTorque adds (I w) x w (Dynamic3dRigidBody.h:113-142).
+// The body's fluid force, torque and net Jacobians come first: the sums of its chunk
+// partials in chunk order (the second stage of the body reduction); the body's samples are
+// moved last (SimulatorBase::updateBoundaryParticles).
+template <class T>
 static __global__ void __launch_bounds__(128) k_rigid_step(BodyState *__restrict__ bs, int nbodies, RigidConsts rc,
-                                                    double *__restrict__ tape_step, ContactStep cs) {
+                                                    double *__restrict__ tape_step, ContactStep cs,
+                                                    const int2 *__restrict__ body_chunks,
+                                                    const double *__restrict__ red_part,
+                                                    const V4<T> *__restrict__ x0d, V4<T> *__restrict__ xd,
+                                                    V4<T> *__restrict__ vd) {
   __shared__ ChainCoef C;
   __shared__ double A[NSTATE * NSTATE];
   __shared__ double Gold[NSTATE * 6];
@@ -593,6 +606,15 @@ static __global__ void __launch_bounds__(128) k_rigid_step(BodyState *__restrict
   }
   __syncthreads();
   BodyState &B = sB;
+  if (B.dyn && t < RED_VALUES) {
+    const int2 r = body_chunks[b];
+    double tot = 0.0;
+    for (int c = r.x; c < r.y; c++) tot += red_part[(size_t)c * RED_VALUES + t];
+    if (t < 3) B.F[t] = tot;
+    else if (t < 3 + NJAC) B.nets[t - 3] = tot;
+    else B.T[t - 3 - NJAC] = tot;
+  }
+  __syncthreads();
   const bool chain = B.dyn && !B.anim && rc.enable_gradient && !rc.manager;
   if (t == 0) B.chain_ran = chain ? 1 : 0;
   if (chain) {
@@ -763,6 +785,8 @@ static __global__ void __launch_bounds__(128) k_rigid_step(BodyState *__restrict
     }
   }
   __syncthreads();
+  if (B.dyn || B.anim)
+    for (int d = B.dstart + t; d < B.dstart + B.dcount; d += blockDim.x) sample_update(B, d, x0d, xd, vd);
   {
     const unsigned long long *src = reinterpret_cast<const unsigned long long *>(&sB);
     unsigned long long *dst = reinterpret_cast<unsigned long long *>(bs + b);
@@ -790,8 +814,6 @@ static __global__ void k_rigid_begin(BodyState *__restrict__ bs, BeginCmd cmd) {
   }
 }
 
-// SimulatorBase::updateBoundaryParticles (SimulatorBase.cpp:1827-1857) for dynamic
-// samples: x_j = R(q) x0_j + x_b, v_j = omega x (x_j - x_b) + v_b, in FP64 then stored in T.
 template <class T>
 static __global__ void k_boundary_update(const BodyState *__restrict__ bs, int nd, const V4<T> *__restrict__ x0d,
                                   const int *__restrict__ bodyd, V4<T> *__restrict__ xd, V4<T> *__restrict__ vd,
@@ -800,21 +822,7 @@ static __global__ void k_boundary_update(const BodyState *__restrict__ bs, int n
   if (d >= nd) return;
   const BodyState &B = bs[bodyd[d]];
   if (only_moving && !(B.dyn || B.anim)) return;
-  const V4<T> p0 = x0d[d];
-  // Quaternion rotation v + w (2 u x v) + u x (2 u x v)
-  const double u[3] = {B.q[1], B.q[2], B.q[3]}, pv[3] = {(double)p0.x, (double)p0.y, (double)p0.z};
-  double uv[3], uuv[3];
-  cross3(u, pv, uv);
-  for (int k = 0; k < 3; k++) uv[k] += uv[k];
-  cross3(u, uv, uuv);
-  double pw[3];
-  for (int k = 0; k < 3; k++) pw[k] = pv[k] + B.q[0] * uv[k] + uuv[k] + B.x[k];
-  const T xs[3] = {(T)pw[0], (T)pw[1], (T)pw[2]};
-  xd[d] = V4<T>{xs[0], xs[1], xs[2], xd[d].w};
-  double rr[3] = {(double)xs[0] - B.x[0], (double)xs[1] - B.x[1], (double)xs[2] - B.x[2]}, vv[3];
-  cross3(B.w, rr, vv);
-  vd[d] = (B.dyn || B.anim) ? V4<T>{(T)(vv[0] + B.v[0]), (T)(vv[1] + B.v[1]), (T)(vv[2] + B.v[2]), T(0)}
-                            : V4<T>{T(0), T(0), T(0), T(0)};
+  sample_update(B, d, x0d, xd, vd);
 }
 
 // Reverse sweep: lambda <- A_n^T lambda for n = last..first, one block per body.
