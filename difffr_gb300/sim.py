@@ -119,9 +119,16 @@ class DiffDFSPH:
 
     # -------------------------------------------------------------- rigid bodies
     def rigid_state(self, b):
-        x, q, v, w = (np.zeros(k) for k in (3, 4, 3, 3))
-        check(self.lib, self.lib.dfsph_get_rigid_state(self.h, int(b), dptr(x), dptr(q), dptr(v), dptr(w)))
-        return x, q, v, w
+        """(x, q (w, x, y, z), v, omega) of body b as new arrays."""
+        if getattr(self, "_rs_ptrs", None) is None:
+            # one output buffer and its four pointers, made once (the per-call ctypes
+            # conversions otherwise dominate this call on slow hosts)
+            self._rs_buf = np.zeros(13)
+            base = self._rs_buf.ctypes.data
+            self._rs_ptrs = tuple(ctypes.cast(base + 8 * o, POINTER(c_double)) for o in (0, 3, 7, 10))
+        check(self.lib, self.lib.dfsph_get_rigid_state(self.h, int(b), *self._rs_ptrs))
+        r = self._rs_buf.copy()
+        return r[0:3], r[3:7], r[7:10], r[10:13]
 
     def rigid_force(self, b):
         F, T = np.zeros(3), np.zeros(3)
