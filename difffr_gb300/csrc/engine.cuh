@@ -293,6 +293,7 @@ class Engine : public EngineBase {
   }
   // rigid-rigid contact (penalty form) and the gradient manager's multi-body chain
   bool contact_ = false, manager_ = false;
+  bool psi_static_done_ = false;  // static samples' psi computed (once)
   ContactConsts cc_;
   DBuf<int> bodyS_;            // body of each static sample (sorted order)
   DBuf<V4<T>> x0S_;            // local coordinates of each static sample (sorted order)

@@ -461,13 +461,21 @@ void Engine<T>::sort_dynamic() {
   pend(DFSPH_K_SORT, nd_);
 }
 
+// The static samples' psi is computed once: they never move, and every reset puts the
+// dynamic samples back at the same initial poses, so their neighbourhoods repeat exactly;
+// later resets recompute the dynamic samples only.
 template <class T>
 void Engine<T>::compute_psi() {
   if (ns_ + nd_ == 0) return;
-  k_boundary_psi<T><<<blocks(ns_ + nd_), 256, 0, stream_>>>(fc_, ns_, nd_, BR_.p, cstartS_.p,
-                                                            nd_ ? cstartD_.p : nullptr, psi_.p);
-  k_set_psi<T><<<blocks(ns_ + nd_), 256, 0, stream_>>>(ns_, nd_, psi_.p, BR_.p, xd_.p, dynSortedToBody_.p);
-  launched(2);
+  const int p0 = psi_static_done_ ? ns_ : 0;
+  const int cnt = ns_ + nd_ - p0;
+  if (cnt > 0) {
+    k_boundary_psi<T><<<blocks(cnt), 256, 0, stream_>>>(fc_, ns_, nd_, BR_.p, cstartS_.p, nd_ ? cstartD_.p : nullptr,
+                                                      psi_.p, p0);
+    k_set_psi<T><<<blocks(cnt), 256, 0, stream_>>>(ns_, nd_, psi_.p, BR_.p, xd_.p, dynSortedToBody_.p, p0);
+    launched(2);
+  }
+  psi_static_done_ = true;
   check_launch();
 }
 

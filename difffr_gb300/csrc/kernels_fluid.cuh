@@ -314,8 +314,8 @@ static __global__ void k_bf_lists(FluidConsts<T> c, int nd, const V4<T> *__restr
 template <class T>
 static __global__ void k_boundary_psi(FluidConsts<T> c, int ns, int nd, const Rec<T> *__restrict__ BR,
                                const int *__restrict__ cstartS, const int *__restrict__ cstartD,
-                               T *__restrict__ psi_out) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+                               T *__restrict__ psi_out, int p0) {
+  const int p = p0 + blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= ns + nd) return;
   const V4<T> xp = BR[p].x;
   int cx, cy, cz;
@@ -337,8 +337,8 @@ static __global__ void k_boundary_psi(FluidConsts<T> c, int ns, int nd, const Re
 
 template <class T>
 static __global__ void k_set_psi(int ns, int nd, const T *__restrict__ psi, Rec<T> *__restrict__ BR,
-                                 V4<T> *__restrict__ xd, const int *__restrict__ dyn_sorted_to_body) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+                                 V4<T> *__restrict__ xd, const int *__restrict__ dyn_sorted_to_body, int p0) {
+  const int p = p0 + blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= ns + nd) return;
   BR[p].x.w = psi[p];
   if (p >= ns) xd[dyn_sorted_to_body[p - ns]].w = psi[p];

@@ -542,6 +542,43 @@ static __device__ __forceinline__ void sample_update(const BodyState &B, int d, 
   vd[d] = (B.dyn || B.anim) ? V4<T>{(T)(vv[0] + B.v[0]), (T)(vv[1] + B.v[1]), (T)(vv[2] + B.v[2]), T(0)}
                             : V4<T>{T(0), T(0), T(0), T(0)};
 }
+// Dynamic3dRigidBody::addForce / addTorque (Dynamic3dRigidBody.h:113-142) on a state
+// (v, w) with the world inertia I and its inverse.
+static __device__ __forceinline__ void body_add_force(double *v, double invMass, const double *f, double dt) {
+  for (int k = 0; k < 3; k++) v[k] += invMass * f[k] * dt;
+}
+static __device__ __forceinline__ void body_add_torque(double *w, const double *I, const double *Iinv,
+                                                       const double *tq, bool gyro, double dt) {
+  double d[3], L[3], cr[3];
+  if (gyro) {
+    mv3(I, w, L);
+    cross3(L, w, cr);
+    for (int k = 0; k < 3; k++) cr[k] += tq[k];
+  } else for (int k = 0; k < 3; k++) cr[k] = tq[k];
+  mv3(Iinv, cr, d);
+  for (int k = 0; k < 3; k++) w[k] += d[k] * dt;
+}
+// Dynamic3dRigidBody::animate + updateInertia (Dynamic3dRigidBody.h:143-154, 215-219)
+static __device__ __forceinline__ void body_animate(double *x, double *q, double *I, double *Iinv, const double *v,
+                                                    const double *w, const double *I0, double dt) {
+  for (int k = 0; k < 3; k++) x[k] += v[k] * dt;
+  const double wq[4] = {0.0, w[0], w[1], w[2]};
+  double dq[4];
+  q_mul(wq, q, dq);
+  for (int k = 0; k < 4; k++) q[k] += dt * 0.5 * dq[k];
+  const double nn = sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+  for (int k = 0; k < 4; k++) q[k] /= nn;
+  double R[9], RI[9], RT[9];
+  q_to_R(q, R);
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) { RT[3 * i + j] = R[3 * j + i]; }
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) RI[3 * i + j] = R[3 * i] * I0[j] + R[3 * i + 1] * I0[3 + j] + R[3 * i + 2] * I0[6 + j];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) I[3 * i + j] = RI[3 * i] * RT[j] + RI[3 * i + 1] * RT[3 + j] + RI[3 * i + 2] * RT[6 + j];
+  inv3<double>(I, Iinv);
+}
+
 // Rigid contact of one sample of a dynamic body (kernels_contact.cuh writes these).
 constexpr int CONTACT_BLK = 2 * NJAC;  // per force-carrying sample: own-body blocks, other-body blocks
 struct ContactRec {
@@ -615,6 +652,24 @@ static __global__ void __launch_bounds__(128) k_rigid_step(BodyState *__restrict
     else B.T[t - 3 - NJAC] = tot;
   }
   __syncthreads();
+  // Without the contact solver the velocity and position step does not depend on the chain
+  // rule (which reads the state before it): one thread of the second warp computes it into
+  // sN while the first warp runs the chain; thread 0 takes it over after the chain.
+  __shared__ double sN[31];  // v w x q I Iinv
+  const bool early = cs.rec == nullptr && B.dyn && blockDim.x > 32;
+  if (early && t == 32) {
+    double *v = sN, *w = sN + 3, *x = sN + 6, *q = sN + 9, *I = sN + 13, *Iinv = sN + 22;
+    for (int k = 0; k < 3; k++) { v[k] = B.v[k]; w[k] = B.w[k]; x[k] = B.x[k]; }
+    for (int k = 0; k < 4; k++) q[k] = B.q[k];
+    for (int k = 0; k < 9; k++) { I[k] = B.I[k]; Iinv[k] = B.Iinv[k]; }
+    if (!B.anim) {
+      const double gm[3] = {rc.gx * B.mass, rc.gy * B.mass, rc.gz * B.mass};
+      body_add_force(v, B.invMass, B.F, rc.dt);
+      body_add_torque(w, I, Iinv, B.T, rc.gyroscopic, rc.dt);
+      body_add_force(v, B.invMass, gm, rc.dt);
+    }
+    body_animate(x, q, I, Iinv, v, w, B.I0, rc.dt);
+  }
   const bool chain = B.dyn && !B.anim && rc.enable_gradient && !rc.manager;
   if (t == 0) B.chain_ran = chain ? 1 : 0;
   if (chain) {
@@ -700,17 +755,8 @@ static __global__ void __launch_bounds__(128) k_rigid_step(BodyState *__restrict
   }
   if (t == 0 && cs.counts) { cs.counts[2 * b] = s_con; cs.counts[2 * b + 1] = s_act; }
   const double dt = rc.dt;
-  auto add_force = [&](const double *f) { for (int k = 0; k < 3; k++) B.v[k] += B.invMass * f[k] * dt; };
-  auto add_torque = [&](const double *tq) {
-    double d[3], L[3], cr[3];
-    if (rc.gyroscopic) {
-      mv3(B.I, B.w, L);
-      cross3(L, B.w, cr);
-      for (int k = 0; k < 3; k++) cr[k] += tq[k];
-    } else for (int k = 0; k < 3; k++) cr[k] = tq[k];
-    mv3(B.Iinv, cr, d);
-    for (int k = 0; k < 3; k++) B.w[k] += d[k] * dt;
-  };
+  auto add_force = [&](const double *f) { body_add_force(B.v, B.invMass, f, dt); };
+  auto add_torque = [&](const double *tq) { body_add_torque(B.w, B.I, B.Iinv, tq, rc.gyroscopic, dt); };
   if (t == 0 && B.dyn) {
     for (int k = 0; k < 3; k++) { B.wpre[k] = B.w[k]; }
     for (int k = 0; k < 4; k++) B.qpre[k] = B.q[k];
@@ -738,36 +784,27 @@ static __global__ void __launch_bounds__(128) k_rigid_step(BodyState *__restrict
     }
   }
   if (t == 0 && B.dyn) {
-    if (cs.rec) {
-      const double zero[3] = {0.0, 0.0, 0.0};
-      if (!B.anim)
-        for (int rep = 0; rep < rc.nbodies; rep++) {
-          add_force(rep == 0 ? B.F : zero);
-          add_torque(rep == 0 ? B.T : zero);
-        }
-    } else if (!B.anim) {
-      const double gm[3] = {rc.gx * B.mass, rc.gy * B.mass, rc.gz * B.mass};
-      add_force(B.F);
-      add_torque(B.T);
-      add_force(gm);
+    if (early) {
+      for (int k = 0; k < 3; k++) { B.v[k] = sN[k]; B.w[k] = sN[3 + k]; B.x[k] = sN[6 + k]; B.wmid[k] = sN[3 + k]; }
+      for (int k = 0; k < 4; k++) B.q[k] = sN[9 + k];
+      for (int k = 0; k < 9; k++) { B.I[k] = sN[13 + k]; B.Iinv[k] = sN[22 + k]; }
+    } else {
+      if (cs.rec) {
+        const double zero[3] = {0.0, 0.0, 0.0};
+        if (!B.anim)
+          for (int rep = 0; rep < rc.nbodies; rep++) {
+            add_force(rep == 0 ? B.F : zero);
+            add_torque(rep == 0 ? B.T : zero);
+          }
+      } else if (!B.anim) {
+        const double gm[3] = {rc.gx * B.mass, rc.gy * B.mass, rc.gz * B.mass};
+        add_force(B.F);
+        add_torque(B.T);
+        add_force(gm);
+      }
+      for (int k = 0; k < 3; k++) B.wmid[k] = B.w[k];
+      body_animate(B.x, B.q, B.I, B.Iinv, B.v, B.w, B.I0, dt);
     }
-    for (int k = 0; k < 3; k++) B.wmid[k] = B.w[k];
-    for (int k = 0; k < 3; k++) B.x[k] += B.v[k] * dt;
-    const double wq[4] = {0.0, B.w[0], B.w[1], B.w[2]};
-    double dq[4];
-    q_mul(wq, B.q, dq);
-    for (int k = 0; k < 4; k++) B.q[k] += dt * 0.5 * dq[k];
-    const double nn = sqrt(B.q[0] * B.q[0] + B.q[1] * B.q[1] + B.q[2] * B.q[2] + B.q[3] * B.q[3]);
-    for (int k = 0; k < 4; k++) B.q[k] /= nn;
-    double R[9], RI[9], RT[9];
-    q_to_R(B.q, R);
-    for (int i = 0; i < 3; i++)
-      for (int j = 0; j < 3; j++) { RT[3 * i + j] = R[3 * j + i]; }
-    for (int i = 0; i < 3; i++)
-      for (int j = 0; j < 3; j++) RI[3 * i + j] = R[3 * i] * B.I0[j] + R[3 * i + 1] * B.I0[3 + j] + R[3 * i + 2] * B.I0[6 + j];
-    for (int i = 0; i < 3; i++)
-      for (int j = 0; j < 3; j++) B.I[3 * i + j] = RI[3 * i] * RT[j] + RI[3 * i + 1] * RT[3 + j] + RI[3 * i + 2] * RT[6 + j];
-    inv3<double>(B.I, B.Iinv);
   }
   // the contact solver's Jacobian blocks of this body, summed in sample order
   if (cs.Mc) {
