@@ -51,5 +51,10 @@ def test_null_arguments_are_rejected_without_device_work():
     lib = _abi.load_library()
     assert lib.dfsph_default_params(None) == _abi.DFSPH_ERR_INVALID_ARG
     assert lib.dfsph_step(None, 1, None) == _abi.DFSPH_ERR_INVALID_ARG
+    out = (ctypes.c_double * 78)()
+    assert lib.dfsph_get_manager_grad(None, 0, 0, out) == _abi.DFSPH_ERR_INVALID_ARG
+    assert lib.dfsph_get_manager_jacobians(None, 0, 0, out) == _abi.DFSPH_ERR_INVALID_ARG
+    nc, na = ctypes.c_int64(), ctypes.c_int64()
+    assert lib.dfsph_get_contact_count(None, ctypes.byref(nc), ctypes.byref(na)) == _abi.DFSPH_ERR_INVALID_ARG
     assert b"NULL" in lib.dfsph_last_error()
     assert lib.dfsph_destroy(None) == 0

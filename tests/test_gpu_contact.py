@@ -164,3 +164,23 @@ def test_many_contact_samples_without_fluid_matches_oracle():
             np.testing.assert_allclose(a, c, rtol=1e-8, atol=1e-10)
     assert g.contact_count()[1] > 256
     assert _rel(g.manager_grad(1, 1), o.manager_grad(1, 1)) < 1e-6
+
+
+def test_manager_and_contact_api_errors():
+    """The manager getters answer DFSPH_ERR_UNSUPPORTED when the manager is off and
+    DFSPH_ERR_INVALID_ARG for a body index out of range or a NULL output; without the
+    contact solver the contact counts are zero."""
+    import ctypes
+    from difffr_gb300 import _abi
+    plain = DiffDFSPH(scn.small_contact_scene())
+    plain.step(1)
+    out = (ctypes.c_double * 78)()
+    assert plain.lib.dfsph_get_manager_grad(plain.h, 1, 1, out) == _abi.DFSPH_ERR_UNSUPPORTED
+    assert plain.lib.dfsph_get_manager_jacobians(plain.h, 1, 1, out) == _abi.DFSPH_ERR_UNSUPPORTED
+    assert plain.contact_count() == (0, 0)
+    g = DiffDFSPH(scn.two_sphere_contact())
+    g.step(1)
+    assert g.lib.dfsph_get_manager_grad(g.h, 3, 1, out) == _abi.DFSPH_ERR_INVALID_ARG
+    assert g.lib.dfsph_get_manager_grad(g.h, 1, -1, out) == _abi.DFSPH_ERR_INVALID_ARG
+    assert g.lib.dfsph_get_manager_jacobians(g.h, 1, 1, None) == _abi.DFSPH_ERR_INVALID_ARG
+    assert g.lib.dfsph_get_contact_count(g.h, None, None) == _abi.DFSPH_ERR_INVALID_ARG
