@@ -38,3 +38,26 @@ def test_two_rank_replica_timing_takes_the_max():
     assert [r[0] for r in res] == [0, 1]
     assert all(r[1] == 2 for r in res)
     assert all(r[3] == 11.0 for r in res)
+
+
+def test_reference_arm_json_line():
+    """`bench.py --impl reference` (the oracle port on the host cores) prints one JSON line
+    with the contract's keys, the same metric and unit as the GPU arm, zero transfer bytes
+    and a cpu_baseline describing the run."""
+    import json
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference", "--config", "0",
+                        "--steps", "1", "--warmup", "1"], capture_output=True, text=True, timeout=600, cwd=root)
+    assert r.returncode == 0, r.stderr[-2000:]
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    for k in ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+              "scaling", "vs_baseline", "dtype", "data", "config", "e2e", "cpu_baseline"):
+        assert k in d, k
+    assert d["impl"] == "reference" and d["value"] > 0 and d["warmup"] >= 3
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
+    import bench
+    assert d["metric"] == bench.METRIC and d["unit"] == bench.UNIT
