@@ -454,6 +454,14 @@ template <class T>
 void Engine<T>::sort_dynamic() {
   if (nd_ == 0) return;
   pbegin();
+  if (nd_ <= SMALL_SORT_MAX) {
+    k_sort_dynamic_small<T><<<1, 1024, 0, stream_>>>(nd_, ns_, fc_.grid, xd_.p, vd_.p, BR_.p, dynSortedToBody_.p,
+                                                     keyD_.p, err_.p);
+    k_cstart_from_keys<<<blocks(ncell_ + 1), 256, 0, stream_>>>(ncell_, nd_, keyD_.p, cstartD_.p);
+    launched(2);
+    pend(DFSPH_K_SORT, nd_);
+    return;
+  }
   sort_points(xd_.p, 1, nd_, keyD_.p, rankD_.p, cstartD_.p, orderD_.p);
   k_gather_dynamic<T><<<blocks(nd_), 256, 0, stream_>>>(nd_, ns_, orderD_.p, xd_.p, vd_.p, BR_.p,
                                                         dynSortedToBody_.p);

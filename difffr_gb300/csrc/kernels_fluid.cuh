@@ -133,6 +133,62 @@ static __global__ void k_gather_fluid(int n, const int *__restrict__ order, cons
   perm2[i] = perm[o];
 }
 
+// Dynamic samples, few of them: one block sorts (cell key, body-order index) pairs with a
+// bitonic network in shared memory (the order the counting sort plus per-cell insertion
+// sort gives: by cell, then by index), writes the sorted records behind the static ones and
+// the sorted keys; k_cstart_from_keys then fills the cell-start table by binary search.
+constexpr int SMALL_SORT_MAX = 4096;
+template <class T>
+static __global__ void __launch_bounds__(1024) k_sort_dynamic_small(int nd, int ns, Grid<T> g,
+                                                                    const V4<T> *__restrict__ xd,
+                                                                    const V4<T> *__restrict__ vd, Rec<T> *__restrict__ BR,
+                                                                    int *__restrict__ dyn_sorted_to_body,
+                                                                    int *__restrict__ skeys, int *__restrict__ err) {
+  __shared__ unsigned long long kv[SMALL_SORT_MAX];
+  int m = 1;
+  while (m < nd) m <<= 1;
+  for (int j = threadIdx.x; j < m; j += blockDim.x) {
+    unsigned long long v = ~0ull;
+    if (j < nd) {
+      const V4<T> p = xd[j];
+      if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) atomicOr(err, ERR_NONFINITE_POSITION);
+      int cx, cy, cz;
+      grid_cell(g, p.x, p.y, p.z, cx, cy, cz);
+      v = ((unsigned long long)(unsigned)grid_key(g, cx, cy, cz) << 32) | (unsigned)j;
+    }
+    kv[j] = v;
+  }
+  __syncthreads();
+  for (int k = 2; k <= m; k <<= 1)
+    for (int jj = k >> 1; jj > 0; jj >>= 1) {
+      for (int a = threadIdx.x; a < m; a += blockDim.x) {
+        const int b = a ^ jj;
+        if (b > a) {
+          const unsigned long long x = kv[a], y = kv[b];
+          const bool up = (a & k) == 0;
+          if ((x > y) == up) { kv[a] = y; kv[b] = x; }
+        }
+      }
+      __syncthreads();
+    }
+  for (int j = threadIdx.x; j < nd; j += blockDim.x) {
+    const int o = (int)(kv[j] & 0xffffffffu);
+    BR[ns + j] = Rec<T>{xd[o], vd[o]};
+    dyn_sorted_to_body[j] = o;
+    skeys[j] = (int)(kv[j] >> 32);
+  }
+}
+static __global__ void k_cstart_from_keys(int ncell, int nd, const int *__restrict__ skeys, int *__restrict__ cstart) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c > ncell) return;
+  int lo = 0, hi = nd;  // first sorted key >= c
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (skeys[mid] < c) lo = mid + 1; else hi = mid;
+  }
+  cstart[c] = lo;
+}
+
 // dynamic boundary: body order -> cell order copy behind the static samples
 template <class T>
 static __global__ void k_gather_dynamic(int nd, int ns, const int *__restrict__ order, const V4<T> *__restrict__ xd,
