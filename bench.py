@@ -347,6 +347,14 @@ def run_ours(args):
         sim = None
         ws = warm_start_ab(args)
 
+    # ---- the rigid contact solver and the gradient manager at the same size
+    contact = None
+    if rank == 0 and args.config == 1 and args.contact_steps > 0:
+        if sim is not None:
+            sim.close()
+            sim = None
+        contact = contact_leg(args)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -377,11 +385,40 @@ def run_ours(args):
             "clocks": clk,
             "cpu_baseline": cpu,
             "warm_start": ws,
+            "contact": contact,
         }
         print(json.dumps(line), flush=True)
     if sim is not None:
         sim.close()
     return 0
+
+
+def contact_leg(args):
+    """Forward + adjoint steps/s of the 1M dam break with two spheres in contact (the rigid
+    contact solver and the gradient manager on), and the rigid-stream time that includes the
+    contact samples, the sequential impulses and the manager's chain."""
+    import numpy as np
+    from difffr_gb300 import scene as scn
+    from difffr_gb300.sim import DiffDFSPH
+    sc = scn.dam_break_two_spheres()
+    s = DiffDFSPH(sc)
+    for _ in range(max(args.warmup, 3)):
+        s.step(1)
+    s.profile_enable(True)
+    k = args.contact_steps
+    s.record_event(0)
+    s.step(k)
+    s.record_event(1)
+    ms = s.event_elapsed_ms(0, 1)
+    prof = s.profile()
+    nc, na = s.contact_count()
+    g = s.manager_grad(2, 1)
+    s.close()
+    return {"workload": f"{sc.name} (two R 0.05 spheres 0.01 m apart, 0.5 m/s towards each other)",
+            "value": k / (ms / 1000.0), "unit": UNIT, "ms_per_step": ms / k,
+            "rigid_stream_ms_per_step": prof["rigid"]["ms"] / k,
+            "contact_samples_last_step": nc, "force_samples_last_step": na,
+            "cross_gradient_finite": bool(np.all(np.isfinite(g))), "steps": k}
 
 
 def warm_start_ab(args):
@@ -419,6 +456,7 @@ def main():
     ap.add_argument("--ws-start", type=int, default=300)
     ap.add_argument("--ws-steps", type=int, default=200)
     ap.add_argument("--train-warm-start", action="store_true")
+    ap.add_argument("--contact-steps", type=int, default=20)
     args = ap.parse_args()
     args.config_name = {0: "tank_sphere_8k (20^3 lattice, r 0.025)",
                         1: "dam_break_sphere_1M (100^3 lattice, r 0.005, 2.4x1.2x1.2 box, R 0.05 sphere)",

@@ -302,6 +302,7 @@ class Engine : public EngineBase {
   DBuf<double> cblk_;
   DBuf<int> clist_, ccount_;
   DBuf<double> Mc_, mgrM_, mgrS_;  // contact blocks of the step, manager blocks, manager chain state
+  DBuf<MgrCoef> mgrC_;              // the manager's per-body coefficients of the step
   void contact_init();
   void manager_reset(bool blocks);
 

@@ -356,6 +356,7 @@ Engine<T>::Engine(const dfsph_scene *sc) {
     Mc_.alloc(nbb * nbb * NJAC);
     mgrM_.alloc(nbb * nbb * NJAC);
     mgrS_.alloc((size_t)NSTATE * nbb * 6 * nbb);
+    mgrC_.alloc(nbb);
   }
   if (nd_ > 0 && P_.enable_gradient) {
     tape_cap_ = 256;
@@ -788,7 +789,7 @@ void Engine<T>::rigid_end() {
     cc_.grad = manager_ ? 1 : 0;
     // samples of the dynamic bodies against every boundary sample; the dynamic cell table
     // is this step's (the samples have not moved since sort_dynamic)
-    k_contact_samples<T><<<blocks(nd_, 128), 128, 0, stream2_>>>(
+    k_contact_samples<T><<<blocks(nd_ * CONTACT_LANES, 128), 128, 0, stream2_>>>(
         cc_, fc_.grid, fc_.h2, ns_, nd_, bs_.p, BR_.p, cstartS_.p, cstartD_.p, bodyS_.p, x0S_.p, bodyd_.p,
         dynSortedToBody_.p, xd_.p, x0d_.p, cvol0S_.p, cvol0D_.p, cdens0D_.p, crec_.p, cc_.grad ? cblk_.p : nullptr);
     nl++;
@@ -801,8 +802,16 @@ void Engine<T>::rigid_end() {
   nl++;
   if (mgr_chain || mgr_blocks) {
     MgrConsts mc{rc_.dt, nb_, rc_.gyroscopic, n_ > 0 ? 1 : 0, contact_ ? 1 : 0, 1, mgr_chain ? 1 : 0};
-    k_manager_chain<<<1, 256, 0, stream2_>>>(bs_.p, mc, mgrM_.p, Mc_.p, mgrS_.p, mgr_chain ? tape_step : nullptr);
-    nl++;
+    if (mgr_chain) {
+      const int ncol = 6 * nb_ + (tape_step ? 2 * NSTATE * nb_ : 0);
+      k_manager_coef<<<1, 64, 0, stream2_>>>(bs_.p, mc, mgrM_.p, mgrC_.p);
+      k_manager_columns<<<ncol, 32, 0, stream2_>>>(mc, mgrC_.p, mgrM_.p, Mc_.p, mgrS_.p, tape_step);
+      nl += 2;
+    }
+    if (mgr_blocks) {
+      k_manager_blocks<<<blocks(nb_ * nb_ * NJAC), 256, 0, stream2_>>>(bs_.p, nb_, mgrM_.p, Mc_.p);
+      nl++;
+    }
   }
   launched(nl);
   pend(DFSPH_K_RIGID, nd_, stream2_);

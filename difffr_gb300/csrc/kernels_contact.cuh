@@ -6,8 +6,9 @@
 //    per sample of a dynamic body with a neighbour of another body its contact density,
 //    penalty normal force, Coulomb friction and the Jacobian blocks of that force
 //    (beforePenaltyInitialize :307-345, solveRigidContactPenalty :419-555).
-//  - k_manager_chain: RigidBodyGradientManager's forward chain over body pairs [R][RR]
-//    (RigidBodyGradientManager.cpp:96-468) and its step maps for the reverse sweep.
+//  - k_manager_coef / k_manager_columns / k_manager_blocks: RigidBodyGradientManager's
+//    forward chain over body pairs [R][RR] (RigidBodyGradientManager.cpp:96-468), its step
+//    maps for the reverse sweep, and the blocks carried into the next step.
 #pragma once
 #include "kernels_fluid.cuh"
 #include "kernels_rigid.cuh"
@@ -81,9 +82,13 @@ static __global__ void k_contact_rest(ContactConsts c, Grid<T> g, T h2, int ns, 
   }
 }
 
-// One thread per sample of a dynamic body (body order): its contact record and, when
-// gradients are on, the Jacobian blocks of its force (own body [R][R] and the other body
-// [R][RR], in the dfsph_get_net_jacobians layout: Fv Fx Fw Fq Tw Tv Tx Tq).
+// CONTACT_LANES lanes per sample of a dynamic body (body order): they split the candidate
+// rows and combine their sums with shuffles, then split the Jacobian blocks of the sample's
+// force between them; the result is the sample's contact record and, when gradients are on,
+// the blocks for its own body [R][R] and the other body [R][RR], in the
+// dfsph_get_net_jacobians layout (Fv Fx Fw Fq Tw Tv Tx Tq). FP64 runs at a low rate on this
+// part, so the work is spread over many SMs rather than one thread per sample.
+constexpr int CONTACT_LANES = 8;
 template <class T>
 static __global__ void __launch_bounds__(128) k_contact_samples(
     ContactConsts c, Grid<T> g, T h2, int ns, int nd, const BodyState *__restrict__ bs, const Rec<T> *__restrict__ BR,
@@ -92,67 +97,85 @@ static __global__ void __launch_bounds__(128) k_contact_samples(
     const V4<T> *__restrict__ xd, const V4<T> *__restrict__ x0d, const double *__restrict__ vol0S,
     const double *__restrict__ vol0D, const double *__restrict__ dens0D, ContactRec *__restrict__ rec,
     double *__restrict__ blk) {
-  const int d = blockIdx.x * blockDim.x + threadIdx.x;
-  if (d >= nd) return;
-  const int b = bodyd[d];
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int d = gt / CONTACT_LANES, sub = gt % CONTACT_LANES;
+  const bool live = d < nd;
+  const int dd = live ? d : 0;
+  const int b = bodyd[dd];
   const BodyState &B = bs[b];
+  const V4<T> xT = xd[dd];
+  const double xr[3] = {(double)xT.x, (double)xT.y, (double)xT.z};
+  double dens = 0.0;
+  double sum_x[3] = {0, 0, 0}, sum_vk[3] = {0, 0, 0}, avg_rk[3] = {0, 0, 0}, gdx[3] = {0, 0, 0};
+  double gdqk[4] = {0, 0, 0, 0};
+  double sum_w = 0.0;
+  int has = 0, RR = -1;
+  if (live && B.dyn) {
+    int cx, cy, cz;
+    grid_cell(g, xT.x, xT.y, xT.z, cx, cy, cz);
+    auto visit = [&](int jb, int je, int off) {
+      for (int j = jb + sub; j < je; j += CONTACT_LANES) {
+        int o = -1, bk;
+        if (off == 0) bk = bodyS[j];
+        else { o = dynSortedToBody[j]; if (o == dd) continue; bk = bodyd[o]; }
+        const V4<T> xkT = BR[off + j].x;
+        if (!(dist2_rn(xT.x - xkT.x, xT.y - xkT.y, xT.z - xkT.z) < h2)) continue;
+        const double xk[3] = {(double)xkT.x, (double)xkT.y, (double)xkT.z};
+        const double rv[3] = {xr[0] - xk[0], xr[1] - xk[1], xr[2] - xk[2]};
+        const double rl = sqrt(dist2_rn(rv[0], rv[1], rv[2]));
+        const double w = cubic_W(rl, c.kc);
+        const double vol = off == 0 ? vol0S[j] : vol0D[o];
+        dens += vol * w;
+        if (bk == b) {
+          for (int k = 0; k < 3; k++) sum_x[k] += xk[k] * w;
+          sum_w += w;
+        } else {
+          has = 1;
+          RR = bk > RR ? bk : RR;
+          const BodyState &C = bs[bk];
+          double vk[3];
+          sample_velocity(C, c, xk, vk);
+          for (int k = 0; k < 3; k++) { sum_vk[k] += vk[k] * w; avg_rk[k] += (xk[k] - C.x[k]) * w; }
+          const V3<double> gw = cubic_gradW(V3<double>{rv[0], rv[1], rv[2]}, rl, c.kh);
+          const double gv[3] = {vol * gw.x, vol * gw.y, vol * gw.z};
+          for (int k = 0; k < 3; k++) gdx[k] += gv[k];
+          if (c.grad) {
+            const V4<T> p0 = off == 0 ? x0S[j] : x0d[o];
+            double Gk[12];
+            grad_Rqp<double>(C.q[0], C.q[1], C.q[2], C.q[3], V3<double>{(double)p0.x, (double)p0.y, (double)p0.z}, Gk);
+            for (int q = 0; q < 4; q++) gdqk[q] -= gv[0] * Gk[q] + gv[1] * Gk[4 + q] + gv[2] * Gk[8 + q];
+          }
+        }
+      }
+    };
+    if (ns > 0) for_each_row(g, cstartS, cx, cy, cz, [&](int jb, int je) { visit(jb, je, 0); });
+    for_each_row(g, cstartD, cx, cy, cz, [&](int jb, int je) { visit(jb, je, ns); });
+  }
+  // combine the lanes' sums (fixed butterfly order)
+  auto red = [](double &v) {
+#pragma unroll
+    for (int o = CONTACT_LANES / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  };
+  red(dens); red(sum_w);
+  for (int k = 0; k < 3; k++) { red(sum_x[k]); red(sum_vk[k]); red(avg_rk[k]); red(gdx[k]); }
+  for (int k = 0; k < 4; k++) red(gdqk[k]);
+#pragma unroll
+  for (int o = CONTACT_LANES / 2; o > 0; o >>= 1) {
+    has |= __shfl_xor_sync(0xffffffffu, has, o);
+    const int r2 = __shfl_xor_sync(0xffffffffu, RR, o);
+    RR = r2 > RR ? r2 : RR;
+  }
+  if (!live) return;
   ContactRec out;
   out.flag = 0;
   out.RR = b;
   for (int k = 0; k < 3; k++) out.f[k] = out.tau[k] = 0.0;
-  if (!B.dyn) { rec[d] = out; return; }
-  const V4<T> xT = xd[d];
-  const double xr[3] = {(double)xT.x, (double)xT.y, (double)xT.z};
-  int cx, cy, cz;
-  grid_cell(g, xT.x, xT.y, xT.z, cx, cy, cz);
-  double dens = vol0D[d] * c.kc.w0;
-  double sum_x[3] = {0, 0, 0}, sum_vk[3] = {0, 0, 0}, avg_rk[3] = {0, 0, 0}, gdx[3] = {0, 0, 0};
-  double gdqk[4] = {0, 0, 0, 0};
-  double sum_w = 0.0;
-  bool has = false;
-  int RR = -1;
-  auto visit = [&](int jb, int je, int off) {
-    for (int j = jb; j < je; j++) {
-      int o = -1, bk;
-      if (off == 0) bk = bodyS[j];
-      else { o = dynSortedToBody[j]; if (o == d) continue; bk = bodyd[o]; }
-      const V4<T> xkT = BR[off + j].x;
-      if (!(dist2_rn(xT.x - xkT.x, xT.y - xkT.y, xT.z - xkT.z) < h2)) continue;
-      const double xk[3] = {(double)xkT.x, (double)xkT.y, (double)xkT.z};
-      const double rv[3] = {xr[0] - xk[0], xr[1] - xk[1], xr[2] - xk[2]};
-      const double rl = sqrt(dist2_rn(rv[0], rv[1], rv[2]));
-      const double w = cubic_W(rl, c.kc);
-      const double vol = off == 0 ? vol0S[j] : vol0D[o];
-      dens += vol * w;
-      if (bk == b) {
-        for (int k = 0; k < 3; k++) sum_x[k] += xk[k] * w;
-        sum_w += w;
-      } else {
-        has = true;
-        RR = bk > RR ? bk : RR;
-        const BodyState &C = bs[bk];
-        double vk[3];
-        sample_velocity(C, c, xk, vk);
-        for (int k = 0; k < 3; k++) { sum_vk[k] += vk[k] * w; avg_rk[k] += (xk[k] - C.x[k]) * w; }
-        const V3<double> gw = cubic_gradW(V3<double>{rv[0], rv[1], rv[2]}, rl, c.kh);
-        const double gv[3] = {vol * gw.x, vol * gw.y, vol * gw.z};
-        for (int k = 0; k < 3; k++) gdx[k] += gv[k];
-        if (c.grad) {
-          const V4<T> p0 = off == 0 ? x0S[j] : x0d[o];
-          double Gk[12];
-          grad_Rqp<double>(C.q[0], C.q[1], C.q[2], C.q[3], V3<double>{(double)p0.x, (double)p0.y, (double)p0.z}, Gk);
-          for (int q = 0; q < 4; q++) gdqk[q] -= gv[0] * Gk[q] + gv[1] * Gk[4 + q] + gv[2] * Gk[8 + q];
-        }
-      }
-    }
-  };
-  if (ns > 0) for_each_row(g, cstartS, cx, cy, cz, [&](int jb, int je) { visit(jb, je, 0); });
-  for_each_row(g, cstartD, cx, cy, cz, [&](int jb, int je) { visit(jb, je, ns); });
-  if (!has) { rec[d] = out; return; }
+  if (!B.dyn || !has) { if (sub == 0) rec[dd] = out; return; }
+  dens += vol0D[dd] * c.kc.w0;
   out.flag = 1;
   out.RR = RR;
-  const double ratio = dens / dens0D[d];
-  if (!(ratio > 1.0)) { rec[d] = out; return; }
+  const double ratio = dens / dens0D[dd];
+  if (!(ratio > 1.0)) { if (sub == 0) rec[dd] = out; return; }
   out.flag = 2;
   double normal[3], vrel[3], vr[3];
   sample_velocity(B, c, xr, vr);
@@ -173,61 +196,80 @@ static __global__ void __launch_bounds__(128) k_contact_samples(
   double tau[3];
   cross3(rr, f, tau);
   for (int k = 0; k < 3; k++) { out.f[k] = f[k]; out.tau[k] = tau[k]; }
-  rec[d] = out;
+  if (sub == 0) rec[dd] = out;
   if (!c.grad) return;
-  // ---- Jacobian blocks (:467-552)
-  const V4<T> p0 = x0d[d];
-  double GqB[12];
-  grad_Rqp<double>(B.q[0], B.q[1], B.q[2], B.q[3], V3<double>{(double)p0.x, (double)p0.y, (double)p0.z}, GqB);
-  double gdq[4];
-  for (int q = 0; q < 4; q++) gdq[q] = gdx[0] * GqB[q] + gdx[1] * GqB[4 + q] + gdx[2] * GqB[8 + q];
-  double gFn_d[3], gFf_d[3];
+  // ---- Jacobian blocks (RigidContactSolver.cpp:467-552), split between the lanes
+  double *D = blk + (size_t)dd * CONTACT_BLK, *X = D + NJAC;
+  double gFn_d[3], gFf_d[3], gd[3];
   for (int k = 0; k < 3; k++) gFn_d[k] = -c.beta * normal[k];
   {
     const double fd = Fn[0] * gFn_d[0] + Fn[1] * gFn_d[1] + Fn[2] * gFn_d[2];
     for (int k = 0; k < 3; k++) gFf_d[k] = (-c.mu * u[k]) * fd / fnn;
   }
-  double gd[3];  // d(normal + friction force) / d(density)
-  for (int k = 0; k < 3; k++) gd[k] = gFn_d[k] + gFf_d[k];
+  for (int k = 0; k < 3; k++) gd[k] = gFn_d[k] + gFf_d[k];  // d(normal + friction force) / d(density)
   double gFf_vr[9];
   {
-    const double s = (-c.mu * fnn) / vn;
+    const double sc = (-c.mu * fnn) / vn;
     for (int i = 0; i < 3; i++)
-      for (int j = 0; j < 3; j++) gFf_vr[3 * i + j] = s * ((i == j ? 1.0 : 0.0) - u[i] * u[j]);
+      for (int j = 0; j < 3; j++) gFf_vr[3 * i + j] = sc * ((i == j ? 1.0 : 0.0) - u[i] * u[j]);
   }
-  double Sr[9], Sa[9], Sf[9];
+  double Sr[9];
   skew3(V3<double>{rr[0], rr[1], rr[2]}, Sr);
-  skew3(V3<double>{avg_rk[0], avg_rk[1], avg_rk[2]}, Sa);
-  skew3(V3<double>{f[0], f[1], f[2]}, Sf);
-  double *D = blk + (size_t)d * CONTACT_BLK, *X = D + NJAC;
-  for (int k = 0; k < CONTACT_BLK; k++) D[k] = 0.0;
-  double gfx[9], gfq[12], gfqk[12];
-  for (int i = 0; i < 3; i++) {
+  double gfx[9];
+  for (int i = 0; i < 3; i++)
     for (int j = 0; j < 3; j++) gfx[3 * i + j] = gd[i] * gdx[j];
-    for (int q = 0; q < 4; q++) { gfq[4 * i + q] = gd[i] * gdq[q]; gfqk[4 * i + q] = gd[i] * gdqk[q]; }
-  }
-  double *DFv = D, *DFx = D + 9, *DFw = D + 18, *DFq = D + 27, *DTx = D + 57, *DTq = D + 66;
-  double *XFv = X, *XFx = X + 9, *XFw = X + 18, *XFq = X + 27, *XTx = X + 57, *XTq = X + 66;
-  for (int k = 0; k < 9; k++) { DFx[k] = gfx[k]; DFv[k] = gFf_vr[k]; XFv[k] = -gFf_vr[k]; XFx[k] = -gfx[k]; }
-  for (int k = 0; k < 12; k++) { DFq[k] = gfq[k]; XFq[k] = gfqk[k]; }
-  mm<3, 3, 3>(Sr, gfx, DTx);
-  for (int k = 0; k < 9; k++) XTx[k] = -DTx[k];
-  // Fw = gFf_vr skew(r)^T, cross Fw = -gFf_vr skew(avg_rk)^T
-  mmT3(gFf_vr, Sr, DFw);
-  {
-    double t[9];
-    mmT3(gFf_vr, Sa, t);
-    for (int k = 0; k < 9; k++) XFw[k] = -t[k];
-  }
-  // Tq = skew(r) gfq + skew(f)^T GqB; cross Tq = skew(r) gfqk
-  {
-    double a[12], SfT[9], b2[12];
-    mm<3, 3, 4>(Sr, gfq, a);
-    for (int i = 0; i < 3; i++)
-      for (int j = 0; j < 3; j++) SfT[3 * i + j] = Sf[3 * j + i];
-    mm<3, 3, 4>(SfT, GqB, b2);
-    for (int k = 0; k < 12; k++) DTq[k] = a[k] + b2[k];
-    mm<3, 3, 4>(Sr, gfqk, XTq);
+  double *DFv = D, *DFx = D + 9, *DFw = D + 18, *DFq = D + 27, *DTw = D + 39, *DTv = D + 48, *DTx = D + 57,
+         *DTq = D + 66;
+  double *XFv = X, *XFx = X + 9, *XFw = X + 18, *XFq = X + 27, *XTw = X + 39, *XTv = X + 48, *XTx = X + 57,
+         *XTq = X + 66;
+  switch (sub) {
+    case 0:
+      for (int k = 0; k < 9; k++) { DFx[k] = gfx[k]; DFv[k] = gFf_vr[k]; XFv[k] = -gFf_vr[k]; XFx[k] = -gfx[k]; }
+      break;
+    case 1: {
+      mm<3, 3, 3>(Sr, gfx, DTx);
+      for (int k = 0; k < 9; k++) XTx[k] = -DTx[k];
+      break;
+    }
+    case 2:
+    case 3:
+    case 4: {
+      const V4<T> p0 = x0d[dd];
+      double GqB[12], gdq[4];
+      grad_Rqp<double>(B.q[0], B.q[1], B.q[2], B.q[3], V3<double>{(double)p0.x, (double)p0.y, (double)p0.z}, GqB);
+      for (int q = 0; q < 4; q++) gdq[q] = gdx[0] * GqB[q] + gdx[1] * GqB[4 + q] + gdx[2] * GqB[8 + q];
+      if (sub == 2) {
+        for (int i = 0; i < 3; i++)
+          for (int q = 0; q < 4; q++) { DFq[4 * i + q] = gd[i] * gdq[q]; XFq[4 * i + q] = gd[i] * gdqk[q]; }
+      } else if (sub == 3) {  // Tq = skew(r) gfq + skew(f)^T GqB
+        double gfq[12], a[12], Sf[9], SfT[9], b2[12];
+        for (int i = 0; i < 3; i++)
+          for (int q = 0; q < 4; q++) gfq[4 * i + q] = gd[i] * gdq[q];
+        mm<3, 3, 4>(Sr, gfq, a);
+        skew3(V3<double>{f[0], f[1], f[2]}, Sf);
+        for (int i = 0; i < 3; i++)
+          for (int j = 0; j < 3; j++) SfT[3 * i + j] = Sf[3 * j + i];
+        mm<3, 3, 4>(SfT, GqB, b2);
+        for (int k = 0; k < 12; k++) DTq[k] = a[k] + b2[k];
+      } else {  // cross Tq = skew(r) gfqk
+        double gfqk[12];
+        for (int i = 0; i < 3; i++)
+          for (int q = 0; q < 4; q++) gfqk[4 * i + q] = gd[i] * gdqk[q];
+        mm<3, 3, 4>(Sr, gfqk, XTq);
+      }
+      break;
+    }
+    case 5: {  // Fw = gFf_vr skew(r)^T, cross Fw = -gFf_vr skew(avg_rk)^T
+      double Sa[9], t9[9];
+      skew3(V3<double>{avg_rk[0], avg_rk[1], avg_rk[2]}, Sa);
+      mmT3(gFf_vr, Sr, DFw);
+      mmT3(gFf_vr, Sa, t9);
+      for (int k = 0; k < 9; k++) XFw[k] = -t9[k];
+      break;
+    }
+    default:  // the torque-to-v / omega blocks of the contact force are zero
+      for (int k = 0; k < 9; k++) { DTw[k] = 0.0; DTv[k] = 0.0; XTw[k] = 0.0; XTv[k] = 0.0; }
+      break;
   }
 }
 
@@ -362,82 +404,93 @@ static __device__ void mgr_stage_coef(const double *q, const double *I0, const d
   mv3(RT, vb, tmp); mv3(I0, tmp, tmp2); grad_Rqp_d(q, tmp2, gRq_b); grad_RqTp_d(q, vb, gRTq_b);
 }
 
-// One block. S (13 nb x 6 nb, row-major: row = 13 body + component, column = 6 body + j,
-// j < 3 the v0 columns) advances by one step; A (two 13 nb x 13 nb maps, v0 then omega0
-// columns, row-major, A[r][c] = component r of the column that starts as unit vector c) is
-// written when tape_step is set. M holds the manager's blocks (the fluid's diagonal blocks
-// are written here first); Mc the contact solver's blocks of this step, which replace M's
-// for every dynamic pair at the end.
-static __global__ void __launch_bounds__(256) k_manager_chain(const BodyState *__restrict__ bs, MgrConsts mc,
-                                                              double *__restrict__ M, const double *__restrict__ Mc,
-                                                              double *__restrict__ S, double *__restrict__ tape_step) {
-  __shared__ MgrCoef Cs[DFSPH_MAX_BODIES_DEV];
+// The manager's step runs as three kernels: the per-body coefficients (two threads per body,
+// one per stage) with the fluid's diagonal blocks written into M
+// (BoundaryModel_Akinci2012::update_rigid_body_gradient_manager, :952-967); then one block
+// per column of the state S (13 nb x 6 nb, row-major: row = 13 body + component, column =
+// 6 body + j, j < 3 the v0 columns) and per column of the step maps A (two 13 nb x 13 nb
+// maps, v0 then omega0 columns, row-major, A[r][c] = component r of the column that starts
+// as unit vector c; written when tape_step is set), spread over the SMs because FP64 runs
+// at a low rate on this part; then the contact solver's blocks of this step replace M's
+// for every dynamic pair (RigidContactSolver::update_rigid_body_gradient_manager,
+// :1341-1369).
+static __global__ void k_manager_coef(const BodyState *__restrict__ bs, MgrConsts mc, double *__restrict__ M,
+                                      MgrCoef *__restrict__ coefs) {
   const int nb = mc.nb, t = threadIdx.x;
   if (nb > DFSPH_MAX_BODIES_DEV) return;
   const bool gyro = mc.gyroscopic != 0;
-  if (mc.chain)
-  for (int a = t; a < nb; a += blockDim.x) {
+  if (t < 2 * nb) {
+    const int a = t >> 1;
     const BodyState &B = bs[a];
-    MgrCoef &C = Cs[a];
-    C.dyn = B.dyn;
-    C.invMass = B.invMass;
-    for (int k = 0; k < 9; k++) { C.I[k] = B.Ipre[k]; C.Iinv[k] = B.Iipre[k]; C.I0[k] = B.I0[k]; }
-    q_to_R(B.qpre, C.R);
-    mgr_stage_coef(B.qpre, B.I0, B.Ipre, B.Iipre, B.wpre, B.T, gyro, C.Iom2, C.om2, C.gRq_a2, C.gRTq_a2, C.gRq_b2,
-                   C.gRTq_b2);
-    const double zero[3] = {0.0, 0.0, 0.0};
-    mgr_stage_coef(B.qpre, B.I0, B.Ipre, B.Iipre, B.wmid, zero, gyro, C.Iom3, C.om3, C.gRq_a3, C.gRTq_a3, C.gRq_b3,
-                   C.gRTq_b3);
-    const double p[4] = {0.0, B.wmid[0], B.wmid[1], B.wmid[2]};
-    double pq[4], nq[4];
-    q_mul(p, B.qpre, pq);
-    for (int k = 0; k < 4; k++) nq[k] = B.qpre[k] + mc.dt * 0.5 * pq[k];
-    const double nn = sqrt(nq[0] * nq[0] + nq[1] * nq[1] + nq[2] * nq[2] + nq[3] * nq[3]);
-    double nv[4];
-    for (int k = 0; k < 4; k++) nv[k] = nq[k] / nn;
-    for (int i = 0; i < 4; i++)
-      for (int j = 0; j < 4; j++) C.Gn[4 * i + j] = ((i == j ? 1.0 : 0.0) - nv[i] * nv[j]) / nn;
-    const double Gpq[16] = {p[0], -p[1], -p[2], -p[3], p[1], p[0], -p[3], p[2],
-                            p[2], p[3], p[0], -p[1], p[3], -p[2], p[1], p[0]};
-    for (int k = 0; k < 16; k++) C.Gpq[k] = Gpq[k];
-    const double *q = B.qpre;
-    const double Gpw[12] = {-q[1], -q[2], -q[3], q[0], q[3], -q[2], -q[3], q[0], q[1], q[2], -q[1], q[0]};
-    for (int k = 0; k < 12; k++) C.Gpw[k] = Gpw[k];
+    MgrCoef &C = coefs[a];
+    if ((t & 1) == 0) {
+      C.dyn = B.dyn;
+      C.invMass = B.invMass;
+      for (int k = 0; k < 9; k++) { C.I[k] = B.Ipre[k]; C.Iinv[k] = B.Iipre[k]; C.I0[k] = B.I0[k]; }
+      q_to_R(B.qpre, C.R);
+      mgr_stage_coef(B.qpre, B.I0, B.Ipre, B.Iipre, B.wpre, B.T, gyro, C.Iom2, C.om2, C.gRq_a2, C.gRTq_a2, C.gRq_b2,
+                     C.gRTq_b2);
+    } else {
+      const double zero[3] = {0.0, 0.0, 0.0};
+      mgr_stage_coef(B.qpre, B.I0, B.Ipre, B.Iipre, B.wmid, zero, gyro, C.Iom3, C.om3, C.gRq_a3, C.gRTq_a3, C.gRq_b3,
+                     C.gRTq_b3);
+      const double p[4] = {0.0, B.wmid[0], B.wmid[1], B.wmid[2]};
+      double pq[4], nq[4];
+      q_mul(p, B.qpre, pq);
+      for (int k = 0; k < 4; k++) nq[k] = B.qpre[k] + mc.dt * 0.5 * pq[k];
+      const double nn = sqrt(nq[0] * nq[0] + nq[1] * nq[1] + nq[2] * nq[2] + nq[3] * nq[3]);
+      double nv[4];
+      for (int k = 0; k < 4; k++) nv[k] = nq[k] / nn;
+      for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) C.Gn[4 * i + j] = ((i == j ? 1.0 : 0.0) - nv[i] * nv[j]) / nn;
+      const double Gpq[16] = {p[0], -p[1], -p[2], -p[3], p[1], p[0], -p[3], p[2],
+                              p[2], p[3], p[0], -p[1], p[3], -p[2], p[1], p[0]};
+      for (int k = 0; k < 16; k++) C.Gpq[k] = Gpq[k];
+      const double *q = B.qpre;
+      const double Gpw[12] = {-q[1], -q[2], -q[3], q[0], q[3], -q[2], -q[3], q[0], q[1], q[2], -q[1], q[0]};
+      for (int k = 0; k < 12; k++) C.Gpw[k] = Gpw[k];
+    }
   }
-  // BoundaryModel_Akinci2012::update_rigid_body_gradient_manager (:952-967): the fluid's net
-  // blocks of every dynamic body that is not animated
-  if (mc.chain && mc.fluid_blocks)
+  if (mc.fluid_blocks)
     for (int k = t; k < nb * NJAC; k += blockDim.x) {
       const int a = k / NJAC, e = k % NJAC;
       if (bs[a].dyn && !bs[a].anim) M[((size_t)a * nb + a) * NJAC + e] = bs[a].nets[e];
     }
-  __syncthreads();
+}
+
+// Block x: the state's columns first, then (with tape_step) the step maps' columns.
+static __global__ void __launch_bounds__(32) k_manager_columns(MgrConsts mc, const MgrCoef *__restrict__ coefs,
+                                                               const double *__restrict__ M,
+                                                               const double *__restrict__ Mc, double *__restrict__ S,
+                                                               double *__restrict__ tape_step) {
+  if (threadIdx.x != 0) return;
+  const int nb = mc.nb;
+  if (nb > DFSPH_MAX_BODIES_DEV) return;
   const int n = NSTATE * nb, ncol = 6 * nb;
+  int c = blockIdx.x;
   double s[NSTATE * DFSPH_MAX_BODIES_DEV];
-  // the step maps from unit columns
-  if (mc.chain && tape_step)
-    for (int k = t; k < 2 * n; k += blockDim.x) {
-      const int c = k % n;
-      const bool wcol = k >= n;
-      for (int r = 0; r < n; r++) s[r] = (r == c) ? 1.0 : 0.0;
-      mgr_apply(Cs, mc, M, Mc, s, wcol);
-      double *A = tape_step + (wcol ? (size_t)n * n : 0);
-      for (int r = 0; r < n; r++) A[(size_t)r * n + c] = s[r];
-    }
-  // the state's columns
-  if (mc.chain)
-  for (int c = t; c < ncol; c += blockDim.x) {
+  if (c < ncol) {
     for (int r = 0; r < n; r++) s[r] = S[(size_t)r * ncol + c];
-    mgr_apply(Cs, mc, M, Mc, s, (c % 6) >= 3);
+    mgr_apply(coefs, mc, M, Mc, s, (c % 6) >= 3);
     for (int r = 0; r < n; r++) S[(size_t)r * ncol + c] = s[r];
+    return;
   }
-  __syncthreads();
-  // RigidContactSolver::update_rigid_body_gradient_manager (:1341-1369)
-  if (mc.contact_stage)
-    for (int k = t; k < nb * nb * NJAC; k += blockDim.x) {
-      const int pr = k / NJAC, a = pr / nb, c = pr % nb;
-      if (bs[a].dyn && bs[c].dyn) M[k] = Mc[k];
-    }
+  c -= ncol;
+  if (!tape_step || c >= 2 * n) return;
+  const int cc = c % n;
+  const bool wcol = c >= n;
+  for (int r = 0; r < n; r++) s[r] = (r == cc) ? 1.0 : 0.0;
+  mgr_apply(coefs, mc, M, Mc, s, wcol);
+  double *A = tape_step + (wcol ? (size_t)n * n : 0);
+  for (int r = 0; r < n; r++) A[(size_t)r * n + cc] = s[r];
+}
+
+static __global__ void k_manager_blocks(const BodyState *__restrict__ bs, int nb, double *__restrict__ M,
+                                        const double *__restrict__ Mc) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nb * nb * NJAC; k += gridDim.x * blockDim.x) {
+    const int pr = k / NJAC, a = pr / nb, c = pr % nb;
+    if (bs[a].dyn && bs[c].dyn) M[k] = Mc[k];
+  }
 }
 
 // Reverse sweep over the manager's step maps: lam_v <- A_v^T lam_v, lam_w <- A_w^T lam_w

@@ -229,6 +229,26 @@ def config1(seed=0, **kw):
     return dam_break_sphere(seed=seed, **kw)
 
 
+def dam_break_two_spheres(seed=0, gap=0.01, speed=0.5, beta=2000.0, **kw):
+    """The 1M dam break with a second sphere beside the first, `gap` apart surface to
+    surface (within one support radius) and the two moving towards each other along x, with
+    the rigid contact solver and the gradient manager on."""
+    sc = dam_break_sphere(seed=seed, use_rigid_contact_solver=1, use_rigid_gradient_manager=1,
+                          rigid_contact_beta=beta, **kw)
+    first = sc.bodies[1]
+    R = float(np.linalg.norm(first.samples, axis=1).max())
+    cx, cy, cz = first.translation
+    first.translation = (cx - (R + 0.5 * gap), cy, cz)
+    first.init_velocity = (speed, 0.0, 0.0)
+    second = Body(samples=first.samples.copy(), translation=(cx + R + 0.5 * gap, cy, cz),
+                  density=first.density, is_dynamic=True, init_velocity=(-speed, 0.0, 0.0),
+                  init_angular_velocity=tuple(-np.asarray(first.init_angular_velocity)),
+                  target_x=first.target_x)
+    sc.bodies.append(second)
+    sc.name = f"dam_break_two_spheres_{sc.n_fluid}"
+    return sc
+
+
 def pool_ellipsoid(n=(125, 16, 125), r=0.004, pool=(1.0, 0.5, 1.0), seed=0, dt=0.0005, steps=1000,
                    precision=_abi.DFSPH_FP32, **kw):
     """250,000-particle layer (125 x 16 x 125 at r = 0.004) in an open 1.0 x 0.5 x 1.0 m pool
