@@ -218,7 +218,10 @@ class Engine : public EngineBase {
   cudaStream_t stream_ = nullptr;
   cudaStream_t stream2_ = nullptr;  // rigid kernels (overlap the next step's fluid sort)
   cudaEvent_t ev_fluid_done_ = nullptr, ev_rigid_done_ = nullptr;
-  bool rigid_pending_ = false;
+  cudaEvent_t ev_rigid_state_ = nullptr;  // after k_rigid_step (bodies and samples of the step)
+  cudaEvent_t ev_contact_in_ = nullptr;   // the fluid stream's point where the contact pass may start
+  bool rigid_pending_ = false, rigid_state_pending_ = false;
+  bool contact_launched_ = false;  // this step's contact pass is already on the rigid stream
   int64_t launches_ = 0;
 
   // host copies
@@ -349,6 +352,14 @@ class Engine : public EngineBase {
     if (!rigid_pending_) return;
     DF_CK(cudaStreamWaitEvent(stream_, ev_rigid_done_, 0));
     rigid_pending_ = false;
+    rigid_state_pending_ = false;
+  }
+  // the next step's fluid work needs the bodies and their samples after k_rigid_step, not
+  // the gradient manager's kernels, which only the rigid stream and host calls read
+  void wait_rigid_state() {
+    if (!rigid_state_pending_) return;
+    DF_CK(cudaStreamWaitEvent(stream_, ev_rigid_state_, 0));
+    rigid_state_pending_ = false;
   }
   void sync_all() {
     wait_rigid();
@@ -395,6 +406,7 @@ class Engine : public EngineBase {
   void launch_velocity(T *kappa_acc);
   void launch_pairs(bool pressure, bool warm, bool grad);
   void rigid_end();
+  void launch_contact();
   double read_residual();
   void grow_tape();
   void upload_fluid_initial();

@@ -233,6 +233,8 @@ Engine<T>::Engine(const dfsph_scene *sc) {
   DF_CK(cudaStreamCreateWithFlags(&stream2_, cudaStreamNonBlocking));
   DF_CK(cudaEventCreateWithFlags(&ev_fluid_done_, cudaEventDisableTiming));
   DF_CK(cudaEventCreateWithFlags(&ev_rigid_done_, cudaEventDisableTiming));
+  DF_CK(cudaEventCreateWithFlags(&ev_rigid_state_, cudaEventDisableTiming));
+  DF_CK(cudaEventCreateWithFlags(&ev_contact_in_, cudaEventDisableTiming));
   {
     int dev = 0;
     DF_CK(cudaGetDevice(&dev));
@@ -411,6 +413,8 @@ Engine<T>::~Engine() {
   if (stream_) cudaStreamSynchronize(stream_);
   if (ev_fluid_done_) cudaEventDestroy(ev_fluid_done_);
   if (ev_rigid_done_) cudaEventDestroy(ev_rigid_done_);
+  if (ev_rigid_state_) cudaEventDestroy(ev_rigid_state_);
+  if (ev_contact_in_) cudaEventDestroy(ev_contact_in_);
   if (stream2_) cudaStreamDestroy(stream2_);
   for (auto &e : ev_) if (e) cudaEventDestroy(e);
   for (auto &r : pending_) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
@@ -775,6 +779,8 @@ void Engine<T>::rigid_end() {
   }
   const bool mgr_chain = manager_ && P_.enable_gradient;
   const bool mgr_blocks = manager_ && contact_;
+  if (contact_ && !contact_launched_) launch_contact();
+  contact_launched_ = false;
   DF_CK(cudaEventRecord(ev_fluid_done_, stream_));
   DF_CK(cudaStreamWaitEvent(stream2_, ev_fluid_done_, 0));
   pbegin(stream2_);
@@ -783,16 +789,8 @@ void Engine<T>::rigid_end() {
     k_body_partials<T><<<nchunks_, RED_THREADS, 0, stream2_>>>(bs_.p, chunks_.p, xd_.p, acc_.p, red_part_.p);
     nl++;
   }
-  ContactStep cs{nullptr, nullptr, nullptr, ccount_.p, nullptr};
+  ContactStep cs{nullptr, nullptr, nullptr, ccount_.p, nullptr, mgr_chain ? mgrM_.p : nullptr};
   if (contact_) {
-    cc_.dt = rc_.dt;
-    cc_.grad = manager_ ? 1 : 0;
-    // samples of the dynamic bodies against every boundary sample; the dynamic cell table
-    // is this step's (the samples have not moved since sort_dynamic)
-    k_contact_samples<T><<<blocks(nd_ * CONTACT_LANES, 128), 128, 0, stream2_>>>(
-        cc_, fc_.grid, fc_.h2, ns_, nd_, bs_.p, BR_.p, cstartS_.p, cstartD_.p, bodyS_.p, x0S_.p, bodyd_.p,
-        dynSortedToBody_.p, xd_.p, x0d_.p, cvol0S_.p, cvol0D_.p, cdens0D_.p, crec_.p, cc_.grad ? cblk_.p : nullptr);
-    nl++;
     cs.rec = crec_.p;
     cs.list = clist_.p;
     if (mgr_blocks) { cs.blk = cblk_.p; cs.Mc = Mc_.p; }
@@ -800,11 +798,12 @@ void Engine<T>::rigid_end() {
   k_rigid_step<T><<<nb_, 128, 0, stream2_>>>(bs_.p, nb_, rc_, manager_ ? nullptr : tape_step, cs, body_chunks_.p,
                                              red_part_.p, x0d_.p, xd_.p, vd_.p);
   nl++;
+  DF_CK(cudaEventRecord(ev_rigid_state_, stream2_));
   if (mgr_chain || mgr_blocks) {
-    MgrConsts mc{rc_.dt, nb_, rc_.gyroscopic, n_ > 0 ? 1 : 0, contact_ ? 1 : 0, 1, mgr_chain ? 1 : 0};
+    MgrConsts mc{rc_.dt, nb_, rc_.gyroscopic, n_ > 0 ? 1 : 0, contact_ ? 1 : 0, mgr_chain ? 1 : 0};
     if (mgr_chain) {
       const int ncol = 6 * nb_ + (tape_step ? 2 * NSTATE * nb_ : 0);
-      k_manager_coef<<<1, 64, 0, stream2_>>>(bs_.p, mc, mgrM_.p, mgrC_.p);
+      k_manager_coef<<<1, 64, 0, stream2_>>>(bs_.p, mc, mgrC_.p);
       k_manager_columns<<<ncol, 32, 0, stream2_>>>(mc, mgrC_.p, mgrM_.p, Mc_.p, mgrS_.p, tape_step);
       nl += 2;
     }
@@ -817,6 +816,29 @@ void Engine<T>::rigid_end() {
   pend(DFSPH_K_RIGID, nd_, stream2_);
   DF_CK(cudaEventRecord(ev_rigid_done_, stream2_));
   rigid_pending_ = true;
+  rigid_state_pending_ = true;
+  check_launch();
+}
+
+// The contact pass reads only the bodies and their samples as the step found them (after
+// the velocity overrides and this step's sort of the samples), which the fluid solve does
+// not change: it runs on the rigid stream from the point the fluid stream has reached.
+template <class T>
+void Engine<T>::launch_contact() {
+  if (nd_ == 0) return;
+  DF_CK(cudaEventRecord(ev_contact_in_, stream_));
+  DF_CK(cudaStreamWaitEvent(stream2_, ev_contact_in_, 0));
+  pbegin(stream2_);
+  cc_.dt = rc_.dt;
+  cc_.grad = manager_ ? 1 : 0;
+  // samples of the dynamic bodies against every boundary sample; the dynamic cell table
+  // is this step's
+  k_contact_samples<T><<<blocks(nd_ * CONTACT_LANES, 128), 128, 0, stream2_>>>(
+      cc_, fc_.grid, fc_.h2, ns_, nd_, bs_.p, BR_.p, cstartS_.p, cstartD_.p, bodyS_.p, x0S_.p, bodyd_.p,
+      dynSortedToBody_.p, xd_.p, x0d_.p, cvol0S_.p, cvol0D_.p, cdens0D_.p, crec_.p, cc_.grad ? cblk_.p : nullptr);
+  launched();
+  pend(DFSPH_K_RIGID, nd_, stream2_);
+  contact_launched_ = true;
   check_launch();
 }
 
@@ -829,7 +851,7 @@ int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
   for (int s = 0; s < nsteps; s++) {
     const double h_step = dt_cur_;  // the step's initial size (positions, time)
     sort_fluid();  // overlaps the previous step's rigid kernels
-    wait_rigid();
+    wait_rigid_state();
     begin_step();
     sort_dynamic();
     if (n_ > 0) {
@@ -889,6 +911,8 @@ int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
       // (updateTimeStepSize runs after the non-pressure forces, TimeStepDiffDFSPH.cpp:583;
       // the advection, position update and time advance keep the step's initial size)
       if (P_.cfl_method == 1) set_dt(cfl_time_step());
+      // the contact pass overlaps the pressure solve (it needs the step size of the rigid step)
+      if (contact_) launch_contact();
       solve(true);
       if (ml_record_ && P_.use_pressure_warmstart) {
         k_ml_target<T><<<blocks(n_), 256, 0, stream_>>>(n_, kappa_[cur_].p, kfin_.p);

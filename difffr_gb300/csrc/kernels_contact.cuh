@@ -289,7 +289,7 @@ struct MgrCoef {
 
 struct MgrConsts {
   double dt;
-  int nb, gyroscopic, fluid_stage, contact_stage, fluid_blocks;
+  int nb, gyroscopic, fluid_stage, contact_stage;
   int chain;  // 0: only carry the contact blocks forward (gradients off), 1: advance the chain too
 };
 
@@ -404,9 +404,9 @@ static __device__ void mgr_stage_coef(const double *q, const double *I0, const d
   mv3(RT, vb, tmp); mv3(I0, tmp, tmp2); grad_Rqp_d(q, tmp2, gRq_b); grad_RqTp_d(q, vb, gRTq_b);
 }
 
-// The manager's step runs as three kernels: the per-body coefficients (two threads per body,
-// one per stage) with the fluid's diagonal blocks written into M
-// (BoundaryModel_Akinci2012::update_rigid_body_gradient_manager, :952-967); then one block
+// The manager's step runs as three kernels after k_rigid_step (which writes the fluid's
+// diagonal blocks into M): the per-body coefficients (two threads per body, one per stage);
+// then one block
 // per column of the state S (13 nb x 6 nb, row-major: row = 13 body + component, column =
 // 6 body + j, j < 3 the v0 columns) and per column of the step maps A (two 13 nb x 13 nb
 // maps, v0 then omega0 columns, row-major, A[r][c] = component r of the column that starts
@@ -414,8 +414,7 @@ static __device__ void mgr_stage_coef(const double *q, const double *I0, const d
 // at a low rate on this part; then the contact solver's blocks of this step replace M's
 // for every dynamic pair (RigidContactSolver::update_rigid_body_gradient_manager,
 // :1341-1369).
-static __global__ void k_manager_coef(const BodyState *__restrict__ bs, MgrConsts mc, double *__restrict__ M,
-                                      MgrCoef *__restrict__ coefs) {
+static __global__ void k_manager_coef(const BodyState *__restrict__ bs, MgrConsts mc, MgrCoef *__restrict__ coefs) {
   const int nb = mc.nb, t = threadIdx.x;
   if (nb > DFSPH_MAX_BODIES_DEV) return;
   const bool gyro = mc.gyroscopic != 0;
@@ -451,11 +450,6 @@ static __global__ void k_manager_coef(const BodyState *__restrict__ bs, MgrConst
       for (int k = 0; k < 12; k++) C.Gpw[k] = Gpw[k];
     }
   }
-  if (mc.fluid_blocks)
-    for (int k = t; k < nb * NJAC; k += blockDim.x) {
-      const int a = k / NJAC, e = k % NJAC;
-      if (bs[a].dyn && !bs[a].anim) M[((size_t)a * nb + a) * NJAC + e] = bs[a].nets[e];
-    }
 }
 
 // Block x: the state's columns first, then (with tape_step) the step maps' columns.

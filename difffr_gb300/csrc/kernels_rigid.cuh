@@ -592,6 +592,8 @@ struct ContactStep {
   int *list;              // scratch: each body's force-carrying samples in order
   int *counts;            // per body: samples in contact, samples with a force
   double *Mc;             // [body][body][NJAC] contact blocks of this step, or null
+  double *Mf;             // the gradient manager's blocks: the fluid's diagonal block of each
+                          // dynamic, non-animated body goes to [b][b] (null: manager chain off)
 };
 
 // exclusive prefix over the block's threads (blockDim.x a multiple of 32, at most 1024)
@@ -821,6 +823,10 @@ static __global__ void __launch_bounds__(128) k_rigid_step(BodyState *__restrict
       cs.Mc[((size_t)b * nb + c) * NJAC + k] = acc;
     }
   }
+  // BoundaryModel_Akinci2012::update_rigid_body_gradient_manager (:952-967): the fluid's
+  // net blocks of this body for the manager's fluid stage
+  if (cs.Mf && B.dyn && !B.anim)
+    for (int e = t; e < NJAC; e += blockDim.x) cs.Mf[((size_t)b * rc.nbodies + b) * NJAC + e] = B.nets[e];
   __syncthreads();
   if (B.dyn || B.anim)
     for (int d = B.dstart + t; d < B.dstart + B.dcount; d += blockDim.x) sample_update(B, d, x0d, xd, vd);
