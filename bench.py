@@ -30,16 +30,16 @@ UNIT = "steps/s"
 
 # Algorithmic DRAM bytes per particle of each kernel class (FP32 fields, compulsory
 # traffic, neighbour gathers assumed cache-resident): the per-unit figures of the
-# measurement model, stated with the kernels in the design doc.
+# measurement model.
 ALGO_BYTES = {
     "sort": 92, "lists_density_factor": 32, "density_pass": 32, "velocity_pass": 52,
     "xsph_advect": 40, "integrate": 36, "bf_lists": 16, "pairs": 32, "rigid": 32,
 }
 
 
-# DRAM bytes per particle and launch (dram__bytes_read.sum + dram__bytes_write.sum) from the
-# ncu capture summarised in profiles/fluid_passes_dam_break_262k.md (262,144 particles, L2
-# flushed by ncu before each launch), scaled by the launch's particle count.
+# DRAM bytes per particle and launch (dram__bytes_read.sum + dram__bytes_write.sum) from an
+# ncu capture of the same passes on the 262,144-particle copy of the dam break (L2 flushed
+# by ncu before each launch), scaled by the launch's particle count.
 MEASURED_TRAFFIC = {"density_pass": 178.3, "velocity_pass": 179.5}
 
 
