@@ -184,3 +184,22 @@ def test_manager_and_contact_api_errors():
     assert g.lib.dfsph_get_manager_grad(g.h, 1, -1, out) == _abi.DFSPH_ERR_INVALID_ARG
     assert g.lib.dfsph_get_manager_jacobians(g.h, 1, 1, None) == _abi.DFSPH_ERR_INVALID_ARG
     assert g.lib.dfsph_get_contact_count(g.h, None, None) == _abi.DFSPH_ERR_INVALID_ARG
+
+
+def test_overlapped_steps_equal_single_steps():
+    """One call of 12 steps (the contact pass beside the pressure solve, the manager's
+    kernels beside the next step's fluid work) equals 12 calls of one step (each ending with
+    both streams synchronised): rigid states, contact counts and the manager's chain state
+    and blocks, bit for bit."""
+    sc = scn.two_sphere_contact()
+    a, b = DiffDFSPH(sc), DiffDFSPH(sc)
+    a.step(12)
+    for _ in range(12):
+        b.step(1)
+    assert a.contact_count() == b.contact_count()
+    for body in DYN:
+        for u, v in zip(a.rigid_state(body), b.rigid_state(body)):
+            np.testing.assert_array_equal(u, v)
+        for RR in DYN:
+            np.testing.assert_array_equal(a.manager_grad(body, RR), b.manager_grad(body, RR))
+            np.testing.assert_array_equal(a.manager_jacobians(body, RR), b.manager_jacobians(body, RR))

@@ -140,6 +140,13 @@ def test_deterministic_replay(gpu_lib):
     a.reset()
     a.step(5)
     assert np.array_equal(a.positions(), b.positions())
+    # five single-step calls (each ends with both streams synchronised) equal one call of
+    # five steps (the rigid stream overlapping the next step's fluid work)
+    c = make(sc)
+    for _ in range(5):
+        c.step(1)
+    assert np.array_equal(c.positions(), b.positions())
+    assert np.array_equal(c.rigid_grad(1), b.rigid_grad(1))
 
 
 def test_edge_cases_empty_and_no_bodies(gpu_lib, oracle_lib):
