@@ -222,6 +222,7 @@ class Engine : public EngineBase {
   cudaEvent_t ev_contact_in_ = nullptr;   // the fluid stream's point where the contact pass may start
   bool rigid_pending_ = false, rigid_state_pending_ = false;
   bool contact_launched_ = false;  // this step's contact pass is already on the rigid stream
+  bool fluid_done_recorded_ = false;  // ev_fluid_done_ marks this step's last solver sweep
   int64_t launches_ = 0;
 
   // host copies

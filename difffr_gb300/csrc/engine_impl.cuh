@@ -781,7 +781,8 @@ void Engine<T>::rigid_end() {
   const bool mgr_blocks = manager_ && contact_;
   if (contact_ && !contact_launched_) launch_contact();
   contact_launched_ = false;
-  DF_CK(cudaEventRecord(ev_fluid_done_, stream_));
+  if (!fluid_done_recorded_) DF_CK(cudaEventRecord(ev_fluid_done_, stream_));
+  fluid_done_recorded_ = false;
   DF_CK(cudaStreamWaitEvent(stream2_, ev_fluid_done_, 0));
   pbegin(stream2_);
   int nl = 0;
@@ -795,7 +796,7 @@ void Engine<T>::rigid_end() {
     cs.list = clist_.p;
     if (mgr_blocks) { cs.blk = cblk_.p; cs.Mc = Mc_.p; }
   }
-  k_rigid_step<T><<<nb_, 128, 0, stream2_>>>(bs_.p, nb_, rc_, manager_ ? nullptr : tape_step, cs, body_chunks_.p,
+  k_rigid_step<T><<<nb_, RIGID_THREADS, 0, stream2_>>>(bs_.p, nb_, rc_, manager_ ? nullptr : tape_step, cs, body_chunks_.p,
                                              red_part_.p, x0d_.p, xd_.p, vd_.p);
   nl++;
   DF_CK(cudaEventRecord(ev_rigid_state_, stream2_));
@@ -918,6 +919,10 @@ int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
         k_ml_target<T><<<blocks(n_), 256, 0, stream_>>>(n_, kappa_[cur_].p, kfin_.p);
         launched();
       }
+      // the rigid kernels need the bodies' forces of the last sweep, not the positions
+      // update: they start beside it
+      DF_CK(cudaEventRecord(ev_fluid_done_, stream_));
+      fluid_done_recorded_ = true;
       pbegin();
       k_integrate<T><<<blocks(n_), 256, 0, stream_>>>(fc_, R_[cur_].p, kappa_[cur_].p,
                                                       P_.use_pressure_warmstart ? 1 : 0, (T)h_step,

@@ -349,6 +349,7 @@ static __global__ void k_visc_boundary_force(FluidConsts<T> c, int nd, const V4<
 constexpr int RED_VALUES = 3 + NJAC + 3;  // force, jacobians, torque
 constexpr int RED_CHUNK = 16;
 constexpr int RED_THREADS = 128;
+constexpr int RIGID_THREADS = 416;  // k_rigid_step: one block per body
 static_assert(RED_VALUES <= RED_THREADS, "one thread per reduced value");
 struct RedChunk {
   int body, start, count;
@@ -363,19 +364,41 @@ static __global__ void __launch_bounds__(RED_THREADS) k_body_partials(const Body
   const RedChunk ch = chunks[blockIdx.x];
   const BodyState &B = bs[ch.body];
   const int v = threadIdx.x;
+  // the loads of a batch are issued together, then summed in sample order (FP64 adds have a
+  // long dependent latency on this part; the loads should not add theirs to each add)
+  constexpr int BATCH = 8;
+  static_assert(RED_CHUNK % BATCH == 0, "whole batches per chunk");
+  // the torque of each sample's force about the body's position, one sample per thread of
+  // the last warp (the FP64 cost is per warp instruction: the lanes share it)
+  __shared__ double tq[RED_CHUNK][3];
+  static_assert(RED_THREADS - 32 >= RED_VALUES && RED_CHUNK <= 32, "the last warp is free");
+  if (v >= RED_THREADS - 32 && v - (RED_THREADS - 32) < ch.count) {
+    const int d = ch.start + v - (RED_THREADS - 32);
+    const double *row = acc + (size_t)d * ACC_STRIDE;
+    const V4<T> xj = xd[d];
+    const double rx = (double)xj.x - B.x[0], ry = (double)xj.y - B.x[1], rz = (double)xj.z - B.x[2];
+    const double fx = row[0], fy = row[1], fz = row[2];
+    double *o = tq[v - (RED_THREADS - 32)];
+    o[0] = ry * fz - rz * fy;
+    o[1] = rz * fx - rx * fz;
+    o[2] = rx * fy - ry * fx;
+  }
+  __syncthreads();
   if (v < RED_VALUES) {
     double s = 0.0;
     if (v < 3 + NJAC) {
-      for (int d = ch.start; d < ch.start + ch.count; d++) s += acc[(size_t)d * ACC_STRIDE + v];
+      for (int k0 = 0; k0 < RED_CHUNK; k0 += BATCH) {
+        double a[BATCH];
+#pragma unroll
+        for (int k = 0; k < BATCH; k++)
+          a[k] = k0 + k < ch.count ? acc[(size_t)(ch.start + k0 + k) * ACC_STRIDE + v] : 0.0;
+#pragma unroll
+        for (int k = 0; k < BATCH; k++)
+          if (k0 + k < ch.count) s += a[k];
+      }
     } else {
       const int comp = v - 3 - NJAC;
-      for (int d = ch.start; d < ch.start + ch.count; d++) {
-        const double *row = acc + (size_t)d * ACC_STRIDE;
-        const V4<T> xj = xd[d];
-        const double rx = (double)xj.x - B.x[0], ry = (double)xj.y - B.x[1], rz = (double)xj.z - B.x[2];
-        const double fx = row[0], fy = row[1], fz = row[2];
-        s += comp == 0 ? ry * fz - rz * fy : (comp == 1 ? rz * fx - rx * fz : rx * fy - ry * fx);
-      }
+      for (int k = 0; k < ch.count; k++) s += tq[k][comp];
     }
     part[(size_t)blockIdx.x * RED_VALUES + v] = s;
   }
@@ -622,7 +645,7 @@ static __device__ __forceinline__ int block_exclusive_scan(int v, int *warp_tot,
 // partials in chunk order (the second stage of the body reduction); the body's samples are
 // moved last (SimulatorBase::updateBoundaryParticles).
 template <class T>
-static __global__ void __launch_bounds__(128) k_rigid_step(BodyState *__restrict__ bs, int nbodies, RigidConsts rc,
+static __global__ void __launch_bounds__(RIGID_THREADS) k_rigid_step(BodyState *__restrict__ bs, int nbodies, RigidConsts rc,
                                                     double *__restrict__ tape_step, ContactStep cs,
                                                     const int2 *__restrict__ body_chunks,
                                                     const double *__restrict__ red_part,
@@ -654,12 +677,25 @@ static __global__ void __launch_bounds__(128) k_rigid_step(BodyState *__restrict
     else B.T[t - 3 - NJAC] = tot;
   }
   __syncthreads();
+  // FP64 on this part costs about the same per warp instruction whatever the number of
+  // active lanes, and each of the SM's four sub-partitions issues its own warps' FP64 work:
+  // independent single-thread pieces run in separate warps between block barriers, and
+  // lane-parallel work shares a warp:
+  //   phase 1: chain coefficients, part A (warp 0) | velocity update (last warp)
+  //   phase 2: chain coefficients, part B (warps 0-3) | position update (last warp)
+  //   phase 3: the 13 chain columns in the lanes of warp 0
   // Without the contact solver the velocity and position step does not depend on the chain
-  // rule (which reads the state before it): one thread of the second warp computes it into
-  // sN while the first warp runs the chain; thread 0 takes it over after the chain.
+  // rule (which reads the state before it): the last warp computes it into sN and thread 0
+  // takes it over after the chain.
   __shared__ double sN[31];  // v w x q I Iinv
-  const bool early = cs.rec == nullptr && B.dyn && blockDim.x > 32;
-  if (early && t == 32) {
+  __shared__ double sVb[3];  // Iinv temp_v
+  const int wid = t >> 5, lane = t & 31, nwarps = blockDim.x >> 5;
+  const int et = (nwarps - 1) * 32;  // the thread that runs the velocity and position step
+  const bool early = cs.rec == nullptr && B.dyn && nwarps >= 5;
+  const bool chain = B.dyn && !B.anim && rc.enable_gradient && !rc.manager;
+  if (t == 0) B.chain_ran = chain ? 1 : 0;
+  // ---- phase 1
+  if (early && t == et) {
     double *v = sN, *w = sN + 3, *x = sN + 6, *q = sN + 9, *I = sN + 13, *Iinv = sN + 22;
     for (int k = 0; k < 3; k++) { v[k] = B.v[k]; w[k] = B.w[k]; x[k] = B.x[k]; }
     for (int k = 0; k < 4; k++) q[k] = B.q[k];
@@ -670,16 +706,12 @@ static __global__ void __launch_bounds__(128) k_rigid_step(BodyState *__restrict
       body_add_torque(w, I, Iinv, B.T, rc.gyroscopic, rc.dt);
       body_add_force(v, B.invMass, gm, rc.dt);
     }
-    body_animate(x, q, I, Iinv, v, w, B.I0, rc.dt);
   }
-  const bool chain = B.dyn && !B.anim && rc.enable_gradient && !rc.manager;
-  if (t == 0) B.chain_ran = chain ? 1 : 0;
   if (chain) {
     if (t == 0) {
       q_to_R(B.q, C.R);
-      for (int k = 0; k < 9; k++) { C.I0[k] = B.I0[k]; C.I[k] = B.I[k]; C.Iinv[k] = B.Iinv[k]; }
       for (int k = 0; k < 3; k++) C.om[k] = B.w[k];
-      mv3(C.I, C.om, C.Iom);
+      mv3(B.I, C.om, C.Iom);
       C.invMass = 1.0 / (B.mass + 1e-10);
       // temp_v (:601, :679, :743)
       if (rc.gradient_mode != 2) {
@@ -689,13 +721,27 @@ static __global__ void __launch_bounds__(128) k_rigid_step(BodyState *__restrict
         if (rc.gyroscopic) cross3(C.Iom, C.om, C.temp_v);
         else for (int k = 0; k < 3; k++) C.temp_v[k] = 0.0;
       }
-      // grad_inertia_v operands: v = omega and v = Iinv temp_v
-      double RT[9] = {C.R[0], C.R[3], C.R[6], C.R[1], C.R[4], C.R[7], C.R[2], C.R[5], C.R[8]};
-      double tmp[3], tmp2[3], va[3], vb[3];
-      for (int k = 0; k < 3; k++) va[k] = C.om[k];
-      mv3(C.Iinv, C.temp_v, vb);
-      mv3(RT, va, tmp); mv3(C.I0, tmp, tmp2); grad_Rqp_d(B.q, tmp2, C.gRq_a); grad_RqTp_d(B.q, va, C.gRTq_a);
-      mv3(RT, vb, tmp); mv3(C.I0, tmp, tmp2); grad_Rqp_d(B.q, tmp2, C.gRq_b); grad_RqTp_d(B.q, vb, C.gRTq_b);
+      mv3(B.Iinv, C.temp_v, sVb);
+    } else if (wid == 1 && lane < 9) {
+      C.I0[lane] = B.I0[lane]; C.I[lane] = B.I[lane]; C.Iinv[lane] = B.Iinv[lane];
+    }
+    for (int k = t; k < NSTATE * 6; k += blockDim.x) Gold[k] = B.G[k];
+  }
+  __syncthreads();
+  // ---- phase 2
+  if (early && t == et) body_animate(sN + 6, sN + 9, sN + 13, sN + 22, sN, sN + 3, B.I0, rc.dt);
+  if (chain && lane == 0 && wid < 4) {
+    // grad_inertia_v operands: v = omega (a) and v = Iinv temp_v (b)
+    const double RT[9] = {C.R[0], C.R[3], C.R[6], C.R[1], C.R[4], C.R[7], C.R[2], C.R[5], C.R[8]};
+    const double *va = C.om, *vb = sVb;
+    double tmp[3], tmp2[3];
+    if (wid == 0) {
+      mv3(RT, va, tmp); mv3(B.I0, tmp, tmp2); grad_Rqp_d(B.q, tmp2, C.gRq_a);
+    } else if (wid == 1) {
+      grad_RqTp_d(B.q, va, C.gRTq_a); grad_RqTp_d(B.q, vb, C.gRTq_b);
+    } else if (wid == 2) {
+      mv3(RT, vb, tmp); mv3(B.I0, tmp, tmp2); grad_Rqp_d(B.q, tmp2, C.gRq_b);
+    } else {
       // rotation block (:827-888)
       double nom[3];
       for (int k = 0; k < 3; k++) nom[k] = C.om[k] + rc.dt * vb[k];
@@ -715,8 +761,12 @@ static __global__ void __launch_bounds__(128) k_rigid_step(BodyState *__restrict
       const double Gpw[12] = {-q[1], -q[2], -q[3], q[0], q[3], -q[2], -q[3], q[0], q[1], q[2], -q[1], q[0]};
       for (int k = 0; k < 12; k++) C.Gpw[k] = Gpw[k];
     }
-    for (int k = t; k < NSTATE * 6; k += blockDim.x) Gold[k] = B.G[k];
-    __syncthreads();
+  }
+  __syncthreads();
+  // ---- phase 3
+  if (chain) {
+    // the columns in the lanes of one warp: an FP64 warp instruction costs the same with 13
+    // active lanes as with one, so more warps would only queue on the FP64 units
     if (t < NSTATE) {
       double e[NSTATE], col[NSTATE];
       for (int k = 0; k < NSTATE; k++) e[k] = (k == t) ? 1.0 : 0.0;
