@@ -260,24 +260,29 @@ static __global__ void __launch_bounds__(128) k_pairs(FluidConsts<T> c, PairCons
       for (int k2 = 0; k2 < 9; k2++) { J[48 + k2] += Tv[k2]; J[57 + k2] += Tx[k2]; }
     }
   }
-  // warp reductions (fixed butterfly order), FP32 partials into the FP64 row
+  // warp reductions (fixed butterfly order); the sums go through shared memory so that the
+  // lanes add them into the FP64 row together (an FP64 warp instruction costs about the same
+  // for one active lane as for 32)
+  static_assert(ACC_FORCE == 0 && ACC_JAC == 3, "row layout: force, then the Jacobian terms");
+  __shared__ T wsum[128 / 32][3 + NJAC];
+  T *ws = wsum[threadIdx.x >> 5];
 #pragma unroll
-  for (int k = 0; k < 3; k++)
+  for (int k = 0; k < 3; k++) {
     for (int o = 16; o > 0; o >>= 1) facc[k] += __shfl_xor_sync(0xffffffffu, facc[k], o);
-  double *row = acc + (size_t)d * ACC_STRIDE;
-  if (lane == 0) {
-    row[ACC_FORCE + 0] += (double)facc[0];
-    row[ACC_FORCE + 1] += (double)facc[1];
-    row[ACC_FORCE + 2] += (double)facc[2];
+    if (lane == 0) ws[ACC_FORCE + k] = facc[k];
   }
   if (grad) {
 #pragma unroll
     for (int k = 0; k < NJAC; k++) {
       T s = J[k];
       for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (lane == 0) row[ACC_JAC + k] += (double)s;
+      if (lane == 0) ws[ACC_JAC + k] = s;
     }
   }
+  __syncwarp();
+  double *row = acc + (size_t)d * ACC_STRIDE;
+  const int nvals = grad ? 3 + NJAC : 3;
+  for (int k = lane; k < nvals; k += 32) row[k] += (double)ws[k];
 }
 
 // CFL: max squared speed over the fluid records and the samples of dynamic or animated
