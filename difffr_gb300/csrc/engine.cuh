@@ -217,9 +217,13 @@ class Engine : public EngineBase {
   int ncell_ = 0;
   cudaStream_t stream_ = nullptr;
   cudaStream_t stream2_ = nullptr;  // rigid kernels (overlap the next step's fluid sort)
+  cudaStream_t stream3_ = nullptr;  // the per-body chain rule (overlaps the next step)
   cudaEvent_t ev_fluid_done_ = nullptr, ev_rigid_done_ = nullptr;
   cudaEvent_t ev_rigid_state_ = nullptr;  // after k_rigid_step (bodies and samples of the step)
   cudaEvent_t ev_contact_in_ = nullptr;   // the fluid stream's point where the contact pass may start
+  cudaEvent_t ev_chain_done_ = nullptr;   // after k_rigid_chain
+  bool chain_pending_ = false;            // k_rigid_chain may still run (G and the tape not final)
+  bool hbs_chain_stale_ = false;          // the host mirror was copied while k_rigid_chain could run
   bool rigid_pending_ = false, rigid_state_pending_ = false;
   bool contact_launched_ = false;  // this step's contact pass is already on the rigid stream
   bool fluid_done_recorded_ = false;  // ev_fluid_done_ marks this step's last solver sweep
@@ -349,7 +353,18 @@ class Engine : public EngineBase {
   }
   // the rigid kernels' stream: the main stream waits for them before it touches rigid
   // data; host synchronisation waits for both
+  // everything queued on the rigid streams (the bodies, the gradient manager and the
+  // per-body chain rule)
   void wait_rigid() {
+    wait_rigid_except_chain();
+    if (chain_pending_) {
+      DF_CK(cudaStreamWaitEvent(stream_, ev_chain_done_, 0));
+      chain_pending_ = false;
+    }
+  }
+  // the end of a step call: the bodies and the manager, while the per-body chain rule (which
+  // only gradient reads and the adjoint need) may still run on its own stream
+  void wait_rigid_except_chain() {
     if (!rigid_pending_) return;
     DF_CK(cudaStreamWaitEvent(stream_, ev_rigid_done_, 0));
     rigid_pending_ = false;
@@ -387,7 +402,7 @@ class Engine : public EngineBase {
   int64_t dev_epoch_ = 0, hbs_epoch_ = -1;
   std::vector<BodyState> hbs_;
   const BodyState &host_body(int b) {
-    if (hbs_epoch_ != dev_epoch_) { body_state_download(hbs_); hbs_epoch_ = dev_epoch_; }
+    if (hbs_epoch_ != dev_epoch_) { body_state_download(hbs_); hbs_epoch_ = dev_epoch_; hbs_chain_stale_ = false; }
     return hbs_[b];
   }
   void check_launch() { DF_CK(cudaGetLastError()); }

@@ -231,10 +231,12 @@ Engine<T>::Engine(const dfsph_scene *sc) {
 
   DF_CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
   DF_CK(cudaStreamCreateWithFlags(&stream2_, cudaStreamNonBlocking));
+  DF_CK(cudaStreamCreateWithFlags(&stream3_, cudaStreamNonBlocking));
   DF_CK(cudaEventCreateWithFlags(&ev_fluid_done_, cudaEventDisableTiming));
   DF_CK(cudaEventCreateWithFlags(&ev_rigid_done_, cudaEventDisableTiming));
   DF_CK(cudaEventCreateWithFlags(&ev_rigid_state_, cudaEventDisableTiming));
   DF_CK(cudaEventCreateWithFlags(&ev_contact_in_, cudaEventDisableTiming));
+  DF_CK(cudaEventCreateWithFlags(&ev_chain_done_, cudaEventDisableTiming));
   {
     int dev = 0;
     DF_CK(cudaGetDevice(&dev));
@@ -409,13 +411,16 @@ void Engine<T>::manager_reset(bool blocks) {
 
 template <class T>
 Engine<T>::~Engine() {
+  if (stream3_) cudaStreamSynchronize(stream3_);
   if (stream2_) cudaStreamSynchronize(stream2_);
   if (stream_) cudaStreamSynchronize(stream_);
   if (ev_fluid_done_) cudaEventDestroy(ev_fluid_done_);
   if (ev_rigid_done_) cudaEventDestroy(ev_rigid_done_);
   if (ev_rigid_state_) cudaEventDestroy(ev_rigid_state_);
   if (ev_contact_in_) cudaEventDestroy(ev_contact_in_);
+  if (ev_chain_done_) cudaEventDestroy(ev_chain_done_);
   if (stream2_) cudaStreamDestroy(stream2_);
+  if (stream3_) cudaStreamDestroy(stream3_);
   for (auto &e : ev_) if (e) cudaEventDestroy(e);
   for (auto &r : pending_) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
   for (auto &e : pool_) cudaEventDestroy(e);
@@ -533,6 +538,7 @@ template <class T>
 void Engine<T>::body_state_upload(const std::vector<BodyState> &in) {
   if (nb_ == 0) return;
   dev_epoch_++;
+  wait_rigid();  // no rigid kernel may still write the records
   DF_CK(cudaMemcpyAsync(bs_.p, in.data(), nb_ * sizeof(BodyState), cudaMemcpyHostToDevice, stream_));
   sync_all();
 }
@@ -784,6 +790,8 @@ void Engine<T>::rigid_end() {
   if (!fluid_done_recorded_) DF_CK(cudaEventRecord(ev_fluid_done_, stream_));
   fluid_done_recorded_ = false;
   DF_CK(cudaStreamWaitEvent(stream2_, ev_fluid_done_, 0));
+  // k_rigid_step writes whole body records: the previous step's chain (which writes G) first
+  DF_CK(cudaStreamWaitEvent(stream2_, ev_chain_done_, 0));
   pbegin(stream2_);
   int nl = 0;
   if (nchunks_ > 0) {
@@ -796,10 +804,22 @@ void Engine<T>::rigid_end() {
     cs.list = clist_.p;
     if (mgr_blocks) { cs.blk = cblk_.p; cs.Mc = Mc_.p; }
   }
-  k_rigid_step<T><<<nb_, RIGID_THREADS, 0, stream2_>>>(bs_.p, nb_, rc_, manager_ ? nullptr : tape_step, cs, body_chunks_.p,
-                                             red_part_.p, x0d_.p, xd_.p, vd_.p);
+  k_rigid_step<T><<<nb_, RIGID_THREADS, 0, stream2_>>>(bs_.p, nb_, rc_, cs, body_chunks_.p, red_part_.p, x0d_.p,
+                                                        xd_.p, vd_.p);
   nl++;
   DF_CK(cudaEventRecord(ev_rigid_state_, stream2_));
+  if (!manager_ && P_.enable_gradient) {
+    // the per-body chain rule and its tape rows, beside the next step
+    DF_CK(cudaStreamWaitEvent(stream3_, ev_rigid_state_, 0));
+    pend(DFSPH_K_RIGID, nd_, stream2_);
+    pbegin(stream3_);
+    k_rigid_chain<<<nb_, CHAIN_THREADS, 0, stream3_>>>(bs_.p, nb_, rc_, tape_step);
+    launched();
+    pend(DFSPH_K_RIGID, nd_, stream3_);
+    DF_CK(cudaEventRecord(ev_chain_done_, stream3_));
+    chain_pending_ = true;
+    pbegin(stream2_);
+  }
   if (mgr_chain || mgr_blocks) {
     MgrConsts mc{rc_.dt, nb_, rc_.gyroscopic, n_ > 0 ? 1 : 0, contact_ ? 1 : 0, mgr_chain ? 1 : 0};
     if (mgr_chain) {
@@ -942,13 +962,15 @@ int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
   }
   // the error word and the body states come back with the step's final synchronisation
   // (the host mirror of the bodies is then current without another round trip)
-  wait_rigid();
+  // (the per-body chain rule may still run: the mirror's G is refreshed by get_rigid_grad)
+  wait_rigid_except_chain();
   if (nb_ > 0)
     DF_CK(cudaMemcpyAsync(hbs_pin_, bs_.p, nb_ * sizeof(BodyState), cudaMemcpyDeviceToHost, stream_));
   DF_CK(cudaMemcpyAsync(err_host_, err_.p, sizeof(int), cudaMemcpyDeviceToHost, stream_));
-  sync_all();
+  DF_CK(cudaStreamSynchronize(stream_));
   hbs_.assign(hbs_pin_, hbs_pin_ + nb_);
   hbs_epoch_ = dev_epoch_;
+  hbs_chain_stale_ = chain_pending_;
   raise_error_word(*err_host_);
   if (st) {
     st->steps_done = nsteps;
@@ -1012,6 +1034,11 @@ void Engine<T>::get_rigid_mass(int b, double *m, double *I) {
 template <class T>
 void Engine<T>::get_rigid_grad(int b, double *out) {
   if (b < 0 || b >= nb_) throw DfsphException(DFSPH_ERR_INVALID_ARG, "body index");
+  if (hbs_chain_stale_) {  // the mirror was copied while the last step's chain rule could run
+    body_state_download(hbs_);  // (waits for it)
+    hbs_epoch_ = dev_epoch_;
+    hbs_chain_stale_ = false;
+  }
   const double *G = host_body(b).G;
   double *o = out;
   // x_v0 x_w0 q_v0 q_w0 v_v0 v_w0 w_v0 w_w0

@@ -354,7 +354,7 @@ static __global__ void k_visc_boundary_force(FluidConsts<T> c, int nd, const V4<
 constexpr int RED_VALUES = 3 + NJAC + 3;  // force, jacobians, torque
 constexpr int RED_CHUNK = 16;
 constexpr int RED_THREADS = 128;
-constexpr int RIGID_THREADS = 416;  // k_rigid_step: one block per body
+constexpr int RIGID_THREADS = 384;  // k_rigid_step: one block per body (samples updated in one round up to this count)
 static_assert(RED_VALUES <= RED_THREADS, "one thread per reduced value");
 struct RedChunk {
   int body, start, count;
@@ -638,8 +638,7 @@ static __device__ __forceinline__ int block_exclusive_scan(int v, int *warp_tot,
   return before + inc - v;
 }
 
-// One block (128 threads) per body: chain rule -> step matrix A (13x13, appended to the
-// tape), G <- A G; then RigidBody3dBoundarySimulator::velocityTimeStep (forces,
+// One block per body: RigidBody3dBoundarySimulator::velocityTimeStep (forces,
 // gyroscopic torque, gravity; :278-320) and positionTimeStep -> animate (:322-344,
 // Dynamic3dRigidBody.h:113-154, 215-235). With the contact solver the velocity step is
 // gravity, then each force-carrying contact sample's force and torque in sample order, then
@@ -648,17 +647,16 @@ static __device__ __forceinline__ int block_exclusive_scan(int v, int *warp_tot,
 // every gyroscopic addTorque adds (I w) x w (Dynamic3dRigidBody.h:113-142).
 // The body's fluid force, torque and net Jacobians come first: the sums of its chunk
 // partials in chunk order (the second stage of the body reduction); the body's samples are
-// moved last (SimulatorBase::updateBoundaryParticles).
+// moved last (SimulatorBase::updateBoundaryParticles). The state before the velocity step is
+// kept (wpre, qpre, Ipre, Iipre) and chain_ran marks the bodies whose chain rule
+// k_rigid_chain then runs.
 template <class T>
 static __global__ void __launch_bounds__(RIGID_THREADS) k_rigid_step(BodyState *__restrict__ bs, int nbodies, RigidConsts rc,
-                                                    double *__restrict__ tape_step, ContactStep cs,
+                                                    ContactStep cs,
                                                     const int2 *__restrict__ body_chunks,
                                                     const double *__restrict__ red_part,
                                                     const V4<T> *__restrict__ x0d, V4<T> *__restrict__ xd,
                                                     V4<T> *__restrict__ vd) {
-  __shared__ ChainCoef C;
-  __shared__ double A[NSTATE * NSTATE];
-  __shared__ double Gold[NSTATE * 6];
   // the body record is worked on in shared memory (the single-thread parts read it
   // many times) and written back at the end
   __shared__ BodyState sB;
@@ -682,116 +680,8 @@ static __global__ void __launch_bounds__(RIGID_THREADS) k_rigid_step(BodyState *
     else B.T[t - 3 - NJAC] = tot;
   }
   __syncthreads();
-  // FP64 on this part costs about the same per warp instruction whatever the number of
-  // active lanes, and each of the SM's four sub-partitions issues its own warps' FP64 work:
-  // independent single-thread pieces run in separate warps between block barriers, and
-  // lane-parallel work shares a warp:
-  //   phase 1: chain coefficients, part A (warp 0) | velocity update (last warp)
-  //   phase 2: chain coefficients, part B (warps 0-3) | position update (last warp)
-  //   phase 3: the 13 chain columns in the lanes of warp 0
-  // Without the contact solver the velocity and position step does not depend on the chain
-  // rule (which reads the state before it): the last warp computes it into sN and thread 0
-  // takes it over after the chain.
-  __shared__ double sN[31];  // v w x q I Iinv
-  __shared__ double sVb[3];  // Iinv temp_v
-  const int wid = t >> 5, lane = t & 31, nwarps = blockDim.x >> 5;
-  const int et = (nwarps - 1) * 32;  // the thread that runs the velocity and position step
-  const bool early = cs.rec == nullptr && B.dyn && nwarps >= 5;
   const bool chain = B.dyn && !B.anim && rc.enable_gradient && !rc.manager;
   if (t == 0) B.chain_ran = chain ? 1 : 0;
-  // ---- phase 1
-  if (early && t == et) {
-    double *v = sN, *w = sN + 3, *x = sN + 6, *q = sN + 9, *I = sN + 13, *Iinv = sN + 22;
-    for (int k = 0; k < 3; k++) { v[k] = B.v[k]; w[k] = B.w[k]; x[k] = B.x[k]; }
-    for (int k = 0; k < 4; k++) q[k] = B.q[k];
-    for (int k = 0; k < 9; k++) { I[k] = B.I[k]; Iinv[k] = B.Iinv[k]; }
-    if (!B.anim) {
-      const double gm[3] = {rc.gx * B.mass, rc.gy * B.mass, rc.gz * B.mass};
-      body_add_force(v, B.invMass, B.F, rc.dt);
-      body_add_torque(w, I, Iinv, B.T, rc.gyroscopic, rc.dt);
-      body_add_force(v, B.invMass, gm, rc.dt);
-    }
-  }
-  if (chain) {
-    if (t == 0) {
-      q_to_R(B.q, C.R);
-      for (int k = 0; k < 3; k++) C.om[k] = B.w[k];
-      mv3(B.I, C.om, C.Iom);
-      C.invMass = 1.0 / (B.mass + 1e-10);
-      // temp_v (:601, :679, :743)
-      if (rc.gradient_mode != 2) {
-        if (rc.gyroscopic) { double cr[3]; cross3(C.Iom, C.om, cr); for (int k = 0; k < 3; k++) C.temp_v[k] = cr[k] + B.T[k]; }
-        else for (int k = 0; k < 3; k++) C.temp_v[k] = B.T[k];
-      } else {
-        if (rc.gyroscopic) cross3(C.Iom, C.om, C.temp_v);
-        else for (int k = 0; k < 3; k++) C.temp_v[k] = 0.0;
-      }
-      mv3(B.Iinv, C.temp_v, sVb);
-    } else if (wid == 1 && lane < 9) {
-      C.I0[lane] = B.I0[lane]; C.I[lane] = B.I[lane]; C.Iinv[lane] = B.Iinv[lane];
-    }
-    for (int k = t; k < NSTATE * 6; k += blockDim.x) Gold[k] = B.G[k];
-  }
-  __syncthreads();
-  // ---- phase 2
-  if (early && t == et) body_animate(sN + 6, sN + 9, sN + 13, sN + 22, sN, sN + 3, B.I0, rc.dt);
-  if (chain && lane == 0 && wid < 4) {
-    // grad_inertia_v operands: v = omega (a) and v = Iinv temp_v (b)
-    const double RT[9] = {C.R[0], C.R[3], C.R[6], C.R[1], C.R[4], C.R[7], C.R[2], C.R[5], C.R[8]};
-    const double *va = C.om, *vb = sVb;
-    double tmp[3], tmp2[3];
-    if (wid == 0) {
-      mv3(RT, va, tmp); mv3(B.I0, tmp, tmp2); grad_Rqp_d(B.q, tmp2, C.gRq_a);
-    } else if (wid == 1) {
-      grad_RqTp_d(B.q, va, C.gRTq_a); grad_RqTp_d(B.q, vb, C.gRTq_b);
-    } else if (wid == 2) {
-      mv3(RT, vb, tmp); mv3(B.I0, tmp, tmp2); grad_Rqp_d(B.q, tmp2, C.gRq_b);
-    } else {
-      // rotation block (:827-888)
-      double nom[3];
-      for (int k = 0; k < 3; k++) nom[k] = C.om[k] + rc.dt * vb[k];
-      const double p[4] = {0.0, nom[0], nom[1], nom[2]};
-      double pq[4], nq[4];
-      q_mul(p, B.q, pq);
-      for (int k = 0; k < 4; k++) nq[k] = B.q[k] + rc.dt * 0.5 * pq[k];
-      const double nn = sqrt(nq[0] * nq[0] + nq[1] * nq[1] + nq[2] * nq[2] + nq[3] * nq[3]);
-      double nv[4];
-      for (int k = 0; k < 4; k++) nv[k] = nq[k] / nn;
-      for (int i = 0; i < 4; i++)
-        for (int j = 0; j < 4; j++) C.Gn[4 * i + j] = ((i == j ? 1.0 : 0.0) - nv[i] * nv[j]) / nn;
-      const double Gpq[16] = {p[0], -p[1], -p[2], -p[3], p[1], p[0], -p[3], p[2],
-                              p[2], p[3], p[0], -p[1], p[3], -p[2], p[1], p[0]};
-      for (int k = 0; k < 16; k++) C.Gpq[k] = Gpq[k];
-      const double *q = B.q;
-      const double Gpw[12] = {-q[1], -q[2], -q[3], q[0], q[3], -q[2], -q[3], q[0], q[1], q[2], -q[1], q[0]};
-      for (int k = 0; k < 12; k++) C.Gpw[k] = Gpw[k];
-    }
-  }
-  __syncthreads();
-  // ---- phase 3
-  if (chain) {
-    // the columns in the lanes of one warp: an FP64 warp instruction costs the same with 13
-    // active lanes as with one, so more warps would only queue on the FP64 units
-    if (t < NSTATE) {
-      double e[NSTATE], col[NSTATE];
-      for (int k = 0; k < NSTATE; k++) e[k] = (k == t) ? 1.0 : 0.0;
-      chain_column(B, C, rc, e, col);
-      for (int k = 0; k < NSTATE; k++) A[k * NSTATE + t] = col[k];
-    }
-    __syncthreads();
-    for (int k = t; k < NSTATE * 6; k += blockDim.x) {
-      const int r = k / 6, cc = k % 6;
-      double s = 0.0;
-      for (int m = 0; m < NSTATE; m++) s += A[r * NSTATE + m] * Gold[m * 6 + cc];
-      B.G[k] = s;
-    }
-    if (tape_step)
-      for (int k = t; k < NSTATE * NSTATE; k += blockDim.x) tape_step[(size_t)b * NSTATE * NSTATE + k] = A[k];
-    __syncthreads();
-  } else if (tape_step) {
-    for (int k = t; k < NSTATE * NSTATE; k += blockDim.x)
-      tape_step[(size_t)b * NSTATE * NSTATE + k] = (k / NSTATE == k % NSTATE) ? 1.0 : 0.0;
-  }
   // the body's force-carrying contact samples, in sample order
   __shared__ int warp_tot[32];
   __shared__ int s_con, s_act;
@@ -841,11 +731,7 @@ static __global__ void __launch_bounds__(RIGID_THREADS) k_rigid_step(BodyState *
     }
   }
   if (t == 0 && B.dyn) {
-    if (early) {
-      for (int k = 0; k < 3; k++) { B.v[k] = sN[k]; B.w[k] = sN[3 + k]; B.x[k] = sN[6 + k]; B.wmid[k] = sN[3 + k]; }
-      for (int k = 0; k < 4; k++) B.q[k] = sN[9 + k];
-      for (int k = 0; k < 9; k++) { B.I[k] = sN[13 + k]; B.Iinv[k] = sN[22 + k]; }
-    } else {
+    {
       if (cs.rec) {
         const double zero[3] = {0.0, 0.0, 0.0};
         if (!B.anim)
@@ -890,6 +776,130 @@ static __global__ void __launch_bounds__(RIGID_THREADS) k_rigid_step(BodyState *
     unsigned long long *dst = reinterpret_cast<unsigned long long *>(bs + b);
     for (int k = t; k < (int)(sizeof(BodyState) / 8); k += blockDim.x) dst[k] = src[k];
   }
+}
+
+// The chain rule of one step (perform_chain_rule, BoundaryModel_Akinci2012.cpp:543-889) for
+// the bodies k_rigid_step marked (chain_ran), from the state the step started from (wpre,
+// qpre, Ipre, Iipre) and its reduced net force and torque blocks: the step map A of the
+// body's 13 states goes to the tape, G = A G. It runs on its own stream after k_rigid_step:
+// the bodies' new states do not wait for it, and it writes only G and the tape. Other
+// bodies get an identity tape block.
+// FP64 on this part costs about the same per warp instruction whatever the number of
+// active lanes, and each of the SM's four sub-partitions issues its own warps' FP64 work:
+// independent single-thread pieces run in separate warps between block barriers, and
+// lane-parallel work shares a warp:
+//   phase 1: coefficients, part A (warp 0)
+//   phase 2: coefficients, part B (warps 0-3)
+//   phase 3: the 13 columns in the lanes of warp 0
+constexpr int CHAIN_THREADS = 128;
+static __global__ void __launch_bounds__(CHAIN_THREADS) k_rigid_chain(BodyState *__restrict__ bs, int nbodies,
+                                                                      RigidConsts rc, double *__restrict__ tape_step) {
+  __shared__ ChainCoef C;
+  __shared__ double A[NSTATE * NSTATE];
+  __shared__ double Gold[NSTATE * 6];
+  __shared__ BodyState sB;
+  static_assert(sizeof(BodyState) % 8 == 0, "BodyState copies as 8-byte words");
+  const int b = blockIdx.x;
+  if (b >= nbodies) return;
+  const int t = threadIdx.x;
+  {
+    const unsigned long long *src = reinterpret_cast<const unsigned long long *>(bs + b);
+    unsigned long long *dst = reinterpret_cast<unsigned long long *>(&sB);
+    for (int k = t; k < (int)(sizeof(BodyState) / 8); k += blockDim.x) dst[k] = src[k];
+  }
+  __syncthreads();
+  BodyState &B = sB;
+  if (!B.chain_ran) {
+    if (tape_step)
+      for (int k = t; k < NSTATE * NSTATE; k += blockDim.x)
+        tape_step[(size_t)b * NSTATE * NSTATE + k] = (k / NSTATE == k % NSTATE) ? 1.0 : 0.0;
+    return;
+  }
+  // the state the step started from
+  if (t < 9) { B.I[t] = B.Ipre[t]; B.Iinv[t] = B.Iipre[t]; }
+  if (t < 4) B.q[t] = B.qpre[t];
+  if (t < 3) B.w[t] = B.wpre[t];
+  __syncthreads();
+  __shared__ double sVb[3];  // Iinv temp_v
+  const int wid = t >> 5, lane = t & 31;
+  // ---- phase 1
+  {
+    if (t == 0) {
+      q_to_R(B.q, C.R);
+      for (int k = 0; k < 3; k++) C.om[k] = B.w[k];
+      mv3(B.I, C.om, C.Iom);
+      C.invMass = 1.0 / (B.mass + 1e-10);
+      // temp_v (:601, :679, :743)
+      if (rc.gradient_mode != 2) {
+        if (rc.gyroscopic) { double cr[3]; cross3(C.Iom, C.om, cr); for (int k = 0; k < 3; k++) C.temp_v[k] = cr[k] + B.T[k]; }
+        else for (int k = 0; k < 3; k++) C.temp_v[k] = B.T[k];
+      } else {
+        if (rc.gyroscopic) cross3(C.Iom, C.om, C.temp_v);
+        else for (int k = 0; k < 3; k++) C.temp_v[k] = 0.0;
+      }
+      mv3(B.Iinv, C.temp_v, sVb);
+    } else if (wid == 1 && lane < 9) {
+      C.I0[lane] = B.I0[lane]; C.I[lane] = B.I[lane]; C.Iinv[lane] = B.Iinv[lane];
+    }
+    for (int k = t; k < NSTATE * 6; k += blockDim.x) Gold[k] = B.G[k];
+  }
+  __syncthreads();
+  // ---- phase 2
+  if (lane == 0 && wid < 4) {
+    // grad_inertia_v operands: v = omega (a) and v = Iinv temp_v (b)
+    const double RT[9] = {C.R[0], C.R[3], C.R[6], C.R[1], C.R[4], C.R[7], C.R[2], C.R[5], C.R[8]};
+    const double *va = C.om, *vb = sVb;
+    double tmp[3], tmp2[3];
+    if (wid == 0) {
+      mv3(RT, va, tmp); mv3(B.I0, tmp, tmp2); grad_Rqp_d(B.q, tmp2, C.gRq_a);
+    } else if (wid == 1) {
+      grad_RqTp_d(B.q, va, C.gRTq_a); grad_RqTp_d(B.q, vb, C.gRTq_b);
+    } else if (wid == 2) {
+      mv3(RT, vb, tmp); mv3(B.I0, tmp, tmp2); grad_Rqp_d(B.q, tmp2, C.gRq_b);
+    } else {
+      // rotation block (:827-888)
+      double nom[3];
+      for (int k = 0; k < 3; k++) nom[k] = C.om[k] + rc.dt * vb[k];
+      const double p[4] = {0.0, nom[0], nom[1], nom[2]};
+      double pq[4], nq[4];
+      q_mul(p, B.q, pq);
+      for (int k = 0; k < 4; k++) nq[k] = B.q[k] + rc.dt * 0.5 * pq[k];
+      const double nn = sqrt(nq[0] * nq[0] + nq[1] * nq[1] + nq[2] * nq[2] + nq[3] * nq[3]);
+      double nv[4];
+      for (int k = 0; k < 4; k++) nv[k] = nq[k] / nn;
+      for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) C.Gn[4 * i + j] = ((i == j ? 1.0 : 0.0) - nv[i] * nv[j]) / nn;
+      const double Gpq[16] = {p[0], -p[1], -p[2], -p[3], p[1], p[0], -p[3], p[2],
+                              p[2], p[3], p[0], -p[1], p[3], -p[2], p[1], p[0]};
+      for (int k = 0; k < 16; k++) C.Gpq[k] = Gpq[k];
+      const double *q = B.q;
+      const double Gpw[12] = {-q[1], -q[2], -q[3], q[0], q[3], -q[2], -q[3], q[0], q[1], q[2], -q[1], q[0]};
+      for (int k = 0; k < 12; k++) C.Gpw[k] = Gpw[k];
+    }
+  }
+  __syncthreads();
+  // ---- phase 3
+  {
+    // the columns in the lanes of one warp: an FP64 warp instruction costs the same with 13
+    // active lanes as with one, so more warps would only queue on the FP64 units
+    if (t < NSTATE) {
+      double e[NSTATE], col[NSTATE];
+      for (int k = 0; k < NSTATE; k++) e[k] = (k == t) ? 1.0 : 0.0;
+      chain_column(B, C, rc, e, col);
+      for (int k = 0; k < NSTATE; k++) A[k * NSTATE + t] = col[k];
+    }
+    __syncthreads();
+    for (int k = t; k < NSTATE * 6; k += blockDim.x) {
+      const int r = k / 6, cc = k % 6;
+      double s = 0.0;
+      for (int m = 0; m < NSTATE; m++) s += A[r * NSTATE + m] * Gold[m * 6 + cc];
+      B.G[k] = s;
+    }
+    if (tape_step)
+      for (int k = t; k < NSTATE * NSTATE; k += blockDim.x) tape_step[(size_t)b * NSTATE * NSTATE + k] = A[k];
+    __syncthreads();
+  }
+  for (int k = t; k < NSTATE * 6; k += blockDim.x) bs[b].G[k] = B.G[k];
 }
 
 // TimeStepDiffDFSPH::beginStep velocity overrides (:379-429), decided on the host.
