@@ -464,6 +464,9 @@ static __device__ __forceinline__ void for_neighbors_sub(int cnt, const int *__r
 #ifndef DFSPH_DENSITY_MIN_BLOCKS
 #define DFSPH_DENSITY_MIN_BLOCKS 6
 #endif
+#ifndef DFSPH_DENSITY_XS_MIN_BLOCKS
+#define DFSPH_DENSITY_XS_MIN_BLOCKS 5
+#endif
 #ifndef DFSPH_VELOCITY_MIN_BLOCKS
 #define DFSPH_VELOCITY_MIN_BLOCKS 4
 #endif
@@ -487,7 +490,7 @@ template <class T> static __device__ __forceinline__ T sub_sum(T v) {
 // records go to R_out. Once the divergence solve's last check passes, R_out holds the
 // state the separate XSPH pass would have produced.
 template <class T, int MODE, bool XS = false>
-static __global__ void __launch_bounds__(256, DFSPH_DENSITY_MIN_BLOCKS) k_density_pass(
+static __global__ void __launch_bounds__(256, XS ? DFSPH_DENSITY_XS_MIN_BLOCKS : DFSPH_DENSITY_MIN_BLOCKS) k_density_pass(
     FluidConsts<T> c, const Rec<T> *__restrict__ R, V4<T> *__restrict__ Q, const Rec<T> *__restrict__ BR,
     const int *__restrict__ flist, const int *__restrict__ fcount, const int *__restrict__ blist,
     const int *__restrict__ bcount, const T *__restrict__ rho, const T *__restrict__ alpha, T *__restrict__ rhoAdv,
