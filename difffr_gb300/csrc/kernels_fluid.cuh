@@ -468,7 +468,7 @@ static __device__ __forceinline__ void for_neighbors_sub(int cnt, const int *__r
 #define DFSPH_DENSITY_XS_MIN_BLOCKS 5
 #endif
 #ifndef DFSPH_VELOCITY_MIN_BLOCKS
-#define DFSPH_VELOCITY_MIN_BLOCKS 4
+#define DFSPH_VELOCITY_MIN_BLOCKS 5
 #endif
 #ifndef DFSPH_XSPH_MIN_BLOCKS
 #define DFSPH_XSPH_MIN_BLOCKS 4
