@@ -227,7 +227,7 @@ static __device__ __forceinline__ void for_each_row(const Grid<T> &g, const int 
 // PASS_DIVERGENCE_WARM, :1698-1788 with :1977-2041): the density change over the same
 // neighbours in the same order, rho_dot = 0 below 20 neighbours, kappaV = 0.5 max(kappaV,
 // -0.5) / h where rho_dot > 0, and Q[i] = (x_i, kappaV) for the warm-start correction.
-constexpr int LIST_THREADS = 256;
+constexpr int LIST_THREADS = 128;
 template <class T, bool DIVWARM>
 static __global__ void __launch_bounds__(LIST_THREADS) k_lists_density_factor(
     FluidConsts<T> c, Rec<T> *__restrict__ R, const int *__restrict__ cstartF,
