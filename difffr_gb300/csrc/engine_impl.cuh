@@ -262,7 +262,7 @@ Engine<T>::Engine(const dfsph_scene *sc) {
   cstartF_.alloc((size_t)ncell_ + 1);
   cstartS_.alloc((size_t)ncell_ + 1);
   cstartD_.alloc((size_t)ncell_ + 1);
-  partials_.alloc((size_t)blocks(std::max(n_, 1) * LPP));
+  partials_.alloc((size_t)blocks(std::max(n_, 1) * LPP, PASS_THREADS));
   resid_.alloc(4);
   err_.alloc(1);
   DF_CK(cudaHostAlloc((void **)&resid_host_, 4 * sizeof(double), cudaHostAllocMapped));
@@ -647,11 +647,11 @@ void Engine<T>::raise_error_word(int e) {
 
 template <class T>
 void Engine<T>::launch_density(int mode, T *kappa_io, bool partials, float4 *feat) {
-  const int nbk = blocks(n_ * LPP);
+  const int nbk = blocks(n_ * LPP, PASS_THREADS);
   double *pp = partials ? partials_.p : nullptr;
   pbegin();
 #define DF_DENS(M, XS)                                                                                             \
-  k_density_pass<T, M, XS><<<nbk, 256, 0, stream_>>>(fc_, R_[cur_].p, Q_.p, BR_.p, flist_.p, fcount_.p, blist_.p,       \
+  k_density_pass<T, M, XS><<<nbk, PASS_THREADS, 0, stream_>>>(fc_, R_[cur_].p, Q_.p, BR_.p, flist_.p, fcount_.p, blist_.p,       \
                                                      bcount_.p, rho_.p, alpha_.p, rhoAdv_.p, kappa_io, pp, feat,      \
                                                      R_[1 - cur_].p)
   // the divergence solve's checked passes also advance the XSPH phase (see k_density_pass)
@@ -672,13 +672,13 @@ void Engine<T>::launch_density(int mode, T *kappa_io, bool partials, float4 *fea
 
 template <class T>
 void Engine<T>::launch_velocity(T *kappa_acc) {
-  const int nbk = blocks(n_ * LPP);
+  const int nbk = blocks(n_ * LPP, PASS_THREADS);
   pbegin();
   if (kappa_acc)
-    k_velocity_pass<T, 1><<<nbk, 256, 0, stream_>>>(fc_, Q_.p, R_[cur_].p, BR_.p, flist_.p, fcount_.p, blist_.p,
+    k_velocity_pass<T, 1><<<nbk, PASS_THREADS, 0, stream_>>>(fc_, Q_.p, R_[cur_].p, BR_.p, flist_.p, fcount_.p, blist_.p,
                                                     bcount_.p, kappa_acc);
   else
-    k_velocity_pass<T, 0><<<nbk, 256, 0, stream_>>>(fc_, Q_.p, R_[cur_].p, BR_.p, flist_.p, fcount_.p, blist_.p,
+    k_velocity_pass<T, 0><<<nbk, PASS_THREADS, 0, stream_>>>(fc_, Q_.p, R_[cur_].p, BR_.p, flist_.p, fcount_.p, blist_.p,
                                                     bcount_.p, nullptr);
   launched();
   pend(DFSPH_K_VELOCITY_PASS, n_);
@@ -734,7 +734,7 @@ void Engine<T>::solve_impl(bool pressure) {
                          : (T(1) / fc_.dt) * (T)P_.max_error_v * T(0.01) * fc_.rho0;
   const int minIt = pressure ? P_.min_iterations : 1;
   const int maxIt = pressure ? P_.max_iterations : P_.max_iterations_v;
-  const int nbk = blocks(n_ * LPP);
+  const int nbk = blocks(n_ * LPP, PASS_THREADS);
   while ((!chk || it < minIt) && it < maxIt) {
     launch_pairs(pressure, false, P_.enable_gradient != 0);
     launch_velocity(warm ? kap : nullptr);

@@ -461,6 +461,12 @@ static __device__ __forceinline__ void for_neighbors_sub(int cnt, const int *__r
 #ifndef DFSPH_XSPH_BATCH
 #define DFSPH_XSPH_BATCH 4
 #endif
+// Threads per block of the density and velocity passes; the minimum resident blocks below
+// are given for 256 threads and scaled, so that the register budget stays the same.
+#ifndef DFSPH_PASS_THREADS
+#define DFSPH_PASS_THREADS 128
+#endif
+constexpr int PASS_THREADS = DFSPH_PASS_THREADS;
 #ifndef DFSPH_DENSITY_MIN_BLOCKS
 #define DFSPH_DENSITY_MIN_BLOCKS 6
 #endif
@@ -490,7 +496,7 @@ template <class T> static __device__ __forceinline__ T sub_sum(T v) {
 // records go to R_out. Once the divergence solve's last check passes, R_out holds the
 // state the separate XSPH pass would have produced.
 template <class T, int MODE, bool XS = false>
-static __global__ void __launch_bounds__(256, XS ? DFSPH_DENSITY_XS_MIN_BLOCKS : DFSPH_DENSITY_MIN_BLOCKS) k_density_pass(
+static __global__ void __launch_bounds__(PASS_THREADS, (XS ? DFSPH_DENSITY_XS_MIN_BLOCKS : DFSPH_DENSITY_MIN_BLOCKS) * 256 / PASS_THREADS) k_density_pass(
     FluidConsts<T> c, const Rec<T> *__restrict__ R, V4<T> *__restrict__ Q, const Rec<T> *__restrict__ BR,
     const int *__restrict__ flist, const int *__restrict__ fcount, const int *__restrict__ blist,
     const int *__restrict__ bcount, const T *__restrict__ rho, const T *__restrict__ alpha, T *__restrict__ rhoAdv,
@@ -574,7 +580,7 @@ static __global__ void __launch_bounds__(256, XS ? DFSPH_DENSITY_XS_MIN_BLOCKS :
 // v_i += -dt k_i (-psi grad W) over boundary neighbours [if |k_i| > eps].
 // ACC = 1 adds k_i to kappa_acc (the solver's running stiffness). v[i].w is kept.
 template <class T, int ACC>
-static __global__ void __launch_bounds__(256, DFSPH_VELOCITY_MIN_BLOCKS) k_velocity_pass(
+static __global__ void __launch_bounds__(PASS_THREADS, DFSPH_VELOCITY_MIN_BLOCKS * 256 / PASS_THREADS) k_velocity_pass(
     FluidConsts<T> c, const V4<T> *__restrict__ Q, Rec<T> *__restrict__ R, const Rec<T> *__restrict__ BR,
     const int *__restrict__ flist, const int *__restrict__ fcount, const int *__restrict__ blist,
     const int *__restrict__ bcount, T *__restrict__ kappa_acc) {
