@@ -892,7 +892,7 @@ int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
       }
       if (nd_) {
         pbegin();
-        k_bf_lists<T><<<blocks(nd_), 256, 0, stream_>>>(fc_, nd_, xd_.p, R_[cur_].p, cstartF_.p, kbf_, bflist_.p,
+        k_bf_lists<T><<<blocks(nd_ * 32, 128), 128, 0, stream_>>>(fc_, nd_, xd_.p, R_[cur_].p, cstartF_.p, kbf_, bflist_.p,
                                                         bfcount_.p, err_.p);
         launched();
         pend(DFSPH_K_BF_LISTS, nd_);

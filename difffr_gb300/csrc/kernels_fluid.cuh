@@ -339,29 +339,78 @@ static __global__ void __launch_bounds__(LIST_THREADS) k_lists_density_factor(
   }
 }
 
-// Fluid neighbours of each dynamic boundary sample (body order).
+// Fluid neighbours of each dynamic boundary sample (body order), one warp per sample. The
+// candidates of the 9 cell rows are numbered in row order; lanes 0-8 read the rows' bounds
+// together, then the lanes test 32 consecutive candidate numbers at a time, across row
+// ends, and append the accepted ones in candidate order (ballot and prefix count): the
+// list a serial scan of the rows in order makes.
 template <class T>
 static __global__ void k_bf_lists(FluidConsts<T> c, int nd, const V4<T> *__restrict__ xd, const Rec<T> *__restrict__ R,
                            const int *__restrict__ cstartF, int kbf, int *__restrict__ bflist,
                            int *__restrict__ bfcount, int *__restrict__ err) {
-  const int d = blockIdx.x * blockDim.x + threadIdx.x;
-  if (d >= nd) return;
+  const int d = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (d >= nd) return;  // whole warps
   const V4<T> xj = xd[d];
   int cx, cy, cz;
   grid_cell(c.grid, xj.x, xj.y, xj.z, cx, cy, cz);
+  // row r = 3 (dz + 1) + (dy + 1): [rb, re) of the cells x-1..x+1 (empty outside the grid)
+  int rb = 0, re = 0;
+  if (lane < 9) {
+    const int z = cz + lane / 3 - 1, y = cy + lane % 3 - 1;
+    if (z >= 0 && z < c.grid.nz && y >= 0 && y < c.grid.ny) {
+      const int x0 = cx > 0 ? cx - 1 : 0, x1 = cx < c.grid.nx - 1 ? cx + 1 : c.grid.nx - 1;
+      const int base = (z * c.grid.ny + y) * c.grid.nx;
+      rb = cstartF[base + x0];
+      re = cstartF[base + x1 + 1];
+    }
+  }
+  // exclusive prefix of the row lengths over lanes 0-8
+  const int len = re - rb;
+  int incl = len;
+#pragma unroll
+  for (int o = 1; o < 16; o <<= 1) {
+    const int u = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += u;
+  }
+  const int total = __shfl_sync(0xffffffffu, incl, 8);
+  int rowb[9], rowoff[9];
+#pragma unroll
+  for (int r = 0; r < 9; r++) {
+    rowb[r] = __shfl_sync(0xffffffffu, rb, r);
+    rowoff[r] = __shfl_sync(0xffffffffu, incl - len, r);
+  }
   int cnt = 0;
-  for_each_row(c.grid, cstartF, cx, cy, cz, [&](int b, int e) {
-    for (int i = b; i < e; i++) {
+  for (int c0 = 0; c0 < total; c0 += 32) {
+    const int q = c0 + lane;
+    bool acc = false;
+    int i = 0;
+    if (q < total) {
+      int r = 0;
+#pragma unroll
+      for (int k = 1; k < 9; k++)
+        if (q >= rowoff[k]) r = k;
+      // rows are numbered in order and empty rows share their successor's offset
+      int bb = rowb[0], oo = rowoff[0];
+#pragma unroll
+      for (int k = 1; k < 9; k++)
+        if (k == r) { bb = rowb[k]; oo = rowoff[k]; }
+      i = bb + (q - oo);
       const V4<T> xi = R[i].x;
       const T dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
-      if (dist2_rn(dx, dy, dz) < c.h2) {
-        if (cnt < kbf) bflist[(size_t)cnt * nd + d] = i;
-        cnt++;
-      }
+      acc = dist2_rn(dx, dy, dz) < c.h2;
     }
-  });
-  if (cnt > kbf) { atomicOr(err, ERR_BF_LIST_OVERFLOW); cnt = kbf; }
-  bfcount[d] = cnt;
+    const unsigned m = __ballot_sync(0xffffffffu, acc);
+    if (acc) {
+      const int k = cnt + __popc(m & ((1u << lane) - 1u));
+      if (k < kbf) bflist[(size_t)k * nd + d] = i;
+    }
+    cnt += __popc(m);
+  }
+  if (lane == 0) {
+    if (cnt > kbf) { atomicOr(err, ERR_BF_LIST_OVERFLOW); cnt = kbf; }
+    bfcount[d] = cnt;
+  }
 }
 
 // psi of every boundary sample: 1 / (W0 + sum_k W over boundary neighbours of any body)
