@@ -8,7 +8,8 @@
  *  - Every function returns an int status: DFSPH_OK (0) or a positive error
  *    code. No C++ exception crosses this boundary. dfsph_last_error() gives a
  *    human-readable message for the last failing call on the calling thread.
- *  - A context owns all device memory and one CUDA stream. Calls on one
+ *  - A context owns all device memory and its CUDA streams (the fluid stream,
+ *    the rigid-body stream and the per-body chain-rule stream). Calls on one
  *    context are not thread-safe; distinct contexts are independent.
  *  - Host buffers are owned by the caller. Positions and velocities cross the
  *    boundary as row-major double[n][3] in the caller's (original) particle
@@ -207,7 +208,10 @@ int dfsph_reset(dfsph_ctx *ctx);
    (SimulatorBase.cpp:999-1016): TimeStepDiffDFSPH::step (TimeStepDiffDFSPH.cpp:526-652)
    followed by RigidBody3dBoundarySimulator::velocityTimeStep and positionTimeStep
    (RigidBody3dBoundarySimulator.cpp:278-344). stats may be NULL. Returns
-   DFSPH_ERR_NOT_CONVERGED (state valid) if a solve hit its iteration cap. */
+   DFSPH_ERR_NOT_CONVERGED (state valid) if a solve hit its iteration cap.
+   Returns once the fluid and the bodies are updated; the last step's per-body chain
+   rule may still run on the device, and every call that reads it (dfsph_get_rigid_grad,
+   dfsph_backward, dfsph_adjoint_sweep, checkpoints, dfsph_synchronize) waits for it. */
 int dfsph_step(dfsph_ctx *ctx, int32_t nsteps, dfsph_step_stats *stats);
 
 /* Replaces TimeStepDiffDFSPH::set_init_v_rb / set_init_omega_rb
@@ -326,7 +330,7 @@ int dfsph_checkpoint_free(dfsph_ctx *ctx, int32_t slot);
    omega0 sweep. */
 int dfsph_adjoint_sweep(dfsph_ctx *ctx, const double *lam_in, double *lam_out);
 
-/* Synchronises the context's stream (for timing from the caller). */
+/* Synchronises all of the context's streams (for timing from the caller). */
 int dfsph_synchronize(dfsph_ctx *ctx);
 
 /* Kernel launches issued by this context since creation (for launch accounting). */
@@ -334,8 +338,10 @@ int dfsph_launch_count(dfsph_ctx *ctx, int64_t *count);
 
 /* Timing on the context's stream (no reference counterpart; the reference times with
    host clocks, Utilities/Timing.h:22-37). dfsph_record_event records CUDA event `slot`
-   (0..7) on the stream; dfsph_event_elapsed gives milliseconds between two recorded
-   slots (synchronises on the second). */
+   (0..7) on the fluid stream, which has joined the rigid-body stream at the end of each
+   dfsph_step call and joins the chain-rule stream at the calls listed under dfsph_step;
+   dfsph_event_elapsed gives milliseconds between two recorded slots (synchronises on the
+   second). */
 int dfsph_record_event(dfsph_ctx *ctx, int32_t slot);
 int dfsph_event_elapsed(dfsph_ctx *ctx, int32_t slot_a, int32_t slot_b, double *ms);
 
