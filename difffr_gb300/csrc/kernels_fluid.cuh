@@ -228,6 +228,9 @@ static __device__ __forceinline__ void for_each_row(const Grid<T> &g, const int 
 // neighbours in the same order, rho_dot = 0 below 20 neighbours, kappaV = 0.5 max(kappaV,
 // -0.5) / h where rho_dot > 0, and Q[i] = (x_i, kappaV) for the warm-start correction.
 constexpr int LIST_THREADS = 128;
+#ifndef DFSPH_LIST_SCAN_BATCH
+#define DFSPH_LIST_SCAN_BATCH 4  // candidate loads in flight per lane in the list build's scan
+#endif
 template <class T, bool DIVWARM>
 static __global__ void __launch_bounds__(LIST_THREADS) k_lists_density_factor(
     FluidConsts<T> c, Rec<T> *__restrict__ R, const int *__restrict__ cstartF,
@@ -251,13 +254,13 @@ static __global__ void __launch_bounds__(LIST_THREADS) k_lists_density_factor(
   // then the lane walks its own list in order. Same neighbours, same order, same formulas.
   int cnt = 0;
   for_each_row(c.grid, cstartF, cx, cy, cz, [&](int b, int e) {
-    for (int j0 = b; j0 < e; j0 += 4) {
-      V4<T> xs[4];
+    for (int j0 = b; j0 < e; j0 += DFSPH_LIST_SCAN_BATCH) {
+      V4<T> xs[DFSPH_LIST_SCAN_BATCH];
 #pragma unroll
-      for (int u = 0; u < 4; u++)
+      for (int u = 0; u < DFSPH_LIST_SCAN_BATCH; u++)
         if (j0 + u < e) xs[u] = R[j0 + u].x;
 #pragma unroll
-      for (int u = 0; u < 4; u++) {
+      for (int u = 0; u < DFSPH_LIST_SCAN_BATCH; u++) {
         const int j = j0 + u;
         if (j >= e || j == i) continue;
         const T dx = xi.x - xs[u].x, dy = xi.y - xs[u].y, dz = xi.z - xs[u].z;
