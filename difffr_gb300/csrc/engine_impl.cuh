@@ -687,12 +687,12 @@ void Engine<T>::launch_velocity(T *kappa_acc) {
 template <class T>
 void Engine<T>::launch_pairs(bool pressure, bool warm, bool grad) {
   if (nd_ == 0) return;
-  const int ndw = blocks(nd_ * 32, 128);
+  const int ndw = blocks(nd_ * 32, PAIR_THREADS);
   PairConsts<T> pc = pressure ? pcP_ : pcD_;
   pc.grad = (grad && !warm) ? 1 : 0;
   pbegin();
 #define DF_PAIRS(M)                                                                                                \
-  k_pairs<T, M><<<ndw, 128, 0, stream_>>>(fc_, pc, nd_, xd_.p, vd_.p, x0d_.p, bodyd_.p, bs_.p, bflist_.p, bfcount_.p, \
+  k_pairs<T, M><<<ndw, PAIR_THREADS, 0, stream_>>>(fc_, pc, nd_, xd_.p, vd_.p, x0d_.p, bodyd_.p, bs_.p, bflist_.p, bfcount_.p, \
                                           Q_.p, R_[cur_].p, alpha_.p, rhoAdv_.p, sumgrad_.p, acc_.p)
   if (pressure) DF_PAIRS(0);
   else DF_PAIRS(1);

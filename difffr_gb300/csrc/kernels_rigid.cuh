@@ -133,8 +133,12 @@ struct PairConsts {
 // The Jacobian switch is a launch constant, not a template parameter: one compiled body
 // serves both, so the force sums (and hence the forward trajectory) are bit-identical
 // whether or not gradients are recorded.
+#ifndef DFSPH_PAIR_THREADS
+#define DFSPH_PAIR_THREADS 128
+#endif
+constexpr int PAIR_THREADS = DFSPH_PAIR_THREADS;  // k_pairs: one warp per dynamic sample
 template <class T, int MODE>
-static __global__ void __launch_bounds__(128) k_pairs(FluidConsts<T> c, PairConsts<T> pc, int nd,
+static __global__ void __launch_bounds__(PAIR_THREADS) k_pairs(FluidConsts<T> c, PairConsts<T> pc, int nd,
                                                const V4<T> *__restrict__ xd, const V4<T> *__restrict__ vd,
                                                const V4<T> *__restrict__ x0d, const int *__restrict__ bodyd,
                                                const BodyState *__restrict__ bs, const int *__restrict__ bflist,
@@ -264,7 +268,7 @@ static __global__ void __launch_bounds__(128) k_pairs(FluidConsts<T> c, PairCons
   // lanes add them into the FP64 row together (an FP64 warp instruction costs about the same
   // for one active lane as for 32)
   static_assert(ACC_FORCE == 0 && ACC_JAC == 3, "row layout: force, then the Jacobian terms");
-  __shared__ T wsum[128 / 32][3 + NJAC];
+  __shared__ T wsum[PAIR_THREADS / 32][3 + NJAC];
   T *ws = wsum[threadIdx.x >> 5];
 #pragma unroll
   for (int k = 0; k < 3; k++) {
