@@ -206,39 +206,100 @@ def allmax(pg, v):
     return float(t.item())
 
 
-def cpu_baseline(args, steps, warmup, threads):
-    """The CPU oracle (C++/OpenMP restatement of the reference step) on this host's cores."""
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the machine type)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.machine()
+
+
+def config_dict(args, sc):
+    """The workload description both arms print (same keys, same values)."""
+    return {"workload": args.config_name, "n_fluid": sc.n_fluid, "n_boundary": sc.n_boundary,
+            "dt": sc.params.time_step, "gradient_mode": "incomplete",
+            "window": f"steps {args.start_step + args.warmup}-{args.start_step + args.warmup + args.steps - 1} "
+                      f"of the trajectory (collapse phase), after {args.warmup} warm-up steps from step "
+                      f"{args.start_step}",
+            "l2": "inputs larger than L2", "parallelism": f"replicas{args.gpus}" if args.gpus > 1 else "single GPU"}
+
+
+def oracle_steps(o, steps):
+    """Times `steps` oracle steps; returns (steps/s, seconds, pressure sweeps per step)."""
+    t0 = time.perf_counter()
+    st = o.step(steps)
+    dt = time.perf_counter() - t0
+    return steps / dt, dt, st["total_pressure_iterations"] / steps
+
+
+def cpu_baseline(args, sim, steps, threads):
+    """The CPU oracle (C++/OpenMP restatement of the reference step) on this host's cores,
+    continuing from the GPU context's current state (fluid fields, warm-start stiffness,
+    bodies, time), so that it times the same phase of the trajectory."""
     import oracle
     oracle.build()
     sc = make_scene(args, enable_gradient=1)
     o = oracle.Oracle(sc, mode=oracle.MODE_MIXED, threads=threads)
-    for _ in range(warmup):
-        o.step(1)
-    t0 = time.perf_counter()
-    o.step(steps)
-    dt = time.perf_counter() - t0
-    return steps / dt, dt
+    o.load_state(sim)
+    o.step(1)
+    return oracle_steps(o, steps)
 
 
 def run_reference(args):
+    """The reference arm: the oracle port on all host cores, run from step 0 through the same
+    pre-roll as the GPU arm (untimed), then `warmup` untimed and `steps` timed steps."""
     world, rank, local, pg = dist_setup()
     if rank != 0:
         return 0
+    import oracle
+    oracle.build()
     threads = os.cpu_count() or 1
+    sc = make_scene(args, enable_gradient=1)
+    o = oracle.Oracle(sc, mode=oracle.MODE_MIXED, threads=threads)
+    if args.start_step > 0:
+        o.step(args.start_step)
+    o.step(args.warmup)
     steps = args.steps
-    val, dt = cpu_baseline(args, steps, args.warmup, threads)
-    sample = (f"{steps} timed steps after {args.warmup} warm-up steps of the full {args.config_name} workload "
-              f"(oracle port, FP32 fluid / FP64 rigid, gradient on)")
+    val, dt, ip = oracle_steps(o, steps)
+    sample = (f"{steps} timed steps (steps {args.start_step + args.warmup}-{args.start_step + args.warmup + steps - 1}, "
+              f"{ip:.2f} pressure sweeps per step) of the full {args.config_name} workload after an untimed "
+              f"pre-roll from step 0; oracle port, FP32 fluid / FP64 rigid, gradient on, {threads} OpenMP threads "
+              f"on {cpu_model()}")
     line = {
         "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * dt / steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lattice + sampled boundaries)",
-        "config": {"workload": args.config_name},
-        "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "config": config_dict(args, sc),
+        "pressure_iterations_per_step": ip,
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                         "cpu_model": cpu_model()},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def timed_fwd_adjoint(sim, steps, dL):
+    """K forward steps with the pair Jacobians recorded, then the reverse sweep once; CUDA
+    events on the context's stream. Returns (ms, step stats)."""
+    sim.synchronize()
+    sim.record_event(0)
+    st = sim.step(steps)
+    sim.backward(dL)
+    sim.record_event(1)
+    return sim.event_elapsed_ms(0, 1), st
 
 
 def run_ours(args):
@@ -253,7 +314,23 @@ def run_ours(args):
     sc = make_scene(args, enable_gradient=1, seed=rank)
     sim = DiffDFSPH(sc)
     nb = sim.n_bodies
-    # ---- warm-up
+    dL = np.zeros((nb, 13))
+    dL[:, 0:3] = 1.0
+
+    # ---- early phase (steps W..W+K-1 from rest: both solves at their minimum sweep counts)
+    for _ in range(args.warmup):
+        sim.step(1)
+    sim.reset_gradient()
+    early_ms, early_st = timed_fwd_adjoint(sim, args.steps, dL)
+    early_ms = allmax(pg, early_ms)
+
+    # ---- untimed pre-roll to the start of the headline window, kept as a device checkpoint
+    t_now, sc_now = sim.time()
+    if args.start_step > sc_now:
+        sim.step(args.start_step - sc_now)
+    slot = sim.checkpoint_save()
+
+    # ---- headline: forward + adjoint over the window (collapse phase)
     for _ in range(args.warmup):
         sim.step(1)
     sim.reset_gradient()
@@ -263,13 +340,7 @@ def run_ours(args):
     l0 = sim.launch_count()
     sim.synchronize()
     barrier(pg)
-    sim.record_event(0)
-    st = sim.step(args.steps)
-    dL = np.zeros((nb, 13))
-    dL[:, 0:3] = 1.0
-    grad = sim.backward(dL)
-    sim.record_event(1)
-    ms = sim.event_elapsed_ms(0, 1)
+    ms, st = timed_fwd_adjoint(sim, args.steps, dL)
     launches = sim.launch_count() - l0
     clk = clocks.stop()
     ms_max = allmax(pg, ms)
@@ -277,7 +348,7 @@ def run_ours(args):
     iters_p = st["total_pressure_iterations"] / args.steps
     iters_v = st["total_divergence_iterations"] / args.steps
 
-    # ---- per-kernel device times over the same number of steps (profiling on)
+    # ---- per-kernel device times over the next K steps of the same phase (profiling on)
     sim.profile_enable(True)
     sim.step(args.steps)
     prof = sim.profile()
@@ -305,40 +376,59 @@ def run_ours(args):
               "achieved": l1_achieved, "peak": l1_peak, "unit": "GB/s", "frac": l1_achieved / l1_peak,
               "peak_basis": "128 B per clock per SM at the maximum SM clock"}
 
-    # ---- forward-only steps/s (no pair Jacobians, no tape)
-    sim_f = DiffDFSPH(make_scene(args, enable_gradient=0, seed=rank))
+    # ---- forward-only steps/s over the same window (no pair Jacobians, no tape)
+    sim.checkpoint_restore(slot)
+    sim.set_gradient_enabled(False)
     for _ in range(args.warmup):
-        sim_f.step(1)
-    sim_f.record_event(0)
-    sim_f.step(args.steps)
-    sim_f.record_event(1)
-    fwd_ms = sim_f.event_elapsed_ms(0, 1)
-    sim_f.close()
+        sim.step(1)
+    sim.synchronize()
+    sim.record_event(0)
+    sim.step(args.steps)
+    sim.record_event(1)
+    fwd_ms = sim.event_elapsed_ms(0, 1)
+    sim.set_gradient_enabled(True)
 
-    # ---- end to end through the public API with host buffers: an optimisation-loop
-    # trajectory: the initial rigid velocities from host memory, reset (the context
-    # restores the initial fluid state it holds on the device and uploads the bodies'
-    # initial records), K steps each followed by a rigid-state read-back to the host,
-    # then the adjoint with its host input and output.
+    # ---- end to end through the public API with host buffers: one optimisation-loop
+    # trajectory over the window. The fluid state comes from the device checkpoint (the
+    # trajectory's saved starting state, as the reference's scripts load theirs), the
+    # bodies' states are uploaded from host memory, K single-step calls each followed by a
+    # read-back of every body's state, then the adjoint with its host input and output.
     n = sim.n_fluid
-    n_boundary = sim.n_boundary
+    host_bodies = [sim.rigid_state(b) for b in range(nb)]
+    sim.synchronize()
     t0 = time.perf_counter()
+    sim.checkpoint_restore(slot)
+    sim.reset_gradient()
     for b in range(nb):
-        v0, w0 = sim.rigid_init(b)
-        sim.set_rigid_init(b, v0, w0)
-    sim.reset()
+        sim.set_rigid_state(b, *host_bodies[b])
     for _ in range(args.steps):
         sim.step(1)
         for b in range(nb):
             sim.rigid_state(b)
-    gout = sim.backward(dL)
+    sim.backward(dL)
     sim.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e_s = allmax(pg, e2e_s)
     body_state_bytes = 1656  # one device BodyState record per body per transfer
-    h2d = (nb * body_state_bytes + 2 * nb * 13 * 8) / args.steps   # reset's body records, adjoint input
-    d2h = nb * body_state_bytes + (nb * 6 * 8) / args.steps         # per-step read-back, gradient
+    h2d = (nb * body_state_bytes + nb * 13 * 8) / args.steps     # the bodies' states, adjoint input
+    d2h = nb * body_state_bytes + (nb * 6 * 8) / args.steps       # per-step read-back, gradient
     e2e_value = world * args.steps / e2e_s
+
+    # ---- the CPU oracle over the same window, from the same device state
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sim.checkpoint_restore(slot)
+        for _ in range(args.warmup):
+            sim.step(1)
+        threads = os.cpu_count() or 1
+        cpu_steps = args.cpu_steps
+        cval, cdt, cip = cpu_baseline(args, sim, cpu_steps, threads)
+        t_start, sc_start = sim.time()
+        cpu = {"value": cval, "unit": UNIT, "cores": threads, "kind": "port", "cpu_model": cpu_model(),
+               "sample": f"{cpu_steps} steps (after 1 warm-up step) from the GPU context's state at step "
+                         f"{sc_start} of the full {args.config_name} workload ({cip:.2f} pressure sweeps per "
+                         f"step), oracle port with FP32 fluid / FP64 rigid, gradient on, {threads} OpenMP threads"}
+    sim.checkpoint_free(slot)
 
     # ---- learned warm start vs the reference warm start (collapse phase of a held-out seed)
     ws = None
@@ -355,25 +445,20 @@ def run_ours(args):
             sim = None
         contact = contact_leg(args)
 
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        threads = os.cpu_count() or 1
-        cpu_steps = args.cpu_steps
-        cval, cdt = cpu_baseline(args, cpu_steps, 1, threads)
-        cpu = {"value": cval, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{cpu_steps} steps after 1 warm-up step of the full {args.config_name} workload, "
-                         f"oracle port with FP32 fluid / FP64 rigid, gradient on, {threads} OpenMP threads"}
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded lattice + sampled boundaries)",
-            "config": {"workload": args.config_name, "n_fluid": n, "n_boundary": n_boundary,
-                       "dt": sc.params.time_step, "gradient_mode": "incomplete", "l2": "inputs larger than L2",
-                       "parallelism": f"replicas{world}" if world > 1 else "single GPU"},
+            "config": config_dict(args, sc),
             "fwd_only_steps_per_s": world * args.steps / (fwd_ms / 1000.0),
             "pressure_iterations_per_step": iters_p, "divergence_iterations_per_step": iters_v,
+            "early_phase": {"value": world * args.steps / (early_ms / 1000.0), "unit": UNIT,
+                            "ms_per_step": early_ms / args.steps,
+                            "window": f"steps {args.warmup}-{args.warmup + args.steps - 1} from rest",
+                            "pressure_iterations_per_step": early_st["total_pressure_iterations"] / args.steps,
+                            "divergence_iterations_per_step": early_st["total_divergence_iterations"] / args.steps},
             "gpu_launches": launches,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -452,7 +537,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", type=int, default=1)
-    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--cpu-steps", type=int, default=10)
+    ap.add_argument("--start-step", type=int, default=300)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ws-start", type=int, default=300)
     ap.add_argument("--ws-steps", type=int, default=200)

@@ -254,6 +254,7 @@ def load_library(path: str | None = None):
         "dfsph_mlp_train_step": ([vp, vp, vp, c_int64, vp, c_int64, c_float, POINTER(c_double)], c_int32),
         "dfsph_mlp_gradient": ([vp, vp, vp, c_int64, POINTER(c_double), POINTER(c_double)], c_int32),
         "dfsph_mlp_predict": ([vp, vp, vp, c_int64], c_int32),
+        "dfsph_mlp_set_wait_limit": ([vp, c_int32], c_int32),
         "dfsph_set_warmstart_model": ([vp, vp], c_int32),
         "dfsph_ml_record": ([vp, c_int32], c_int32),
         "dfsph_ml_capture": ([vp, vp, vp, c_int64, POINTER(c_int64)], c_int32),
@@ -278,6 +279,7 @@ EXPORTED_SYMBOLS = (
     "dfsph_checkpoint_save", "dfsph_checkpoint_restore", "dfsph_checkpoint_free", "dfsph_adjoint_sweep",
     "dfsph_mlp_create", "dfsph_mlp_destroy", "dfsph_mlp_get_params", "dfsph_mlp_set_params",
     "dfsph_mlp_fit_normalization", "dfsph_mlp_train_step", "dfsph_mlp_gradient", "dfsph_mlp_predict",
+    "dfsph_mlp_set_wait_limit",
     "dfsph_set_warmstart_model", "dfsph_ml_record", "dfsph_ml_capture",
     "dfsph_get_manager_grad", "dfsph_get_manager_jacobians", "dfsph_get_contact_count",
 )

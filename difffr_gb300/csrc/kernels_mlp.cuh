@@ -178,7 +178,11 @@ static __global__ void __launch_bounds__(MLP_THREADS) k_mlp_infer(MlpView mv, IO
       tc::mma_commit(bar);
     }
     pending = true;
-    bool ok = tc::mbar_wait(bar, phase, MLP_WAIT_LIMIT);
+    // the first wait may be given fewer polls (a test of the failure path below); the wait
+    // for the product still in flight after a failure always has the regular limit
+    const uint32_t lim = (tile == (int)blockIdx.x && mv.first_wait_polls >= 0) ? (uint32_t)mv.first_wait_polls
+                                                                              : MLP_WAIT_LIMIT;
+    bool ok = tc::mbar_wait(bar, phase, lim);
     ok = __syncthreads_and(ok) != 0;
     if (!ok) break;
     pending = false;

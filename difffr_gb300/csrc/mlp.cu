@@ -26,6 +26,7 @@ struct dfsph_mlp {
   int *err = nullptr;
   float norm[dfsph::MLP_NNORM] = {0, 0, 0, 0, 1, 1, 1, 1, 0, 1};
   int64_t adam_t = 0;
+  int first_wait_polls = -1;
 };
 
 namespace dfsph {
@@ -36,6 +37,7 @@ MlpView mlp_view(const dfsph_mlp *m) {
   v.w2img = m->w2img;
   std::memcpy(v.norm, m->norm, sizeof(v.norm));
   v.device = m->device;
+  v.first_wait_polls = m->first_wait_polls;
   return v;
 }
 
@@ -306,6 +308,15 @@ int dfsph_mlp_predict(dfsph_mlp *m, const float *x, float *y, int64_t n) {
     DF_CK(cudaMemcpyAsync(&e, m->err, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
     DF_CK(cudaStreamSynchronize(m->stream));
     if (e) throw DfsphException(DFSPH_ERR_DEVICE, "tensor-core MMA wait timed out in the inference kernel");
+    return DFSPH_OK;
+  });
+}
+
+int dfsph_mlp_set_wait_limit(dfsph_mlp *m, int32_t polls) {
+  return guard_mlp([&] {
+    if (!m) throw DfsphException(DFSPH_ERR_INVALID_ARG, "model is NULL");
+    if (polls < -1) throw DfsphException(DFSPH_ERR_INVALID_ARG, "polls must be -1 (default) or >= 0");
+    m->first_wait_polls = polls;
     return DFSPH_OK;
   });
 }

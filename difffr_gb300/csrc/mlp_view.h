@@ -28,6 +28,9 @@ struct MlpView {
   const uint16_t *w2img = nullptr;
   float norm[MLP_NNORM] = {0, 0, 0, 0, 1, 1, 1, 1, 0, 1};
   int device = 0;
+  // polls allowed to the first tensor-core wait of each inference CTA; -1: the regular limit
+  // (a failure-path test hook set by dfsph_mlp_set_wait_limit)
+  int first_wait_polls = -1;
 };
 
 // Current view of a model (defined in mlp.cu).

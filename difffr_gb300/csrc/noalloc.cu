@@ -18,7 +18,11 @@
 //    on the scratch and must not be issued;
 //  - the first call on each device resolves the scratch array's device address with
 //    cudaGetSymbolAddress (device set-up); make that first call before any stream
-//    capture on that device.
+//    capture on that device;
+//  - the resolved address is cached per device index for the life of the process. A
+//    reset of the device's primary context (cudaDeviceReset) reloads the module and may
+//    move the array, so resetting a device while this library is loaded is not supported
+//    by this entry point.
 #include <cuda_runtime.h>
 
 #include <cstdint>

@@ -631,3 +631,20 @@ class _NoGui:
 
 
 GUI = types.SimpleNamespace(Simulator_GUI_imgui=_NoGui)
+
+
+class _Timing:
+    """Utilities.Timing (Utilities/Timing.h, bound in pySPlisHSPlasH/UtilitiesModule.cpp):
+    the reference prints its CPU timers' sums and averages; the GPU path's per-kernel device
+    times come from DiffDFSPH.profile(), so these print a short note instead."""
+
+    @staticmethod
+    def printAverageTimes():
+        print("timing: per-kernel device times are available from DiffDFSPH.profile()")
+
+    @staticmethod
+    def printTimeSums():
+        print("timing: per-kernel device times are available from DiffDFSPH.profile()")
+
+
+Utilities = types.SimpleNamespace(Timing=_Timing)

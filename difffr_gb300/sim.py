@@ -1,7 +1,7 @@
 """DiffDFSPH simulation handle: a thin wrapper over the libdfsph C ABI.
 
-One ``DiffDFSPH`` owns one device context (all particle state in HBM, one CUDA
-stream). Arrays cross the boundary as float64 numpy arrays in the caller's particle
+One ``DiffDFSPH`` owns one device context (all particle state in HBM; three CUDA
+streams: the fluid solve, the rigid bodies, and the per-body chain rule). Arrays cross the boundary as float64 numpy arrays in the caller's particle
 order. Every method raises ``DfsphError`` on a non-zero status; nothing falls back
 to the CPU.
 """

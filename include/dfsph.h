@@ -406,6 +406,14 @@ int dfsph_mlp_train_step(dfsph_mlp *m, const float *x, const float *y, int64_t n
 int dfsph_mlp_gradient(dfsph_mlp *m, const float *x, const float *y, int64_t n, double *grad, double *loss);
 /* Predicted targets (denormalised) for n samples. */
 int dfsph_mlp_predict(dfsph_mlp *m, const float *x, float *y, int64_t n);
+/* Failure-path test hook (no counterpart in the reference, whose CPU path has no device
+   waits): the number of polls the first tensor-core wait of each inference CTA may take
+   before it gives up (-1: the regular limit). With 0 that wait gives up while the product
+   is still in flight; the kernel then sets its error bit, waits for the product with the
+   regular limit, frees its tensor memory and returns, and the call (dfsph_mlp_predict, or
+   the dfsph_step whose warm start used the model) returns DFSPH_ERR_DEVICE. A context takes
+   the model's setting when dfsph_set_warmstart_model is called. */
+int dfsph_mlp_set_wait_limit(dfsph_mlp *m, int32_t polls);
 /* Use model m for the pressure warm start of ctx (NULL: the reference formula). The
    context keeps the pointer: detach before destroying the model. Needs
    use_pressure_warmstart. */
@@ -421,11 +429,15 @@ int dfsph_ml_capture(dfsph_ctx *ctx, float *x, float *y, int64_t capacity, int64
    or a real-time loop that forbids allocations after start-up). No counterpart in the
    reference. Computes mean(rho0 * rho_adv - rho0) (pressure_mode != 0) or
    mean(rho0 * rho_adv) (pressure_mode == 0) over n device values (float or double per
-   fluid_precision) into *out (device pointer, one double), with the same fixed-order
-   FP64 reduction the solver uses, on `stream` (a cudaStream_t; NULL = default stream).
-   Its only scratch is a static device array in the library: n is limited to 4,194,304;
-   calls on one device share that array, so calls that overlap on the GPU race; the first
-   call on each device resolves the array's address (make it before any stream capture). */
+   fluid_precision) into *out (device pointer, one double), by a fixed-order FP64
+   reduction (deterministic for a given input order; equal to the solver's own average up
+   to FP64 rounding, since the solver sums in cell-sorted order), on `stream` (a
+   cudaStream_t; NULL = default stream). Its only scratch is a static device array in the
+   library: n is limited to 4,194,304; calls on one device share that array, so calls that
+   overlap on the GPU race; the first call on each device resolves the array's address
+   (make it before any stream capture). That address is kept for the life of the process:
+   resetting a device's primary context (cudaDeviceReset) while the library is loaded is
+   not supported by this entry point. */
 int dfsph_density_error_noalloc(const void *rho_adv, int32_t fluid_precision, int64_t n, double density0,
                                 int32_t pressure_mode, double *out, void *stream);
 

@@ -59,6 +59,8 @@ def lib():
             getattr(L, n).argtypes = [c_void_p, c_int, dp]
         for n in ("orc_get_manager_grad", "orc_get_manager_jacobians"):
             getattr(L, n).argtypes = [c_void_p, c_int, c_int, dp]
+        L.orc_set_rigid_state.argtypes = [c_void_p, c_int, dp, dp, dp, dp]
+        L.orc_set_time.argtypes = [c_void_p, c_double, c_int64]
         L.orc_get_contact_count.argtypes = [c_void_p, POINTER(c_int64), POINTER(c_int64)]
         L.orc_get_neighbors.argtypes = [c_void_p, c_int, POINTER(c_int64), POINTER(c_int32), POINTER(c_int64)]
         L.orc_reset.argtypes = [c_void_p]
@@ -76,6 +78,20 @@ def lib():
         L.orc_mlp_eval.restype = c_double
         _lib = L
     return _lib
+
+
+def reference_root():
+    """The DiffFR checkout the reference pins are built from, or None when it is absent.
+
+    Taken from the DIFFFR_REFERENCE environment variable, else a directory named
+    ``reference`` beside this repository. Only the pin recipes and the fixture scripts
+    read it; GPU tests, ``smoke()`` and ``bench.py`` never do.
+    """
+    p = os.environ.get("DIFFFR_REFERENCE")
+    if not p:
+        p = os.path.join(os.path.dirname(_HERE), "..", "reference")
+    p = os.path.abspath(p)
+    return p if os.path.isdir(os.path.join(p, "SPlisHSPlasH")) else None
 
 
 def _p(a):
@@ -188,6 +204,25 @@ class Oracle:
     def set_rigid_velocity(self, b, v, w):
         v = np.asarray(v, dtype=np.float64); w = np.asarray(w, dtype=np.float64)
         assert self.L.orc_set_rigid_velocity(self.h, b, _p(v), _p(w)) == 0
+
+    def set_rigid_state(self, b, x, q, v, w):
+        a = [np.ascontiguousarray(z, dtype=np.float64) for z in (x, q, v, w)]
+        assert self.L.orc_set_rigid_state(self.h, int(b), *[_p(z) for z in a]) == 0
+
+    def set_time(self, t, step_count=0):
+        assert self.L.orc_set_time(self.h, float(t), int(step_count)) == 0
+
+    def load_state(self, sim):
+        """Takes over another run's fluid and rigid state (positions, velocities, both warm-start
+        stiffness fields, every body's state, time and step count), e.g. a GPU context's state in
+        the middle of a trajectory, so that both continue from the same inputs."""
+        from difffr_gb300 import _abi
+        for f in (_abi.FIELD_X, _abi.FIELD_V, _abi.FIELD_KAPPA, _abi.FIELD_KAPPA_V):
+            self.set_field(f, sim.field(f))
+        for b in range(sim.n_bodies):
+            self.set_rigid_state(b, *sim.rigid_state(b))
+        t, sc = sim.time()
+        self.set_time(t, sc)
 
     def neighbors(self, which):
         tot = c_int64()

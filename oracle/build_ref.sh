@@ -4,7 +4,10 @@
 # The rest of the reference is not buildable here: its hot-path translation units include
 # CompactNSearch, GenericParameters and Discregrid, which its CMake fetches by git.
 set -e
-REF=${1:-/root/reference}
+# The checkout comes from the first argument, else DIFFFR_REFERENCE, else ../reference
+# beside the repository.
+HERE=$(cd "$(dirname "$0")" && pwd)
+REF=${1:-${DIFFFR_REFERENCE:-$HERE/../../reference}}
 OUT=$(cd "$(dirname "$0")" && pwd)/_ref
 mkdir -p "$OUT"
 SRC=$(cd "$(dirname "$0")" && pwd)/ref_pin.cpp

@@ -345,6 +345,8 @@ struct Base {
   virtual int net_jac(int b, double *out) = 0;
   virtual int set_init(int b, const double *v, const double *w) = 0;
   virtual int set_velocity(int b, const double *v, const double *w) = 0;
+  virtual int set_rigid_state(int b, const double *x, const double *q, const double *v, const double *w) = 0;
+  virtual int set_time(double t, int64_t step_count) = 0;
   virtual int neighbors(int which, int64_t *start, int32_t *idx, int64_t *total) = 0;
   virtual int reset() = 0;
   virtual int reset_gradient() = 0;
@@ -1453,6 +1455,30 @@ struct Sim : Base {
       bv[j] = (B.dyn || B.anim) ? (cross(B.w, bx[j].template cast<R>() - B.x) + B.v).template cast<F>() : V3F::zero();
     return 0;
   }
+  // A body's whole state (x, q as w x y z, v, omega), e.g. taken from another run at some step,
+  // with the world inertia and the samples moved as Dynamic3dRigidBody::setPosition /
+  // setRotation and SimulatorBase::updateBoundaryParticles do (Dynamic3dRigidBody.h:215-219).
+  int set_rigid_state(int b, const double *xx, const double *qq, const double *vv, const double *ww) override {
+    if (b < 0 || b >= (int)bodies.size()) return DFSPH_ERR_INVALID_ARG;
+    const double qn = std::sqrt(qq[0] * qq[0] + qq[1] * qq[1] + qq[2] * qq[2] + qq[3] * qq[3]);
+    if (!(qn > 0)) return DFSPH_ERR_INVALID_ARG;
+    Body &B = bodies[b];
+    B.x = v3<R>((R)xx[0], (R)xx[1], (R)xx[2]);
+    B.q = QR{(R)(qq[0] / qn), (R)(qq[1] / qn), (R)(qq[2] / qn), (R)(qq[3] / qn)};
+    B.v = v3<R>((R)vv[0], (R)vv[1], (R)vv[2]);
+    B.w = v3<R>((R)ww[0], (R)ww[1], (R)ww[2]);
+    update_inertia(B);
+    for (int64_t j = B.start; j < B.start + B.count; j++) {
+      bx[j] = (B.q.rotate(bx0[j].template cast<R>()) + B.x).template cast<F>();
+      bv[j] = (B.dyn || B.anim) ? (cross(B.w, bx[j].template cast<R>() - B.x) + B.v).template cast<F>() : V3F::zero();
+    }
+    return 0;
+  }
+  int set_time(double tt, int64_t sc) override {
+    t = (R)tt;
+    step_count = sc;
+    return 0;
+  }
   int neighbors(int which, int64_t *start, int32_t *idx, int64_t *total) override {
     const std::vector<int64_t> *S; const std::vector<int32_t> *I;
     if (which == DFSPH_NB_FLUID_FLUID) { S = &ffS; I = &ff; }
@@ -1512,6 +1538,10 @@ int orc_get_rigid_grad(void *s, int b, double *o) { return ((orc::Base *)s)->rig
 int orc_get_net_jacobians(void *s, int b, double *o) { return ((orc::Base *)s)->net_jac(b, o); }
 int orc_set_rigid_init(void *s, int b, const double *v, const double *w) { return ((orc::Base *)s)->set_init(b, v, w); }
 int orc_set_rigid_velocity(void *s, int b, const double *v, const double *w) { return ((orc::Base *)s)->set_velocity(b, v, w); }
+int orc_set_rigid_state(void *s, int b, const double *x, const double *q, const double *v, const double *w) {
+  return ((orc::Base *)s)->set_rigid_state(b, x, q, v, w);
+}
+int orc_set_time(void *s, double t, int64_t sc) { return ((orc::Base *)s)->set_time(t, sc); }
 int orc_get_neighbors(void *s, int which, int64_t *st, int32_t *idx, int64_t *tot) { return ((orc::Base *)s)->neighbors(which, st, idx, tot); }
 int orc_reset(void *s) { return ((orc::Base *)s)->reset(); }
 int orc_reset_gradient(void *s) { return ((orc::Base *)s)->reset_gradient(); }

@@ -1,0 +1,186 @@
+"""GPU against the oracle at the benchmark's own sizes (through the C ABI).
+
+- The 1M-particle dam break the benchmark times (FP32 fluid / FP64 rigid), against the
+  oracle in the same precision split: the three neighbour sets bit-exact as sorted lists
+  (after the first step, and again after five steps from identical inputs); per-particle
+  densities, DFSPH factors, advected densities and velocities within FP32 tolerances;
+  equal pressure and divergence sweep counts; rigid state within 1e-4.
+- The 250k pool with the ellipsoid (its configuration: v ~ U(-2,2)^3, omega ~ U(-5,5)^3):
+  the autograd gradient of a loss on the final rigid state with respect to the six initial
+  velocities, against the oracle's forward chain over the same horizon, cosine >= 0.999.
+- The per-step check of experiments/others/python/finite-difference.py:78-126 at both
+  sizes on the GPU: central differences of the net fluid force on the body with respect to
+  its velocity against the step's own dF/dv block (the reference's formulation drops the
+  fluid's coupled response, so the direction is compared: cosine > 0.9).
+
+Tolerances (FP32 fluid; the oracle sums in another order and evaluates the kernel with
+IEEE square roots where the GPU uses rsqrt): densities 1e-5, factors and advected densities
+1e-4 relative to the field's maximum; velocities 1e-4 of the field's maximum after one
+step, 1e-3 after five.
+"""
+import numpy as np
+import pytest
+
+from difffr_gb300 import _abi
+from difffr_gb300 import scene as scn
+
+pytestmark = pytest.mark.gpu
+
+NB_SETS = (_abi.NB_FLUID_FLUID, _abi.NB_FLUID_BOUNDARY, _abi.NB_BOUNDARY_FLUID)
+
+
+def rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-30))
+
+
+def same_sets(gpu, ref):
+    for which in NB_SETS:
+        sg, ig = gpu.neighbors(which)
+        sr, ir = ref.neighbors(which)
+        assert np.array_equal(sg, sr), f"set {which}: row lengths differ"
+        assert np.array_equal(ig, ir), f"set {which}: indices differ"
+    return int(gpu.neighbor_total(_abi.NB_FLUID_FLUID))
+
+
+@pytest.fixture(scope="module")
+def bench_pair(gpu_lib, oracle_lib):
+    from difffr_gb300.sim import DiffDFSPH
+    sc = scn.dam_break_sphere(enable_gradient=1)
+    gpu = DiffDFSPH(sc)
+    ref = oracle_lib.Oracle(sc, mode=oracle_lib.MODE_MIXED)
+    yield sc, gpu, ref
+    gpu.close()
+
+
+def test_bench_scene_1M_first_step(bench_pair):
+    sc, gpu, ref = bench_pair
+    assert gpu.n_fluid == 1_000_000
+    sg, sr = gpu.step(1), ref.step(1)
+    assert sg["pressure_iterations"] == sr["pressure_iterations"]
+    assert sg["divergence_iterations"] == sr["divergence_iterations"]
+    nff = same_sets(gpu, ref)
+    assert nff > 25 * gpu.n_fluid
+    errs = {f: rel(gpu.field(f), ref.field(f)) for f in
+            (_abi.FIELD_DENSITY, _abi.FIELD_FACTOR, _abi.FIELD_DENSITY_ADV, _abi.FIELD_V, _abi.FIELD_X)}
+    print("1M step 1 relative errors", errs)
+    assert errs[_abi.FIELD_DENSITY] < 1e-5
+    assert errs[_abi.FIELD_FACTOR] < 1e-4
+    assert errs[_abi.FIELD_DENSITY_ADV] < 1e-4
+    assert errs[_abi.FIELD_V] < 1e-4
+    assert errs[_abi.FIELD_X] < 1e-6
+    for b in range(len(sc.bodies)):
+        for a, c in zip(gpu.rigid_state(b), ref.rigid_state(b)):
+            assert np.allclose(a, c, rtol=1e-4, atol=1e-6), (b, a, c)
+
+
+def test_bench_scene_1M_five_steps(bench_pair):
+    sc, gpu, ref = bench_pair
+    for _ in range(4):
+        sg, sr = gpu.step(1), ref.step(1)
+        assert sg["pressure_iterations"] == sr["pressure_iterations"]
+        assert sg["divergence_iterations"] == sr["divergence_iterations"]
+    errs = {f: rel(gpu.field(f), ref.field(f)) for f in
+            (_abi.FIELD_DENSITY, _abi.FIELD_FACTOR, _abi.FIELD_V, _abi.FIELD_X)}
+    print("1M step 5 relative errors", errs)
+    assert errs[_abi.FIELD_DENSITY] < 1e-4
+    assert errs[_abi.FIELD_V] < 1e-3
+    assert errs[_abi.FIELD_X] < 1e-6
+    for b in range(len(sc.bodies)):
+        for a, c in zip(gpu.rigid_state(b), ref.rigid_state(b)):
+            assert np.allclose(a, c, rtol=1e-4, atol=1e-6), (b, a, c)
+    # identical inputs again (the GPU's state taken over by the oracle): the next step's
+    # neighbour sets are bit-exact
+    ref.load_state(gpu)
+    sg, sr = gpu.step(1), ref.step(1)
+    same_sets(gpu, ref)
+    assert sg["pressure_iterations"] == sr["pressure_iterations"]
+
+
+# The horizon of the pool gradient check: the longest over which the FP32 fluid of the GPU
+# and of the oracle stay close enough for the chain's blocks to agree (measured: cosine
+# >= 0.9999 up to this horizon; over 1000 steps the FP32 trajectories separate).
+POOL_HORIZON = 100
+
+
+def test_pool_250k_gradient_matches_oracle(gpu_lib, oracle_lib):
+    import torch
+    from difffr_gb300.autograd import rollout
+    from difffr_gb300.sim import DiffDFSPH
+    from difffr_gb300.validate import _init_params
+    sc = scn.pool_ellipsoid(enable_gradient=1)
+    sim = DiffDFSPH(sc)
+    p0 = _init_params(sim)
+    p = torch.tensor(p0, dtype=torch.float64, requires_grad=True)
+    out = rollout(sim, p, POOL_HORIZON)
+    rng = np.random.default_rng(5)
+    wts = rng.normal(size=(sim.n_bodies, 13))
+    (out * torch.as_tensor(wts)).sum().backward()
+    g = p.grad.numpy()
+    ref = oracle_lib.Oracle(sc, mode=oracle_lib.MODE_MIXED)
+    for b in range(sim.n_bodies):
+        ref.set_rigid_init(b, p0[b, :3], p0[b, 3:])
+    ref.step(POOL_HORIZON)
+    checked = 0
+    for b, body in enumerate(sc.bodies):
+        if not body.is_dynamic:
+            continue
+        blk = ref.rigid_grad_blocks(b)
+        Gv = np.vstack([blk["x_v0"], blk["q_v0"], blk["v_v0"], blk["w_v0"]])
+        Gw = np.vstack([blk["x_w0"], blk["q_w0"], blk["v_w0"], blk["w_w0"]])
+        rg = np.concatenate([wts[b] @ Gv, wts[b] @ Gw])
+        cos = float(rg @ g[b] / (np.linalg.norm(rg) * np.linalg.norm(g[b])))
+        print("pool gradient cosine", b, cos)
+        assert cos >= 0.999, (b, cos)
+        sx, ox = sim.rigid_state(b)[0], ref.rigid_state(b)[0]
+        assert np.linalg.norm(sx - ox) <= 1e-3 * np.linalg.norm(ox)
+        checked += 1
+    assert checked == 1
+    sim.close()
+
+
+def _fd_force_jacobian(sim, body, eps, max_steps):
+    """Steps until the fluid pushes on the body, then central differences of the next step's
+    net fluid force with respect to the body's velocity, and that step's dF/dv block."""
+    # (the first two steps set the body's velocity from its initial values, beginStep's
+    # override for t <= dt, so a perturbation there would be overwritten)
+    for k in range(max_steps):
+        sim.step(1)
+        if k >= 2 and np.linalg.norm(sim.rigid_force(body)[0]) > 0:
+            break
+    assert np.linalg.norm(sim.rigid_force(body)[0]) > 0, "the body never touched the fluid"
+    slot = sim.checkpoint_save()
+    x, q, v, w = sim.rigid_state(body)
+    J = np.zeros((3, 3))
+    for c in range(3):
+        F = []
+        for sgn in (1.0, -1.0):
+            sim.checkpoint_restore(slot)
+            vp = v.copy()
+            vp[c] += sgn * eps
+            sim.set_rigid_state(body, x, q, vp, w)
+            sim.step(1)
+            F.append(sim.rigid_force(body)[0])
+        J[:, c] = (F[0] - F[1]) / (2 * eps)
+    sim.checkpoint_restore(slot)
+    sim.set_rigid_state(body, x, q, v, w)
+    sim.reset_gradient()
+    sim.step(1)
+    Fv = sim.net_jacobians(body)[0:9].reshape(3, 3)
+    sim.checkpoint_free(slot)
+    return float(np.sum(Fv * J) / (np.linalg.norm(Fv) * np.linalg.norm(J)))
+
+
+@pytest.mark.parametrize("size", ["pool_250k", "dam_break_1M"])
+def test_step_force_jacobian_against_finite_differences(gpu_lib, size):
+    from difffr_gb300.sim import DiffDFSPH
+    if size == "pool_250k":
+        sc = scn.pool_ellipsoid(enable_gradient=1)
+    else:
+        sc = scn.dam_break_sphere(enable_gradient=1)
+    body = next(b for b, bd in enumerate(sc.bodies) if bd.is_dynamic)
+    sim = DiffDFSPH(sc)
+    cos = _fd_force_jacobian(sim, body, eps=1e-3, max_steps=400)
+    print("finite-difference cosine", size, cos)
+    assert cos > 0.9, cos
+    sim.close()

@@ -50,7 +50,7 @@ def test_reference_arm_json_line():
     import sys
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference", "--config", "0",
-                        "--steps", "1", "--warmup", "1"], capture_output=True, text=True, timeout=600, cwd=root)
+                        "--steps", "1", "--warmup", "1", "--start-step", "4"], capture_output=True, text=True, timeout=600, cwd=root)
     assert r.returncode == 0, r.stderr[-2000:]
     d = json.loads(r.stdout.strip().splitlines()[-1])
     for k in ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
@@ -61,3 +61,8 @@ def test_reference_arm_json_line():
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
     import bench
     assert d["metric"] == bench.METRIC and d["unit"] == bench.UNIT
+    # the same workload description as the GPU arm's line
+    from types import SimpleNamespace
+    args = SimpleNamespace(config=0, config_name=d["config"]["workload"], start_step=4, warmup=3, steps=1, gpus=1)
+    assert d["config"] == bench.config_dict(args, bench.make_scene(args))
+    assert "steps 7-7" in d["cpu_baseline"]["sample"] and d["cpu_baseline"]["cpu_model"]

@@ -8,6 +8,9 @@ import pytest
 from difffr_gb300 import _abi
 from difffr_gb300 import scene as scn
 from difffr_gb300.scene_json import load_scene
+from oracle import reference_root
+
+REF = reference_root()
 
 
 def test_benchmark_scene_sizes():
@@ -228,11 +231,11 @@ def test_scene_json_obj_body(tmp_path):
     assert np.all(np.max(np.abs(b), axis=1) > 0.5 - 1e-9)
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/experiments"), reason="reference checkout not present")
+@pytest.mark.skipif(REF is None, reason="reference checkout not present")
 def test_reference_scene_files_load():
     """The reference's own scene files (read-only checkout, when present) load with their OBJ
     bodies sampled from the meshes."""
-    base = "/root/reference/experiments/rigid_body_trajectory_optimization/scene"
+    base = os.path.join(REF, "experiments", "rigid_body_trajectory_optimization", "scene")
     sc = load_scene(os.path.join(base, "diff-stone-skipping.json"))
     assert sc.params.surface_tension_method == 2 and sc.params.particle_radius == 0.015
     assert sc.n_fluid > 100000 and len(sc.bodies) == 2
@@ -266,21 +269,21 @@ def test_scene_json_fluid_model_from_bgeo(tmp_path):
     assert np.allclose(sc.fluid_v[1], [-2.0, 0.0, 0.0], atol=1e-6)
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/experiments"), reason="reference checkout not present")
+@pytest.mark.skipif(REF is None, reason="reference checkout not present")
 def test_reference_state_file_reads():
     from difffr_gb300.partio_bgeo import read_bgeo
-    d = read_bgeo("/root/reference/experiments/rigid_body_trajectory_optimization/state/billiards/"
-                  "state_17_particle_Fluid.bgeo")
+    d = read_bgeo(os.path.join(REF, "experiments", "rigid_body_trajectory_optimization", "state", "billiards",
+                               "state_17_particle_Fluid.bgeo"))
     assert d["position"].shape == (87374, 3) and d["velocity"].shape == (87374, 3)
     assert {"id", "kappa", "kappa_v"} <= set(d)
     assert np.all(np.isfinite(d["position"])) and np.abs(d["position"]).max() < 2.0
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/experiments"), reason="reference checkout not present")
+@pytest.mark.skipif(REF is None, reason="reference checkout not present")
 def test_reference_contact_scene_loads():
     """The reference's two-ball billiards scene turns on the rigid contact solver and the
     gradient manager (its Configuration keys reach dfsph_params)."""
-    base = "/root/reference/experiments/rigid_body_trajectory_optimization/scene"
+    base = os.path.join(REF, "experiments", "rigid_body_trajectory_optimization", "scene")
     sc = load_scene(os.path.join(base, "billiards-on-water-2balls.json"))
     p = sc.params
     assert p.use_rigid_contact_solver == 1 and p.use_rigid_gradient_manager == 1
@@ -368,12 +371,12 @@ def test_state_bin_rigid_records_round_trip(tmp_path, real):
     np.testing.assert_array_equal(got2[1][0], got[1][0])
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/experiments"), reason="reference checkout not present")
+@pytest.mark.skipif(REF is None, reason="reference checkout not present")
 def test_reference_state_file_rigid_records():
     """The reference's billiards state (state/billiards/state_17.bin, two moving balls):
     float records with unit quaternions at the end of the file."""
     from difffr_gb300.state_bin import read_rigid_records
-    f = "/root/reference/experiments/rigid_body_trajectory_optimization/state/billiards/state_17.bin"
+    f = os.path.join(REF, "experiments", "rigid_body_trajectory_optimization", "state", "billiards", "state_17.bin")
     recs, dt = read_rigid_records(f, 2)
     assert dt == np.dtype(np.float32)
     np.testing.assert_allclose(recs[0][0], [-0.95, 0.7864, 0.0], atol=1e-4)

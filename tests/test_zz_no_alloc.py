@@ -57,3 +57,40 @@ def test_noalloc_rejects_oversized_input(gpu_lib):
                                          ctypes.c_void_p(16), None)
     assert rc == _abi.DFSPH_ERR_INVALID_ARG
     assert b"4,194,304" in lib.dfsph_last_error()
+
+
+def _noalloc(lib, d, precision, n, pressure_mode, out):
+    rc = lib.dfsph_density_error_noalloc(ctypes.c_void_p(d.data_ptr()), precision, n, 1000.0, pressure_mode,
+                                         ctypes.c_void_p(out.data_ptr()), None)
+    assert rc == 0, lib.dfsph_last_error()
+
+
+@pytest.mark.parametrize("precision", [_abi.DFSPH_FP32, _abi.DFSPH_FP64])
+@pytest.mark.parametrize("pressure_mode", [1, 0])
+@pytest.mark.parametrize("n", [1_000_003, 4_194_304])
+def test_noalloc_many_blocks_against_float64_mean(gpu_lib, precision, pressure_mode, n):
+    """More partials than the final block has threads (its strided loop), up to the largest
+    accepted size, in both precisions and both modes, against numpy's float64 mean of the
+    same per-value terms formed in the input's precision; twice in a row on the shared
+    scratch. Tolerance: 1e-9 relative in FP64; 1e-6 in FP32, where the compiler may form
+    rho0 * r - rho0 with one rounding (a fused multiply-add) or two, a difference of up to
+    half an FP32 ulp of 1000 per value."""
+    import torch
+    lib = _abi.load_library()
+    rng = np.random.default_rng(n + 7 * pressure_mode + precision)
+    ra = 1.0 + 0.01 * rng.random(n)
+    dt = np.float32 if precision == _abi.DFSPH_FP32 else np.float64
+    ra = ra.astype(dt)
+    rho0 = dt(1000.0)
+    terms = (rho0 * ra - rho0) if pressure_mode else (rho0 * ra)
+    want = float(np.mean(terms.astype(np.float64)))
+    d = torch.tensor(ra, device="cuda")
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    for _ in range(2):
+        out.fill_(0.0)
+        torch.cuda.synchronize()
+        _noalloc(lib, d, precision, n, pressure_mode, out)
+        torch.cuda.synchronize()
+        tol = 1e-6 if precision == _abi.DFSPH_FP32 else 1e-9
+        assert float(out.item()) == pytest.approx(want, rel=tol, abs=1e-12)
