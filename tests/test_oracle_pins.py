@@ -69,3 +69,29 @@ def test_kernel_normalisation_and_antisymmetry(oracle_lib):
     assert W.sum() * dx ** 3 == pytest.approx(1.0, rel=2e-3)
     W2, G2, _ = oracle_lib.kernel_eval(h, -r)
     assert np.array_equal(W, W2) and np.allclose(G, -G2, atol=0, rtol=0)
+
+
+# --------------------------------------------------------------------------- the step itself
+# tests/golden/reference_step.npz holds what the reference's own DiffDFSPH step (its sources
+# compiled by oracle/build_ref_step.sh) produced on small contact scenes: per step the sweep
+# counts, the body's state, fluid force and torque and gradient chain state; after the last
+# step the fluid fields and the boundary volumes. In FP64 the oracle reproduces it to the last
+# bits (1e-12 relative allows for summation-order rounding; the fields were equal bit for bit
+# when the fixture was made). In FP32 (the reference's float build against the oracle's float
+# mode) the tolerance is 1e-5.
+import ref_step_fixture as rsf  # noqa: E402
+
+_STEP_GOLD, _STEP_META = rsf.load()
+
+
+@pytest.mark.parametrize("case", sorted(_STEP_META))
+def test_oracle_step_matches_reference_step(oracle_lib, case):
+    m = _STEP_META[case]
+    sc = rsf.scene_of(m)
+    mode = oracle_lib.MODE_F64 if m["build"] == "double" else oracle_lib.MODE_F32
+    o = oracle_lib.Oracle(sc, mode=mode)
+    worst, iters_equal = rsf.compare(o, sc, _STEP_GOLD, case, m["steps"])
+    assert iters_equal
+    tol = 1e-12 if m["build"] == "double" else 1e-5
+    bad = {k: v for k, v in worst.items() if v > tol}
+    assert not bad, (case, bad)
