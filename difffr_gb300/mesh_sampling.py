@@ -63,6 +63,11 @@ def _unique_edges(faces):
     return np.unique(e, axis=0)  # sorted by (first, second) index
 
 
+def _dot3(a, b):
+    """a . b summed as Eigen sums a 3-vector of doubles: (a0 b0 + a1 b1) + a2 b2."""
+    return (a[..., 0] * b[..., 0] + a[..., 1] * b[..., 1]) + a[..., 2] * b[..., 2]
+
+
 def regular_triangle_samples(vertices, faces, d):
     v = np.asarray(vertices, dtype=np.float64)
     faces = np.asarray(faces, dtype=np.int64)
@@ -71,7 +76,7 @@ def regular_triangle_samples(vertices, faces, d):
     for a, b in _unique_edges(faces):
         v0 = v[a]
         direction = v[b] - v0
-        n = int(math.ceil(np.linalg.norm(direction) / d)) + 1
+        n = int(math.ceil(math.sqrt(_dot3(direction, direction)) / d)) + 1
         if n == 1:
             out.append(v0[None, :])
             continue
@@ -83,14 +88,15 @@ def regular_triangle_samples(vertices, faces, d):
         l2, v0, base, top = 0.0, None, None, None
         for c in range(3):
             e = v[f[(c + 1) % 3]] - v[f[c]]
-            le2 = float(e @ e)
+            le2 = float(_dot3(e, e))
             if le2 > l2:
                 l2, v0, base, top = le2, v[f[c]], e, v[f[(c + 2) % 3]] - v[f[c]]
         if v0 is None:
             continue
         length = math.sqrt(l2)
         bn = base / length
-        height = float(np.linalg.norm(top - (bn @ top) * bn))
+        hv = top - _dot3(bn, top) * bn
+        height = math.sqrt(_dot3(hv, hv))
         num_lines = int(math.ceil(height / d)) + 1
         for line in range(1, num_lines - 1):
             alpha = line / (num_lines - 1)

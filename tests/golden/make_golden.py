@@ -2,7 +2,9 @@
 
 Runs oracle/_ref/ref_pin_{double,float} (built by oracle/build_ref.sh from the
 reference's SPHKernels.h/.cpp and GradientUtils.cpp) on seeded inputs and stores
-inputs and outputs in tests/golden/reference_kernels.npz. Run in a container that
+inputs and outputs in tests/golden/reference_kernels.npz; runs oracle/_ref/ref_sampling_double
+(the reference's RegularTriangleSampling.cpp) on a cube and a seeded triangle soup and stores
+the meshes and samples in tests/golden/reference_sampling.npz. Run in a container that
 has the reference checkout:
 
     sh oracle/build_ref.sh /path/to/DiffFR && python tests/golden/make_golden.py
@@ -55,7 +57,37 @@ def run(binary, h, r, qp, dtype):
             "cohesion": st[:, 0], "adhesion": st[:, 1]}
 
 
+def sampling_meshes(seed=3):
+    """A unit cube (12 triangles) and a seeded triangle soup, with the spacings they are
+    sampled at."""
+    v = np.array([[x, y, z] for x in (-.5, .5) for y in (-.5, .5) for z in (-.5, .5)])
+    f = np.array([[0, 1, 3], [0, 3, 2], [4, 6, 7], [4, 7, 5], [0, 4, 5], [0, 5, 1], [2, 3, 7], [2, 7, 6], [0, 2, 6],
+                  [0, 6, 4], [1, 5, 7], [1, 7, 3]])
+    rng = np.random.default_rng(seed)
+    sv = rng.normal(size=(12, 3))
+    sf = rng.integers(0, 12, size=(14, 3))
+    sf = sf[(sf[:, 0] != sf[:, 1]) & (sf[:, 1] != sf[:, 2]) & (sf[:, 0] != sf[:, 2])]
+    return [("cube", v, f, 0.0375), ("cube", v, f, 0.1), ("soup", sv, sf, 0.15)]
+
+
+def run_sampling(v, f, d):
+    """The reference's RegularTriangleSampling::sampleMesh (oracle/_ref/ref_sampling_double)."""
+    import tempfile
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
+        np.concatenate([np.array([len(v), len(f), d], np.float64), np.asarray(v, np.float64).ravel(),
+                        np.asarray(f, np.float64).ravel()]).tofile(fin)
+        subprocess.run([os.path.join(REF, "ref_sampling_double"), fin, fout], check=True)
+        return np.fromfile(fout, np.float64).reshape(-1, 3)
+
+
 def main():
+    samp = {}
+    for k, (name, v, f, d) in enumerate(sampling_meshes()):
+        samp[f"{k}_vertices"], samp[f"{k}_faces"], samp[f"{k}_d"] = v, f, np.array(d)
+        samp[f"{k}_samples"] = run_sampling(v, f, d)
+    np.savez_compressed(os.path.join(HERE, "reference_sampling.npz"), **samp)
+    print("wrote", os.path.join(HERE, "reference_sampling.npz"))
     h, r, qp = inputs()
     res = {"h": np.array(h), "r": r, "qp": qp}
     for prec, dt in (("double", "<f8"), ("float", "<f4")):

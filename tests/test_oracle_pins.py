@@ -95,3 +95,18 @@ def test_oracle_step_matches_reference_step(oracle_lib, case):
     tol = 1e-12 if m["build"] == "double" else 1e-5
     bad = {k: v for k, v in worst.items() if v > tol}
     assert not bad, (case, bad)
+
+
+def test_regular_triangle_sampling_bit_exact():
+    """difffr_gb300.mesh_sampling's regular triangle pattern (samplingMode 1) against the
+    reference's own RegularTriangleSampling::sampleMesh (tests/golden/make_golden.py): the
+    same samples in the same order, bit for bit, on a cube at two spacings and on a seeded
+    triangle soup."""
+    from difffr_gb300.mesh_sampling import regular_triangle_samples
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "reference_sampling.npz"))
+    k = 0
+    while f"{k}_samples" in g:
+        s = regular_triangle_samples(g[f"{k}_vertices"], g[f"{k}_faces"], float(g[f"{k}_d"]))
+        assert np.array_equal(s, g[f"{k}_samples"]), k
+        k += 1
+    assert k == 3
