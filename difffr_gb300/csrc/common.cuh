@@ -18,6 +18,31 @@ enum : int {
   ERR_MLP_TIMEOUT = 1 << 4,
 };
 
+// Bounds-checked build (-DDFSPH_BOUNDS_CHECK, libdfsph_boundscheck.so): every neighbour index
+// read from a list, and every cell-row range, is checked against its array before use. A bad
+// index sets a bit of this translation unit's g_dfsph_bounds_err and is replaced by index 0,
+// so the access stays in bounds; the engine reads the word after each step and reports it as
+// a device error. In the regular build the checks compile to nothing.
+enum : int {
+  BOUNDS_FLUID_LIST = 1 << 0,     // fluid neighbour index outside [0, n)
+  BOUNDS_BOUNDARY_LIST = 1 << 1,  // boundary neighbour index outside [0, boundary samples)
+  BOUNDS_SAMPLE_LIST = 1 << 2,    // a dynamic sample's fluid neighbour outside [0, n)
+  BOUNDS_CELL_RANGE = 1 << 3,     // a cell row's [start, end) outside [0, points]
+};
+#ifdef DFSPH_BOUNDS_CHECK
+static __device__ int g_dfsph_bounds_err;
+__device__ __forceinline__ int checked_index(int j, int lim, int bit) {
+  if ((unsigned)j >= (unsigned)lim) {
+    atomicOr(&g_dfsph_bounds_err, bit);
+    return 0;
+  }
+  return j;
+}
+#define DF_INDEX(j, lim, bit) ::dfsph::checked_index((j), (lim), (bit))
+#else
+#define DF_INDEX(j, lim, bit) (j)
+#endif
+
 template <class T>
 struct alignas(4 * sizeof(T)) V4 {
   T x, y, z, w;

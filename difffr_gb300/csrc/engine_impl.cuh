@@ -197,6 +197,7 @@ Engine<T>::Engine(const dfsph_scene *sc) {
     body_init_.push_back(B);
   }
   anim_ = body_anim0_;
+  fc_.nbr = ns_ + nd_;
   boundary_is_dyn_.assign(boundary_index, 0);
   boundary_slot_.assign(boundary_index, 0);
 
@@ -971,6 +972,22 @@ int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
   hbs_.assign(hbs_pin_, hbs_pin_ + nb_);
   hbs_epoch_ = dev_epoch_;
   hbs_chain_stale_ = chain_pending_;
+#ifdef DFSPH_BOUNDS_CHECK
+  {
+    int be = 0;
+    DF_CK(cudaMemcpyFromSymbol(&be, g_dfsph_bounds_err, sizeof(int)));
+    if (be) {
+      const int zero = 0;
+      DF_CK(cudaMemcpyToSymbol(g_dfsph_bounds_err, &zero, sizeof(int)));
+      std::string m = "bounds-checked build: index out of range:";
+      if (be & BOUNDS_FLUID_LIST) m += " fluid neighbour list;";
+      if (be & BOUNDS_BOUNDARY_LIST) m += " boundary neighbour list;";
+      if (be & BOUNDS_SAMPLE_LIST) m += " dynamic sample's fluid list;";
+      if (be & BOUNDS_CELL_RANGE) m += " cell range;";
+      throw DfsphException(DFSPH_ERR_DEVICE, m);
+    }
+  }
+#endif
   raise_error_word(*err_host_);
   if (st) {
     st->steps_done = nsteps;

@@ -70,8 +70,8 @@ static __global__ void k_contact_rest(ContactConsts c, Grid<T> g, T h2, int ns, 
       else acc += (off == 0 ? vol0S[j] : vol0D[dynSortedToBody[j]]) * w;
     }
   };
-  if (ns > 0) for_each_row(g, cstartS, cx, cy, cz, [&](int b, int e) { visit(b, e, 0); });
-  if (nd > 0) for_each_row(g, cstartD, cx, cy, cz, [&](int b, int e) { visit(b, e, ns); });
+  if (ns > 0) for_each_row(g, cstartS, cx, cy, cz, [&](int b, int e) { visit(b, e, 0); }, ns);
+  if (nd > 0) for_each_row(g, cstartD, cx, cy, cz, [&](int b, int e) { visit(b, e, ns); }, nd);
   if (phase == 0) {
     const double v0 = gamma / acc;
     if (p < ns) vol0S[p] = v0; else vol0D[dynSortedToBody[p - ns]] = v0;
@@ -148,8 +148,8 @@ static __global__ void __launch_bounds__(128) k_contact_samples(
         }
       }
     };
-    if (ns > 0) for_each_row(g, cstartS, cx, cy, cz, [&](int jb, int je) { visit(jb, je, 0); });
-    for_each_row(g, cstartD, cx, cy, cz, [&](int jb, int je) { visit(jb, je, ns); });
+    if (ns > 0) for_each_row(g, cstartS, cx, cy, cz, [&](int jb, int je) { visit(jb, je, 0); }, ns);
+    for_each_row(g, cstartD, cx, cy, cz, [&](int jb, int je) { visit(jb, je, ns); }, nd);
   }
   // combine the lanes' sums (fixed butterfly order)
   auto red = [](double &v) {

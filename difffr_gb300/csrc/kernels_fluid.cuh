@@ -30,6 +30,7 @@ struct FluidConsts {
   Cubic<T> kc;
   Grid<T> grid;
   int kf, kb;  // list capacities
+  int nbr;     // boundary records (static and dynamic samples): the bound of boundary indices
   // Akinci2013 surface tension: coefficients, cohesion kernel k and c, adhesion kernel k
   T st_k, st_kb, coh_k, coh_c, adh_k;
   T visc_b;  // XSPH coefficient against boundary samples (viscosityBoundary)
@@ -206,7 +207,7 @@ static __global__ void k_gather_dynamic(int nd, int ns, const int *__restrict__ 
 // range of the cell-sorted array.
 template <class T, class F>
 static __device__ __forceinline__ void for_each_row(const Grid<T> &g, const int *__restrict__ cstart, int cx, int cy,
-                                             int cz, F &&f) {
+                                             int cz, F &&f, int npts = 0x7fffffff) {
   const int x0 = cx > 0 ? cx - 1 : 0, x1 = cx < g.nx - 1 ? cx + 1 : g.nx - 1;
   for (int dz = -1; dz <= 1; dz++) {
     const int z = cz + dz;
@@ -215,7 +216,17 @@ static __device__ __forceinline__ void for_each_row(const Grid<T> &g, const int 
       const int y = cy + dy;
       if (y < 0 || y >= g.ny) continue;
       const int rb = (z * g.ny + y) * g.nx;
+#ifdef DFSPH_BOUNDS_CHECK
+      int b = cstart[rb + x0], e = cstart[rb + x1 + 1];
+      if (b < 0 || e < b || e > npts) {
+        atomicOr(&g_dfsph_bounds_err, BOUNDS_CELL_RANGE);
+        b = e = 0;
+      }
+      f(b, e);
+#else
+      (void)npts;
       f(cstart[rb + x0], cstart[rb + x1 + 1]);
+#endif
     }
   }
 }
@@ -270,14 +281,14 @@ static __global__ void __launch_bounds__(LIST_THREADS) k_lists_density_factor(
         }
       }
     }
-  });
+  }, c.n);
   if (cnt > c.kf) { atomicOr(err, ERR_FLUID_LIST_OVERFLOW); cnt = c.kf; }
   fcount[i] = cnt;
   for (int k0 = 0; k0 < cnt; k0 += 4) {
     int js[4];
     V4<T> xs[4];
 #pragma unroll
-    for (int u = 0; u < 4; u++) js[u] = (k0 + u < cnt) ? flist[(size_t)(k0 + u) * c.n + i] : i;
+    for (int u = 0; u < 4; u++) js[u] = (k0 + u < cnt) ? DF_INDEX(flist[(size_t)(k0 + u) * c.n + i], c.n, BOUNDS_FLUID_LIST) : i;
 #pragma unroll
     for (int u = 0; u < 4; u++) xs[u] = R[js[u]].x;
 #pragma unroll
@@ -307,12 +318,12 @@ static __global__ void __launch_bounds__(LIST_THREADS) k_lists_density_factor(
       }
     }
   };
-  for_each_row(c.grid, cstartS, cx, cy, cz, [&](int b, int e) { scan_boundary(b, e, 0); });
-  if (cstartD) for_each_row(c.grid, cstartD, cx, cy, cz, [&](int b, int e) { scan_boundary(b, e, ns); });
+  for_each_row(c.grid, cstartS, cx, cy, cz, [&](int b, int e) { scan_boundary(b, e, 0); }, ns);
+  if (cstartD) for_each_row(c.grid, cstartD, cx, cy, cz, [&](int b, int e) { scan_boundary(b, e, ns); }, c.nbr - ns);
   if (bc > c.kb) { atomicOr(err, ERR_BOUNDARY_LIST_OVERFLOW); bc = c.kb; }
   bcount[i] = bc;
   for (int k = 0; k < bc; k++) {
-    const int j = blist[(size_t)k * c.n + i];
+    const int j = DF_INDEX(blist[(size_t)k * c.n + i], c.nbr, BOUNDS_BOUNDARY_LIST);
     const V4<T> xj = BR[j].x;
     const T dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
     const T d2 = dist2_rn(dx, dy, dz);
@@ -438,8 +449,8 @@ static __global__ void k_boundary_psi(FluidConsts<T> c, int ns, int nd, const Re
       if (d2 < c.h2) delta += KEval<T>::W(d2, c.kc);
     }
   };
-  if (ns > 0) for_each_row(c.grid, cstartS, cx, cy, cz, [&](int b, int e) { visit(b, e, 0); });
-  if (nd > 0) for_each_row(c.grid, cstartD, cx, cy, cz, [&](int b, int e) { visit(b, e, ns); });
+  if (ns > 0) for_each_row(c.grid, cstartS, cx, cy, cz, [&](int b, int e) { visit(b, e, 0); }, ns);
+  if (nd > 0) for_each_row(c.grid, cstartD, cx, cy, cz, [&](int b, int e) { visit(b, e, ns); }, nd);
   psi_out[p] = T(1) / delta;
 }
 
@@ -482,12 +493,16 @@ constexpr int LPP = 1;  // lanes per particle in the neighbour passes
 // for sub-lane s, U at a time, as a software pipeline: the U list indices of the next
 // batch are requested before the U gathers (load(j)) of the current batch are consumed,
 // so the list's DRAM latency overlaps the gathers. Bodies run in ascending k.
+// lim, bit: the bound of the list's indices and its bit in the bounds-checked build.
 template <int U, class D, class LoadF, class BodyF>
 static __device__ __forceinline__ void for_neighbors_sub(int cnt, const int *__restrict__ list, int n, int i, int s,
-                                                         LoadF &&load, BodyF &&body) {
+                                                         LoadF &&load, BodyF &&body, int lim, int bit) {
+  (void)lim;
+  (void)bit;
   int js[U];
 #pragma unroll
-  for (int u = 0; u < U; u++) js[u] = (s + u * LPP < cnt) ? __ldcs(list + (size_t)(s + u * LPP) * n + i) : 0;
+  for (int u = 0; u < U; u++)
+    js[u] = (s + u * LPP < cnt) ? DF_INDEX(__ldcs(list + (size_t)(s + u * LPP) * n + i), lim, bit) : 0;
   for (int k0 = s; k0 < cnt; k0 += U * LPP) {
     D d[U];
 #pragma unroll
@@ -495,7 +510,8 @@ static __device__ __forceinline__ void for_neighbors_sub(int cnt, const int *__r
       if (k0 + u * LPP < cnt) d[u] = load(js[u]);
     const int k1 = k0 + U * LPP;
 #pragma unroll
-    for (int u = 0; u < U; u++) js[u] = (k1 + u * LPP < cnt) ? __ldcs(list + (size_t)(k1 + u * LPP) * n + i) : 0;
+    for (int u = 0; u < U; u++)
+      js[u] = (k1 + u * LPP < cnt) ? DF_INDEX(__ldcs(list + (size_t)(k1 + u * LPP) * n + i), lim, bit) : 0;
 #pragma unroll
     for (int u = 0; u < U; u++)
       if (k0 + u * LPP < cnt) body(d[u]);
@@ -577,13 +593,13 @@ static __global__ void __launch_bounds__(PASS_THREADS, (XS ? DFSPH_DENSITY_XS_MI
         ay -= f * (vi4.y - d.v.y) * w;
         az -= f * (vi4.z - d.v.z) * w;
       }
-    });
+    }, c.n, BOUNDS_FLUID_LIST);
     nb = bcount[i];
     for_neighbors_sub<DFSPH_DENSITY_BATCH, Rec<T>>(nb, blist, c.n, i, s, [&](int j) { return ld_rec(BR + j); }, [&](const Rec<T> &d) {
       const T rx = xi.x - d.x.x, ry = xi.y - d.x.y, rz = xi.z - d.x.z;
       const T g = KEval<T>::G(rx * rx + ry * ry + rz * rz, c.kc);
       delta += d.x.w * (g * ((vi4.x - d.v.x) * rx + (vi4.y - d.v.y) * ry + (vi4.z - d.v.z) * rz));
-    });
+    }, c.nbr, BOUNDS_BOUNDARY_LIST);
   }
   delta = sub_sum(delta);
   if (live && s == 0) {
@@ -652,14 +668,14 @@ static __global__ void __launch_bounds__(PASS_THREADS, DFSPH_VELOCITY_MIN_BLOCKS
         const T f = sV * kSum * KEval<T>::G(rx * rx + ry * ry + rz * rz, c.kc);
         dvx += f * rx; dvy += f * ry; dvz += f * rz;
       }
-    });
+    }, c.n, BOUNDS_FLUID_LIST);
     if (fabs(ki) > c.eps) {
       const T sk = c.dt * ki;
       for_neighbors_sub<DFSPH_VELOCITY_BATCH, V4<T>>(bcount[i], blist, c.n, i, s, [&](int j) { return BR[j].x; }, [&](const V4<T> &xj) {
         const T rx = qi.x - xj.x, ry = qi.y - xj.y, rz = qi.z - xj.z;
         const T f = sk * xj.w * KEval<T>::G(rx * rx + ry * ry + rz * rz, c.kc);
         dvx += f * rx; dvy += f * ry; dvz += f * rz;
-      });
+      }, c.nbr, BOUNDS_BOUNDARY_LIST);
     }
   }
   dvx = sub_sum(dvx); dvy = sub_sum(dvy); dvz = sub_sum(dvz);
@@ -712,7 +728,7 @@ static __global__ void __launch_bounds__(256, DFSPH_XSPH_MIN_BLOCKS) k_xsph_adve
         }
         cx -= c.st_k * (ni.x - nj.x); cy -= c.st_k * (ni.y - nj.y); cz -= c.st_k * (ni.z - nj.z);
         ax += Kij * cx; ay += Kij * cy; az += Kij * cz;
-      });
+      }, c.n, BOUNDS_FLUID_LIST);
       for_neighbors_sub<DFSPH_XSPH_BATCH, V4<T>>(bcount[i], blist, c.n, i, s, [&](int j) { return BR[j].x; },
                                                  [&](const V4<T> &xj) {
         const T rx = xi.x - xj.x, ry = xi.y - xj.y, rz = xi.z - xj.z;
@@ -722,7 +738,7 @@ static __global__ void __launch_bounds__(256, DFSPH_XSPH_MIN_BLOCKS) k_xsph_adve
           const T f = c.st_kb * c.rho0 * xj.w * adhesion_W(r1, r2, c) / r1;
           ax -= f * rx; ay -= f * ry; az -= f * rz;
         }
-      });
+      }, c.nbr, BOUNDS_BOUNDARY_LIST);
     }
     const T cvis = c.invH * c.visc;
     for_neighbors_sub<DFSPH_XSPH_BATCH, Rec<T>>(fcount[i], flist, c.n, i, s, [&](int j) { return ld_rec(R + j); },
@@ -733,7 +749,7 @@ static __global__ void __launch_bounds__(256, DFSPH_XSPH_MIN_BLOCKS) k_xsph_adve
       ax -= f * (vi.x - d.v.x) * w;
       ay -= f * (vi.y - d.v.y) * w;
       az -= f * (vi.z - d.v.z) * w;
-    });
+    }, c.n, BOUNDS_FLUID_LIST);
     if (c.visc_b != T(0)) {
       const T fb = -c.invH * c.visc_b;
       const T rho_i = rho[i];
@@ -745,7 +761,7 @@ static __global__ void __launch_bounds__(256, DFSPH_XSPH_MIN_BLOCKS) k_xsph_adve
         ax += f * (vi.x - d.v.x) * w;
         ay += f * (vi.y - d.v.y) * w;
         az += f * (vi.z - d.v.z) * w;
-      });
+      }, c.nbr, BOUNDS_BOUNDARY_LIST);
     }
   }
   ax = sub_sum(ax); ay = sub_sum(ay); az = sub_sum(az);
@@ -772,7 +788,7 @@ static __global__ void __launch_bounds__(256) k_normals(FluidConsts<T> c, const 
     const T rx = xi.x - d.x.x, ry = xi.y - d.x.y, rz = xi.z - d.x.z;
     const T g = d.v.w * KEval<T>::G(rx * rx + ry * ry + rz * rz, c.kc);
     nx += g * rx; ny += g * ry; nz += g * rz;
-  });
+  }, c.n, BOUNDS_FLUID_LIST);
   N[i] = V4<T>{c.kc.h * nx, c.kc.h * ny, c.kc.h * nz, rho[i]};
 }
 

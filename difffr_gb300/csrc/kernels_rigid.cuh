@@ -178,7 +178,7 @@ static __global__ void __launch_bounds__(PAIR_THREADS) k_pairs(FluidConsts<T> c,
   }
 
   for (int k = lane; k < cnt; k += 32) {
-    const int i = bflist[(size_t)k * nd + d];
+    const int i = DF_INDEX(bflist[(size_t)k * nd + d], c.n, BOUNDS_SAMPLE_LIST);
     const V4<T> xi4 = x[i];  // position and the pass's stiffness k_i
     const V3<T> r = {xi4.x - xj.x, xi4.y - xj.y, xi4.z - xj.z};
     const T rl = sqrt(dot(r, r));
@@ -339,7 +339,7 @@ static __global__ void k_visc_boundary_force(FluidConsts<T> c, int nd, const V4<
   T f[3] = {T(0), T(0), T(0)};
   const int cnt = bfcount[d];
   for (int k = 0; k < cnt; k++) {
-    const int i = bflist[(size_t)k * nd + d];
+    const int i = DF_INDEX(bflist[(size_t)k * nd + d], c.n, BOUNDS_SAMPLE_LIST);
     const Rec<T> ri = R[i];
     const T rx = ri.x.x - xj.x, ry = ri.x.y - xj.y, rz = ri.x.z - xj.z;
     const T w = KEval<T>::W(rx * rx + ry * ry + rz * rz, c.kc);

@@ -98,9 +98,11 @@ def test_bench_scene_1M_five_steps(bench_pair):
 
 
 # The horizon of the pool gradient check: the longest over which the FP32 fluid of the GPU
-# and of the oracle stay close enough for the chain's blocks to agree (measured: cosine
-# >= 0.9999 up to this horizon; over 1000 steps the FP32 trajectories separate).
-POOL_HORIZON = 100
+# and of the oracle stay close enough for the chain's blocks to agree. Measured on a GB300
+# (the ellipsoid flies free for its first 200 steps and is in the water from about step
+# 230): cosine of the whole chain state 0.99993 at 300 steps, 0.99992 at 400, 0.9946 at
+# 600; over 1000 FP32 steps the trajectories separate.
+POOL_HORIZON = 400
 
 
 def test_pool_250k_gradient_matches_oracle(gpu_lib, oracle_lib):
@@ -180,7 +182,7 @@ def test_step_force_jacobian_against_finite_differences(gpu_lib, size):
         sc = scn.dam_break_sphere(enable_gradient=1)
     body = next(b for b, bd in enumerate(sc.bodies) if bd.is_dynamic)
     sim = DiffDFSPH(sc)
-    cos = _fd_force_jacobian(sim, body, eps=1e-3, max_steps=400)
+    cos = _fd_force_jacobian(sim, body, eps=1e-3, max_steps=2000)
     print("finite-difference cosine", size, cos)
     assert cos > 0.9, cos
     sim.close()
