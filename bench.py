@@ -538,7 +538,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", type=int, default=1)
     ap.add_argument("--cpu-steps", type=int, default=10)
-    ap.add_argument("--start-step", type=int, default=300)
+    # the headline window: from step 400 of the dam break the pressure solve needs 7-12 sweeps
+    # per step (2 before step 275); the early phase is reported beside it
+    ap.add_argument("--start-step", type=int, default=400)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ws-start", type=int, default=300)
     ap.add_argument("--ws-steps", type=int, default=200)
