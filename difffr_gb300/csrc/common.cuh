@@ -16,7 +16,6 @@ enum : int {
   ERR_BF_LIST_OVERFLOW = 1 << 2,
   ERR_NONFINITE_POSITION = 1 << 3,
   ERR_MLP_TIMEOUT = 1 << 4,
-  ERR_STAGE_TIMEOUT = 1 << 5,  // a chunk's bulk copies into shared memory did not land in time
 };
 
 // Bounds-checked build (-DDFSPH_BOUNDS_CHECK, libdfsph_boundscheck.so): every neighbour index

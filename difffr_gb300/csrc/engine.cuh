@@ -249,14 +249,6 @@ class Engine : public EngineBase {
   DBuf<T> rho_, alpha_, rhoAdv_;
   DBuf<V4<T>> sumgrad_;
   DBuf<int> fcount_, flist_, bcount_, blist_;
-  // chunk-staged passes: the chunk grid, per-chunk tables, the owned chunks (scanned flags,
-  // their count at [nchunk]; the list), the fluid lists as stage slots, and the passes' grids
-  ChunkGrid cg_{1, 1, 1};
-  DBuf<int> ctab_, cpos_, clistc_;
-  DBuf<uint16_t> flist16_;
-  Scanner cscan_;
-  int grid_density_ = 0, grid_velocity_ = 0;
-  void build_chunks();
   DBuf<int> key_, rank_, order_, cstartF_;
   // boundary
   DBuf<Rec<T>> BR_;           // [ns + nd] static (fixed) then dynamic (cell-sorted copy)

@@ -258,37 +258,12 @@ Engine<T>::Engine(const dfsph_scene *sc) {
   fcount_.alloc(N); bcount_.alloc(N);
   // +8 entries: a batched 16-byte load may read up to 7 entries past a short last row
   flist_.alloc(N * (size_t)fc_.kf + 8);
-  flist16_.alloc(N * (size_t)fc_.kf + 16);
-  cg_.nxc = (fc_.grid.nx + CHUNK_X - 1) / CHUNK_X;
-  cg_.nyc = (fc_.grid.ny + CHUNK_Y - 1) / CHUNK_Y;
-  cg_.nzc = (fc_.grid.nz + CHUNK_Z - 1) / CHUNK_Z;
-  ctab_.alloc((size_t)cg_.count() * CHUNK_TAB);
-  cpos_.alloc((size_t)cg_.count() + 1);
-  clistc_.alloc((size_t)cg_.count());
-  cscan_.prepare((size_t)cg_.count() + 1);
-  {
-    // the chunk passes' grids: every block resident at once, striding over the owned chunks
-    auto grid_of = [&](const void *fn) {
-      DF_CK(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared));
-      int per_sm = 0;
-      DF_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, CHUNK_THREADS, CHUNK_STAGE_BYTES));
-      return std::max(1, per_sm) * num_sms_;
-    };
-    // one grid for all density variants: the residual partials of every pass have the same count
-    grid_density_ = std::min({grid_of((const void *)k_density_chunks<T, PASS_PRESSURE, false>),
-                              grid_of((const void *)k_density_chunks<T, PASS_DIVERGENCE, false>),
-                              grid_of((const void *)k_density_chunks<T, PASS_DIVERGENCE, true>),
-                              grid_of((const void *)k_density_chunks<T, PASS_PRESSURE_WARM, false>),
-                              grid_of((const void *)k_density_chunks<T, PASS_DIVERGENCE_WARM, false>)});
-    grid_velocity_ = grid_of((const void *)k_velocity_chunks<T, 0>);
-    grid_velocity_ = std::min(grid_velocity_, grid_of((const void *)k_velocity_chunks<T, 1>));
-  }
   blist_.alloc(N * (size_t)fc_.kb + 8);
   key_.alloc(N); rank_.alloc(N); order_.alloc(N);
   cstartF_.alloc((size_t)ncell_ + 1);
   cstartS_.alloc((size_t)ncell_ + 1);
   cstartD_.alloc((size_t)ncell_ + 1);
-  partials_.alloc((size_t)std::max(blocks(std::max(n_, 1) * LPP, PASS_THREADS), grid_density_));
+  partials_.alloc((size_t)blocks(std::max(n_, 1) * LPP, PASS_THREADS));
   resid_.alloc(4);
   err_.alloc(1);
   DF_CK(cudaHostAlloc((void **)&resid_host_, 4 * sizeof(double), cudaHostAllocMapped));
@@ -482,21 +457,8 @@ void Engine<T>::sort_fluid() {
                                                      perm_[cur_].p, R_[nx].p, kappa_[nx].p, kappaV_[nx].p,
                                                      perm_[nx].p);
   launched();
-  cur_ = nx;
-  build_chunks();
   pend(DFSPH_K_SORT, n_);
-}
-
-// The chunk tables of this step's cell order and the list of owned chunks (the list build
-// stores stage slots through the tables; the chunk-staged passes stride over the list).
-template <class T>
-void Engine<T>::build_chunks() {
-  const int nch = cg_.count();
-  k_chunk_table<T><<<blocks(nch + 1), 256, 0, stream_>>>(fc_.grid, cg_, cstartF_.p, ctab_.p, cpos_.p);
-  launched();
-  cscan_.run(cpos_.p, nch + 1, stream_, launches_);
-  k_chunk_compact<<<blocks(nch), 256, 0, stream_>>>(nch, cpos_.p, clistc_.p);
-  launched();
+  cur_ = nx;
 }
 
 template <class T>
@@ -680,20 +642,20 @@ void Engine<T>::raise_error_word(int e) {
     if (e & ERR_BF_LIST_OVERFLOW) m += " dynamic-boundary fluid list overflow;";
     if (e & ERR_NONFINITE_POSITION) m += " non-finite particle position;";
     if (e & ERR_MLP_TIMEOUT) m += " tensor-core wait timed out in the warm-start model;";
-    if (e & ERR_STAGE_TIMEOUT) m += " bulk copies into shared memory did not land in time;";
     throw DfsphException(DFSPH_ERR_DEVICE, m);
   }
 }
 
 template <class T>
 void Engine<T>::launch_density(int mode, T *kappa_io, bool partials, float4 *feat) {
+  const int nbk = blocks(n_ * LPP, PASS_THREADS);
   double *pp = partials ? partials_.p : nullptr;
   pbegin();
 #define DF_DENS(M, XS)                                                                                             \
-  k_density_chunks<T, M, XS><<<grid_density_, CHUNK_THREADS, CHUNK_STAGE_BYTES, stream_>>>(                        \
-      fc_, clistc_.p, cpos_.p + cg_.count(), ctab_.p, R_[cur_].p, Q_.p, BR_.p, flist_.p, flist16_.p, fcount_.p,    \
-      blist_.p, bcount_.p, rho_.p, alpha_.p, rhoAdv_.p, kappa_io, pp, feat, R_[1 - cur_].p, err_.p)
-  // the divergence solve's checked passes also advance the XSPH phase (see k_density_chunks)
+  k_density_pass<T, M, XS><<<nbk, PASS_THREADS, 0, stream_>>>(fc_, R_[cur_].p, Q_.p, BR_.p, flist_.p, fcount_.p, blist_.p,       \
+                                                     bcount_.p, rho_.p, alpha_.p, rhoAdv_.p, kappa_io, pp, feat,      \
+                                                     R_[1 - cur_].p)
+  // the divergence solve's checked passes also advance the XSPH phase (see k_density_pass)
   const bool xs = mode == PASS_DIVERGENCE && partials && xs_fuse_;
   switch (mode) {
     case PASS_PRESSURE: DF_DENS(PASS_PRESSURE, false); break;
@@ -711,15 +673,14 @@ void Engine<T>::launch_density(int mode, T *kappa_io, bool partials, float4 *fea
 
 template <class T>
 void Engine<T>::launch_velocity(T *kappa_acc) {
+  const int nbk = blocks(n_ * LPP, PASS_THREADS);
   pbegin();
   if (kappa_acc)
-    k_velocity_chunks<T, 1><<<grid_velocity_, CHUNK_THREADS, CHUNK_STAGE_BYTES, stream_>>>(
-        fc_, clistc_.p, cpos_.p + cg_.count(), ctab_.p, Q_.p, R_[cur_].p, BR_.p, flist_.p, flist16_.p, fcount_.p,
-        blist_.p, bcount_.p, kappa_acc, err_.p);
+    k_velocity_pass<T, 1><<<nbk, PASS_THREADS, 0, stream_>>>(fc_, Q_.p, R_[cur_].p, BR_.p, flist_.p, fcount_.p, blist_.p,
+                                                    bcount_.p, kappa_acc);
   else
-    k_velocity_chunks<T, 0><<<grid_velocity_, CHUNK_THREADS, CHUNK_STAGE_BYTES, stream_>>>(
-        fc_, clistc_.p, cpos_.p + cg_.count(), ctab_.p, Q_.p, R_[cur_].p, BR_.p, flist_.p, flist16_.p, fcount_.p,
-        blist_.p, bcount_.p, nullptr, err_.p);
+    k_velocity_pass<T, 0><<<nbk, PASS_THREADS, 0, stream_>>>(fc_, Q_.p, R_[cur_].p, BR_.p, flist_.p, fcount_.p, blist_.p,
+                                                    bcount_.p, nullptr);
   launched();
   pend(DFSPH_K_VELOCITY_PASS, n_);
 }
@@ -774,13 +735,14 @@ void Engine<T>::solve_impl(bool pressure) {
                          : (T(1) / fc_.dt) * (T)P_.max_error_v * T(0.01) * fc_.rho0;
   const int minIt = pressure ? P_.min_iterations : 1;
   const int maxIt = pressure ? P_.max_iterations : P_.max_iterations_v;
+  const int nbk = blocks(n_ * LPP, PASS_THREADS);
   while ((!chk || it < minIt) && it < maxIt) {
     launch_pairs(pressure, false, P_.enable_gradient != 0);
     launch_velocity(warm ? kap : nullptr);
     const bool need = (it + 1 >= minIt) || (it + 1 >= maxIt);
     launch_density(im, nullptr, need);
     if (need) {
-      k_final_sum<<<1, 256, 0, stream_>>>(grid_density_, partials_.p, 1.0 / (double)std::max(n_, 1), resid_.p,
+      k_final_sum<<<1, 256, 0, stream_>>>(nbk, partials_.p, 1.0 / (double)std::max(n_, 1), resid_.p,
                                           resid_host_dev_, err_.p);
       launched();
       check_launch();
@@ -922,7 +884,7 @@ int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
 #define DF_LISTS(W)                                                                                                \
   k_lists_density_factor<T, W><<<blocks(n_, LIST_THREADS), LIST_THREADS, 0, stream_>>>(                            \
       fc_, R_[cur_].p, cstartF_.p, BR_.p, cstartS_.p, nd_ ? cstartD_.p : nullptr, ns_, flist_.p, fcount_.p, blist_.p, \
-      bcount_.p, rho_.p, alpha_.p, sumgrad_.p, err_.p, Q_.p, rhoAdv_.p, kappaV_[cur_].p, cg_, ctab_.p, flist16_.p)
+      bcount_.p, rho_.p, alpha_.p, sumgrad_.p, err_.p, Q_.p, rhoAdv_.p, kappaV_[cur_].p)
         if (divwarm) DF_LISTS(true);
         else DF_LISTS(false);
 #undef DF_LISTS

@@ -20,7 +20,6 @@
 // { x, y, z, psi | vx, vy, vz, - }.
 #pragma once
 #include "common.cuh"
-#include "tc.cuh"
 
 namespace dfsph {
 
@@ -232,121 +231,6 @@ static __device__ __forceinline__ void for_each_row(const Grid<T> &g, const int 
   }
 }
 
-// ------------------------------------------------------------------ chunks
-// The Jacobi passes work on chunks of CHUNK_X x CHUNK_Y x CHUNK_Z cells (x fastest). A
-// chunk's particles are CHUNK_Y * CHUNK_Z contiguous ranges of the cell-sorted arrays (one
-// per row of cells), and every fluid neighbour of them lies in the (CHUNK_Y + 2) x
-// (CHUNK_Z + 2) rows around, over cells x0 - 1 .. x0 + CHUNK_X, each one contiguous range
-// as well. A pass copies those ranges into shared memory with bulk copies and gathers the
-// neighbours from there; the list build stores each fluid neighbour j also as its slot in
-// that copy (uint16): slot = row_off[v] + (j - row_lo[v]) for the row v it lies in.
-// At rest density a chunk holds about 256 particles and stages about 1280 records.
-constexpr int CHUNK_X = 8, CHUNK_Y = 2, CHUNK_Z = 2;
-constexpr int CHUNK_SEGS = CHUNK_Y * CHUNK_Z;
-constexpr int CHUNK_ROWS_Y = CHUNK_Y + 2;
-constexpr int CHUNK_ROWS = CHUNK_ROWS_Y * (CHUNK_Z + 2);
-// per-chunk table (ints): owned ranges (first particle, prefix of counts) and staged rows
-// (first particle, slot prefix)
-constexpr int CT_SEG_LO = 0;                           // [CHUNK_SEGS]
-constexpr int CT_SEG_CUM = CT_SEG_LO + CHUNK_SEGS;     // [CHUNK_SEGS + 1]
-constexpr int CT_ROW_LO = CT_SEG_CUM + CHUNK_SEGS + 1; // [CHUNK_ROWS]
-constexpr int CT_ROW_OFF = CT_ROW_LO + CHUNK_ROWS;     // [CHUNK_ROWS + 1]
-constexpr int CHUNK_TAB = 48;
-static_assert(CT_ROW_OFF + CHUNK_ROWS + 1 <= CHUNK_TAB, "chunk table entry");
-constexpr int CHUNK_THREADS = 256;
-// shared memory for the staged records of one chunk (records beyond it: the chunk gathers
-// from global memory instead)
-#ifndef DFSPH_CHUNK_STAGE_BYTES
-#define DFSPH_CHUNK_STAGE_BYTES (44 * 1024)
-#endif
-constexpr int CHUNK_STAGE_BYTES = DFSPH_CHUNK_STAGE_BYTES;
-
-struct ChunkGrid {
-  int nxc, nyc, nzc;
-  __host__ __device__ int count() const { return nxc * nyc * nzc; }
-};
-
-__device__ __forceinline__ int chunk_of(const ChunkGrid &cg, int cx, int cy, int cz) {
-  return ((cz / CHUNK_Z) * cg.nyc + cy / CHUNK_Y) * cg.nxc + cx / CHUNK_X;
-}
-
-// One thread per chunk: its table entry, and flag[c] = 1 if it owns particles (flag is then
-// scanned in place; flag[count] = 0 so that the scan ends with the number of owned chunks).
-template <class T>
-static __global__ void k_chunk_table(Grid<T> g, ChunkGrid cg, const int *__restrict__ cstart, int *__restrict__ tab,
-                                     int *__restrict__ flag) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nch = cg.count();
-  if (c == nch) flag[c] = 0;
-  if (c >= nch) return;
-  const int xc = c % cg.nxc, t = c / cg.nxc, yc = t % cg.nyc, zc = t / cg.nyc;
-  const int x0 = xc * CHUNK_X, y0 = yc * CHUNK_Y, z0 = zc * CHUNK_Z;
-  const int xe = min(x0 + CHUNK_X, g.nx);
-  int *e = tab + (size_t)c * CHUNK_TAB;
-  int cum = 0;
-  for (int k = 0; k < CHUNK_SEGS; k++) {
-    const int y = y0 + k % CHUNK_Y, z = z0 + k / CHUNK_Y;
-    int lo = 0, hi = 0;
-    if (y < g.ny && z < g.nz) {
-      const int rb = (z * g.ny + y) * g.nx;
-      lo = cstart[rb + x0];
-      hi = cstart[rb + xe];
-    }
-    e[CT_SEG_LO + k] = lo;
-    e[CT_SEG_CUM + k] = cum;
-    cum += hi - lo;
-  }
-  e[CT_SEG_CUM + CHUNK_SEGS] = cum;
-  const int xa = x0 > 0 ? x0 - 1 : 0, xb = min(x0 + CHUNK_X, g.nx - 1);
-  int off = 0;
-  for (int v = 0; v < CHUNK_ROWS; v++) {
-    const int y = y0 - 1 + v % CHUNK_ROWS_Y, z = z0 - 1 + v / CHUNK_ROWS_Y;
-    int lo = 0, hi = 0;
-    if (y >= 0 && y < g.ny && z >= 0 && z < g.nz) {
-      const int rb = (z * g.ny + y) * g.nx;
-      lo = cstart[rb + xa];
-      hi = cstart[rb + xb + 1];
-    }
-    e[CT_ROW_LO + v] = lo;
-    e[CT_ROW_OFF + v] = off;
-    off += hi - lo;
-  }
-  e[CT_ROW_OFF + CHUNK_ROWS] = off;
-  flag[c] = cum > 0 ? 1 : 0;
-}
-
-// The owned chunks in ascending order: list[pos[c]] = c where pos (the scanned flags) steps.
-static __global__ void k_chunk_compact(int nch, const int *__restrict__ pos, int *__restrict__ list) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c < nch && pos[c + 1] > pos[c]) list[pos[c]] = c;
-}
-
-// The cell rows of for_each_row, with each row's (y, z) passed along: f(b, e, y, z).
-template <class T, class F>
-static __device__ __forceinline__ void for_each_row_yz(const Grid<T> &g, const int *__restrict__ cstart, int cx, int cy,
-                                                      int cz, F &&f, int npts) {
-  const int x0 = cx > 0 ? cx - 1 : 0, x1 = cx < g.nx - 1 ? cx + 1 : g.nx - 1;
-  for (int dz = -1; dz <= 1; dz++) {
-    const int z = cz + dz;
-    if (z < 0 || z >= g.nz) continue;
-    for (int dy = -1; dy <= 1; dy++) {
-      const int y = cy + dy;
-      if (y < 0 || y >= g.ny) continue;
-      const int rb = (z * g.ny + y) * g.nx;
-      int b = cstart[rb + x0], e = cstart[rb + x1 + 1];
-#ifdef DFSPH_BOUNDS_CHECK
-      if (b < 0 || e < b || e > npts) {
-        atomicOr(&g_dfsph_bounds_err, BOUNDS_CELL_RANGE);
-        b = e = 0;
-      }
-#else
-      (void)npts;
-#endif
-      f(b, e, y, z);
-    }
-  }
-}
-
 // Neighbour lists (fluid and boundary), density (TimeStep.cpp:147-200) and the
 // DFSPH factor with sum_grad_p_k (TimeStepDiffDFSPH.cpp:883-962), fused in one pass.
 // Also stores the XSPH weight m_i / rho_i in v[i].w for the viscosity pass.
@@ -364,8 +248,7 @@ static __global__ void __launch_bounds__(LIST_THREADS) k_lists_density_factor(
     const Rec<T> *__restrict__ BR, const int *__restrict__ cstartS, const int *__restrict__ cstartD, int ns,
     int *__restrict__ flist, int *__restrict__ fcount, int *__restrict__ blist, int *__restrict__ bcount,
     T *__restrict__ rho, T *__restrict__ alpha, V4<T> *__restrict__ sumgrad, int *__restrict__ err,
-    V4<T> *__restrict__ Q, T *__restrict__ rhoAdv, T *__restrict__ kappaV, ChunkGrid cg,
-    const int *__restrict__ ctab, uint16_t *__restrict__ flist16) {
+    V4<T> *__restrict__ Q, T *__restrict__ rhoAdv, T *__restrict__ kappaV) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= c.n) return;
   const Rec<T> ri = ld_rec(R + i);
@@ -381,12 +264,7 @@ static __global__ void __launch_bounds__(LIST_THREADS) k_lists_density_factor(
   // fused accept branch would be taken by some lane of the warp nearly every iteration),
   // then the lane walks its own list in order. Same neighbours, same order, same formulas.
   int cnt = 0;
-  // the chunk whose staged rows hold the neighbours: a neighbour's slot there is j + d, d of its row
-  const int *ce = ctab + (size_t)chunk_of(cg, cx, cy, cz) * CHUNK_TAB;
-  const int ybase = (cy / CHUNK_Y) * CHUNK_Y - 1, zbase = (cz / CHUNK_Z) * CHUNK_Z - 1;
-  for_each_row_yz(c.grid, cstartF, cx, cy, cz, [&](int b, int e, int ry, int rz) {
-    const int v = (rz - zbase) * CHUNK_ROWS_Y + (ry - ybase);
-    const int d = ce[CT_ROW_OFF + v] - ce[CT_ROW_LO + v];
+  for_each_row(c.grid, cstartF, cx, cy, cz, [&](int b, int e) {
     for (int j0 = b; j0 < e; j0 += DFSPH_LIST_SCAN_BATCH) {
       V4<T> xs[DFSPH_LIST_SCAN_BATCH];
 #pragma unroll
@@ -398,10 +276,7 @@ static __global__ void __launch_bounds__(LIST_THREADS) k_lists_density_factor(
         if (j >= e || j == i) continue;
         const T dx = xi.x - xs[u].x, dy = xi.y - xs[u].y, dz = xi.z - xs[u].z;
         if (dist2_rn(dx, dy, dz) < c.h2) {
-          if (cnt < c.kf) {
-            flist[(size_t)cnt * c.n + i] = j;
-            flist16[(size_t)cnt * c.n + i] = (uint16_t)(j + d);
-          }
+          if (cnt < c.kf) flist[(size_t)cnt * c.n + i] = j;
           cnt++;
         }
       }
@@ -619,15 +494,15 @@ constexpr int LPP = 1;  // lanes per particle in the neighbour passes
 // batch are requested before the U gathers (load(j)) of the current batch are consumed,
 // so the list's DRAM latency overlaps the gathers. Bodies run in ascending k.
 // lim, bit: the bound of the list's indices and its bit in the bounds-checked build.
-template <int U, class D, class L, class LoadF, class BodyF>
-static __device__ __forceinline__ void for_neighbors_sub(int cnt, const L *__restrict__ list, int n, int i, int s,
+template <int U, class D, class LoadF, class BodyF>
+static __device__ __forceinline__ void for_neighbors_sub(int cnt, const int *__restrict__ list, int n, int i, int s,
                                                          LoadF &&load, BodyF &&body, int lim, int bit) {
   (void)lim;
   (void)bit;
   int js[U];
 #pragma unroll
   for (int u = 0; u < U; u++)
-    js[u] = (s + u * LPP < cnt) ? DF_INDEX((int)__ldcs(list + (size_t)(s + u * LPP) * n + i), lim, bit) : 0;
+    js[u] = (s + u * LPP < cnt) ? DF_INDEX(__ldcs(list + (size_t)(s + u * LPP) * n + i), lim, bit) : 0;
   for (int k0 = s; k0 < cnt; k0 += U * LPP) {
     D d[U];
 #pragma unroll
@@ -636,7 +511,7 @@ static __device__ __forceinline__ void for_neighbors_sub(int cnt, const L *__res
     const int k1 = k0 + U * LPP;
 #pragma unroll
     for (int u = 0; u < U; u++)
-      js[u] = (k1 + u * LPP < cnt) ? DF_INDEX((int)__ldcs(list + (size_t)(k1 + u * LPP) * n + i), lim, bit) : 0;
+      js[u] = (k1 + u * LPP < cnt) ? DF_INDEX(__ldcs(list + (size_t)(k1 + u * LPP) * n + i), lim, bit) : 0;
 #pragma unroll
     for (int u = 0; u < U; u++)
       if (k0 + u * LPP < cnt) body(d[u]);
@@ -809,228 +684,6 @@ static __global__ void __launch_bounds__(PASS_THREADS, DFSPH_VELOCITY_MIN_BLOCKS
     V4<T> vi = R[i].v;
     vi.x += dvx; vi.y += dvy; vi.z += dvz;
     R[i].v = vi;
-  }
-}
-
-// ------------------------------------------------------------------ chunk-staged passes
-// The same passes over chunks (see "chunks" above), one chunk per block at a time, the grid
-// striding over the owned chunks (their count is read on the device). Thread 0 copies the
-// chunk's staged rows of the gathered array (R for the density pass, Q for the velocity pass)
-// into shared memory with bulk copies completing on an mbarrier; every fluid neighbour is
-// then read from there through its slot. A chunk whose rows exceed the stage gathers from
-// global memory through the int32 list instead. Boundary neighbours are gathered from global
-// memory as before. Sums run over the same neighbours in the same order as the global path.
-// The wait for the copies is bounded; if it runs out the block records ERR_STAGE_TIMEOUT,
-// waits once more (bounded) for its copies and, if they still have not landed, stops.
-#ifndef DFSPH_STAGE_WAIT_LIMIT
-#define DFSPH_STAGE_WAIT_LIMIT (1u << 22)
-#endif
-// neighbours in flight per thread: from shared memory (short latency), and on the global
-// fallback path of oversized chunks
-#ifndef DFSPH_CHUNK_BATCH
-#define DFSPH_CHUNK_BATCH 2
-#endif
-#ifndef DFSPH_CHUNK_DENSITY_MIN_BLOCKS
-#define DFSPH_CHUNK_DENSITY_MIN_BLOCKS 4
-#endif
-#ifndef DFSPH_CHUNK_VELOCITY_MIN_BLOCKS
-#define DFSPH_CHUNK_VELOCITY_MIN_BLOCKS 4
-#endif
-
-// Stages the chunk's rows of `src` (the table entry in `tab`) into `stage`; all threads call
-// it. Returns 1 when the records are in shared memory, 0 when the chunk is too large for the
-// stage (gather from global memory), -1 when the copies did not land within the limits.
-template <class E>
-static __device__ __forceinline__ int stage_chunk(const int *tab, const E *__restrict__ src, E *stage, uint64_t *bar,
-                                                  uint32_t &phase, int *err) {
-  const int S = tab[CT_ROW_OFF + CHUNK_ROWS];
-  if (S * (int)sizeof(E) > CHUNK_STAGE_BYTES) return 0;
-  if (threadIdx.x == 0) {
-    // the previous chunk's generic reads of the stage come before these async-proxy writes
-    tc::fence_async_smem();
-    tc::mbar_arrive_expect_tx(bar, (uint32_t)(S * sizeof(E)));
-    for (int v = 0; v < CHUNK_ROWS; v++) {
-      const int len = tab[CT_ROW_OFF + v + 1] - tab[CT_ROW_OFF + v];
-      if (len > 0) tc::bulk_g2s(stage + tab[CT_ROW_OFF + v], src + tab[CT_ROW_LO + v], (uint32_t)(len * sizeof(E)), bar);
-    }
-  }
-  int ok = __syncthreads_and(tc::mbar_wait(bar, phase, DFSPH_STAGE_WAIT_LIMIT));
-  if (!ok) {
-    if (threadIdx.x == 0) atomicOr(err, ERR_STAGE_TIMEOUT);
-    ok = __syncthreads_and(tc::mbar_wait(bar, phase, DFSPH_STAGE_WAIT_LIMIT));
-    if (!ok) return -1;
-  }
-  phase ^= 1u;
-  return 1;
-}
-
-// particle of the chunk's q-th owned slot
-static __device__ __forceinline__ int chunk_particle(const int *tab, int q) {
-  int k = 0;
-#pragma unroll
-  for (int u = 1; u < CHUNK_SEGS; u++) k += (q >= tab[CT_SEG_CUM + u]) ? 1 : 0;
-  return tab[CT_SEG_LO + k] + (q - tab[CT_SEG_CUM + k]);
-}
-
-template <class T, int MODE, bool XS = false>
-static __global__ void __launch_bounds__(CHUNK_THREADS, DFSPH_CHUNK_DENSITY_MIN_BLOCKS) k_density_chunks(
-    FluidConsts<T> c, const int *__restrict__ chunk_list, const int *__restrict__ nchunks, const int *__restrict__ ctab,
-    const Rec<T> *__restrict__ R, V4<T> *__restrict__ Q, const Rec<T> *__restrict__ BR, const int *__restrict__ flist,
-    const uint16_t *__restrict__ flist16, const int *__restrict__ fcount, const int *__restrict__ blist,
-    const int *__restrict__ bcount, const T *__restrict__ rho, const T *__restrict__ alpha, T *__restrict__ rhoAdv,
-    T *__restrict__ kappa_io, double *__restrict__ partials, float4 *__restrict__ feat, Rec<T> *__restrict__ R_out,
-    int *__restrict__ err) {
-  extern __shared__ __align__(128) unsigned char chunk_stage_raw[];
-  Rec<T> *stage = reinterpret_cast<Rec<T> *>(chunk_stage_raw);
-  __shared__ __align__(8) uint64_t bar;
-  __shared__ int tab[CHUNK_TAB];
-  if (threadIdx.x == 0) {
-    tc::mbar_init(&bar, 1);
-    tc::fence_mbar_init();
-  }
-  __syncthreads();
-  const int nch = *nchunks;
-  uint32_t phase = 0;
-  double e = 0.0;
-  const T cvis = c.invH * c.visc;
-  for (int ci = blockIdx.x; ci < nch; ci += gridDim.x) {
-    const int chunk = chunk_list[ci];
-    if (threadIdx.x < CHUNK_TAB) tab[threadIdx.x] = ctab[(size_t)chunk * CHUNK_TAB + threadIdx.x];
-    __syncthreads();
-    const int staged = stage_chunk(tab, R, stage, &bar, phase, err);
-    if (staged < 0) break;
-    const int S = tab[CT_ROW_OFF + CHUNK_ROWS];
-    const int total = tab[CT_SEG_CUM + CHUNK_SEGS];
-    for (int q = threadIdx.x; q < total; q += blockDim.x) {
-      const int i = chunk_particle(tab, q);
-      const Rec<T> ri = ld_rec(R + i);
-      const V4<T> xi = ri.x, vi4 = ri.v;
-      T delta = T(0), ax = T(0), ay = T(0), az = T(0);
-      auto fluid = [&](const Rec<T> &d) {
-        const T rx = xi.x - d.x.x, ry = xi.y - d.x.y, rz = xi.z - d.x.z;
-        const T g = KEval<T>::G(rx * rx + ry * ry + rz * rz, c.kc);
-        delta += c.V * (g * ((vi4.x - d.v.x) * rx + (vi4.y - d.v.y) * ry + (vi4.z - d.v.z) * rz));
-        if (XS) {
-          const T w = KEval<T>::W(rx * rx + ry * ry + rz * rz, c.kc);
-          const T f = cvis * d.v.w;
-          ax -= f * (vi4.x - d.v.x) * w;
-          ay -= f * (vi4.y - d.v.y) * w;
-          az -= f * (vi4.z - d.v.z) * w;
-        }
-      };
-      const int nf = fcount[i];
-      if (staged)
-        for_neighbors_sub<DFSPH_CHUNK_BATCH, Rec<T>>(nf, flist16, c.n, i, 0, [&](int sl) { return stage[sl]; }, fluid,
-                                                     S, BOUNDS_FLUID_LIST);
-      else
-        for_neighbors_sub<1, Rec<T>>(nf, flist, c.n, i, 0, [&](int j) { return ld_rec(R + j); }, fluid, c.n,
-                                     BOUNDS_FLUID_LIST);
-      const int nb = bcount[i];
-      for_neighbors_sub<1, Rec<T>>(nb, blist, c.n, i, 0, [&](int j) { return ld_rec(BR + j); },
-                                                     [&](const Rec<T> &d) {
-        const T rx = xi.x - d.x.x, ry = xi.y - d.x.y, rz = xi.z - d.x.z;
-        const T g = KEval<T>::G(rx * rx + ry * ry + rz * rz, c.kc);
-        delta += d.x.w * (g * ((vi4.x - d.v.x) * rx + (vi4.y - d.v.y) * ry + (vi4.z - d.v.z) * rz));
-      }, c.nbr, BOUNDS_BOUNDARY_LIST);
-      T ra;
-      if (MODE == PASS_PRESSURE || MODE == PASS_PRESSURE_WARM) {
-        ra = rho[i] / c.rho0 + c.dt * delta;
-        ra = ra > T(1) ? ra : T(1);
-      } else {
-        ra = delta > T(0) ? delta : T(0);
-        if (nf + nb < 20) ra = T(0);
-      }
-      rhoAdv[i] = ra;
-      T kq;
-      if (MODE == PASS_PRESSURE) {
-        kq = (ra - T(1)) * alpha[i] * c.invH2;
-        e += (double)(c.rho0 * ra - c.rho0);
-      } else if (MODE == PASS_DIVERGENCE) {
-        kq = ra * alpha[i] * c.invH;
-        e += (double)(c.rho0 * ra);
-      } else if (MODE == PASS_PRESSURE_WARM) {
-        const T kp = kappa_io[i];
-        kq = (ra > T(1)) ? T(0.5) * (kp > T(-0.00025) ? kp : T(-0.00025)) * c.invH2 : T(0);
-        kappa_io[i] = kq;
-        if (feat)
-          feat[i] = make_float4((float)(ra - T(1)), (float)(nf + nb), (float)(kp * c.invH2),
-                                (float)sqrt(ri.v.x * ri.v.x + ri.v.y * ri.v.y + ri.v.z * ri.v.z));
-      } else {
-        const T kp = kappa_io[i];
-        kq = (ra > T(0)) ? T(0.5) * (kp > T(-0.5) ? kp : T(-0.5)) * c.invH : T(0);
-        kappa_io[i] = kq;
-      }
-      Q[i] = V4<T>{ri.x.x, ri.x.y, ri.x.z, kq};
-      if (XS) {
-        ax += c.gx; ay += c.gy; az += c.gz;
-        R_out[i] = Rec<T>{ri.x, V4<T>{vi4.x + c.dt * ax, vi4.y + c.dt * ay, vi4.z + c.dt * az, vi4.w}};
-      }
-    }
-    __syncthreads();  // the stage is read by every thread before the next chunk's copies land
-  }
-  if (partials) block_partial_sum(e, partials);
-}
-
-template <class T, int ACC>
-static __global__ void __launch_bounds__(CHUNK_THREADS, DFSPH_CHUNK_VELOCITY_MIN_BLOCKS) k_velocity_chunks(
-    FluidConsts<T> c, const int *__restrict__ chunk_list, const int *__restrict__ nchunks, const int *__restrict__ ctab,
-    const V4<T> *__restrict__ Q, Rec<T> *__restrict__ R, const Rec<T> *__restrict__ BR, const int *__restrict__ flist,
-    const uint16_t *__restrict__ flist16, const int *__restrict__ fcount, const int *__restrict__ blist,
-    const int *__restrict__ bcount, T *__restrict__ kappa_acc, int *__restrict__ err) {
-  extern __shared__ __align__(128) unsigned char chunk_stage_raw[];
-  V4<T> *stage = reinterpret_cast<V4<T> *>(chunk_stage_raw);
-  __shared__ __align__(8) uint64_t bar;
-  __shared__ int tab[CHUNK_TAB];
-  if (threadIdx.x == 0) {
-    tc::mbar_init(&bar, 1);
-    tc::fence_mbar_init();
-  }
-  __syncthreads();
-  const int nch = *nchunks;
-  uint32_t phase = 0;
-  const T sV = c.dt * c.V;
-  for (int ci = blockIdx.x; ci < nch; ci += gridDim.x) {
-    const int chunk = chunk_list[ci];
-    if (threadIdx.x < CHUNK_TAB) tab[threadIdx.x] = ctab[(size_t)chunk * CHUNK_TAB + threadIdx.x];
-    __syncthreads();
-    const int staged = stage_chunk(tab, Q, stage, &bar, phase, err);
-    if (staged < 0) break;
-    const int S = tab[CT_ROW_OFF + CHUNK_ROWS];
-    const int total = tab[CT_SEG_CUM + CHUNK_SEGS];
-    for (int q = threadIdx.x; q < total; q += blockDim.x) {
-      const int i = chunk_particle(tab, q);
-      const V4<T> qi = Q[i];
-      const T ki = qi.w;
-      T dvx = T(0), dvy = T(0), dvz = T(0);
-      auto fluid = [&](const V4<T> &qj) {
-        const T kSum = ki + qj.w;
-        if (fabs(kSum) > c.eps) {
-          const T rx = qi.x - qj.x, ry = qi.y - qj.y, rz = qi.z - qj.z;
-          const T f = sV * kSum * KEval<T>::G(rx * rx + ry * ry + rz * rz, c.kc);
-          dvx += f * rx; dvy += f * ry; dvz += f * rz;
-        }
-      };
-      if (staged)
-        for_neighbors_sub<DFSPH_CHUNK_BATCH, V4<T>>(fcount[i], flist16, c.n, i, 0, [&](int sl) { return stage[sl]; },
-                                                    fluid, S, BOUNDS_FLUID_LIST);
-      else
-        for_neighbors_sub<1, V4<T>>(fcount[i], flist, c.n, i, 0, [&](int j) { return Q[j]; }, fluid, c.n,
-                                    BOUNDS_FLUID_LIST);
-      if (fabs(ki) > c.eps) {
-        const T sk = c.dt * ki;
-        for_neighbors_sub<2, V4<T>>(bcount[i], blist, c.n, i, 0, [&](int j) { return BR[j].x; },
-                                                       [&](const V4<T> &xj) {
-          const T rx = qi.x - xj.x, ry = qi.y - xj.y, rz = qi.z - xj.z;
-          const T f = sk * xj.w * KEval<T>::G(rx * rx + ry * ry + rz * rz, c.kc);
-          dvx += f * rx; dvy += f * ry; dvz += f * rz;
-        }, c.nbr, BOUNDS_BOUNDARY_LIST);
-      }
-      if (ACC) kappa_acc[i] += ki;
-      V4<T> vi = R[i].v;
-      vi.x += dvx; vi.y += dvy; vi.z += dvz;
-      R[i].v = vi;
-    }
-    __syncthreads();
   }
 }
 

@@ -104,20 +104,6 @@ static __device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity)
       : "memory");
   return ok != 0;
 }
-// ---- 1-D bulk copies (TMA without a tensor map) into shared memory, completing on an
-// mbarrier: one thread announces the bytes with arrive.expect_tx, then issues the copies;
-// the phase completes when all announced bytes have landed. Source, destination and size
-// must be multiples of 16 bytes.
-static __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-static __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                   smem_u32(dst)),
-               "l"(src), "r"(bytes), "r"(smem_u32(bar))
-               : "memory");
-}
-
 // Waits for the phase with the given parity to complete; gives up after `limit` polls
 // (with a short sleep between polls) and returns false.
 static __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t limit) {
