@@ -38,18 +38,51 @@ static __device__ __forceinline__ float tanh_approx(float x) {
   return y;
 }
 
+// GELU, tanh form: g(x) = h + h t with h = x / 2, t = tanh(x (c + c a x^2)), c = sqrt(2/pi),
+// a = 0.044715; d = g'(x).
+constexpr float GELU_C = 0.7978845608028654f, GELU_A = 0.044715f, GELU_CA = 0.7978845608028654f * 0.044715f;
 static __device__ __forceinline__ float gelu_d(float x, float &d) {
-  // tanh form: 0.5 x (1 + tanh(c (x + a x^3)))
-  const float c = 0.7978845608028654f, a = 0.044715f;
   const float x2 = x * x;
-  const float u = c * (x + a * x2 * x);
-  const float t = tanh_approx(u);
-  d = 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * c * (1.0f + 3.0f * a * x2);
-  return 0.5f * x * (1.0f + t);
+  const float t = tanh_approx(x * fmaf(GELU_CA, x2, GELU_C));
+  const float h = 0.5f * x;
+  d = 0.5f * (1.0f + t) + h * (1.0f - t * t) * GELU_C * (1.0f + 3.0f * GELU_A * x2);
+  return fmaf(h, t, h);
 }
 static __device__ __forceinline__ float gelu_f(float x) {
-  float d;
-  return gelu_d(x, d);
+  const float t = tanh_approx(x * fmaf(GELU_CA, x * x, GELU_C));
+  const float h = 0.5f * x;
+  return fmaf(h, t, h);
+}
+
+// ---- packed FP32 pairs (Blackwell f32x2 arithmetic: two IEEE FP32 operations per
+// instruction, each rounded as its scalar form)
+static __device__ __forceinline__ unsigned long long f2_bits(float2 v) {
+  return (unsigned long long)__float_as_uint(v.x) | ((unsigned long long)__float_as_uint(v.y) << 32);
+}
+static __device__ __forceinline__ float2 f2_of(unsigned long long u) {
+  return make_float2(__uint_as_float((unsigned)u), __uint_as_float((unsigned)(u >> 32)));
+}
+static __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+  unsigned long long d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)), "l"(f2_bits(c)));
+  return f2_of(d);
+}
+static __device__ __forceinline__ float2 mul2(float2 a, float2 b) {
+  unsigned long long d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+  return f2_of(d);
+}
+static __device__ __forceinline__ float2 add2(float2 a, float2 b) {
+  unsigned long long d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+  return f2_of(d);
+}
+// gelu_f on a pair
+static __device__ __forceinline__ float2 gelu2(float2 x) {
+  const float2 u = mul2(x, fma2(make_float2(GELU_CA, GELU_CA), mul2(x, x), make_float2(GELU_C, GELU_C)));
+  const float2 t = make_float2(tanh_approx(u.x), tanh_approx(u.y));
+  const float2 h = mul2(make_float2(0.5f, 0.5f), x);
+  return fma2(h, t, h);
 }
 
 static __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
@@ -71,8 +104,23 @@ static __device__ __forceinline__ uint8_t *align1024(uint8_t *p) {
   return reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
 }
 
-// Small weights in shared memory: W1 (256), b1 (64), b2 (64), w3 (64), b3 (1).
+// Small weights in shared memory: W1 (256), b1 (64), b2 (64), w3 (64), b3 (1). The inference
+// kernel keeps W1 in unit pairs instead: float2 {W1[2p][k], W1[2p+1][k]} at 8 p + 2 k.
 constexpr int MLP_SW_W1 = 0, MLP_SW_B1 = 256, MLP_SW_B2 = 320, MLP_SW_W3 = 384, MLP_SW_B3 = 448, MLP_SW_N = 452;
+
+static __device__ __forceinline__ void mlp_stage_small_paired(const float *wuse, float *sw) {
+  for (int k = threadIdx.x; k < MLP_SW_N; k += blockDim.x) {
+    float v = 0.f;
+    if (k < MLP_SW_B1) {
+      const int p = k >> 3, kk = (k >> 1) & 3, odd = k & 1;  // W1 pair p, input kk, unit 2p + odd
+      v = wuse[MLP_OFF_W1 + 4 * (2 * p + odd) + kk];
+    } else if (k < MLP_SW_B2) v = wuse[k];                          // b1
+    else if (k < MLP_SW_W3) v = wuse[MLP_OFF_B2 + (k - MLP_SW_B2)];  // b2
+    else if (k < MLP_SW_B3) v = wuse[MLP_OFF_W3 + (k - MLP_SW_W3)];  // w3
+    else if (k == MLP_SW_B3) v = wuse[MLP_OFF_B3];
+    sw[k] = v;
+  }
+}
 
 static __device__ __forceinline__ void mlp_stage_small(const float *wuse, float *sw) {
   for (int k = threadIdx.x; k < MLP_SW_N; k += blockDim.x) {
@@ -110,6 +158,33 @@ static __device__ __forceinline__ void mlp_layer1(const float *sw, const float f
   }
 }
 
+// hidden layer 1 of the inference kernel, two units per packed operation (W1 paired as
+// staged by mlp_stage_small_paired)
+static __device__ __forceinline__ void mlp_layer1_paired(const float *sw, const float f[4], uint8_t *tile, int row,
+                                                         int cols) {
+  const float2 *w1p = reinterpret_cast<const float2 *>(sw + MLP_SW_W1);
+  const float2 *b1p = reinterpret_cast<const float2 *>(sw + MLP_SW_B1);
+  const float2 f0 = make_float2(f[0], f[0]), f1 = make_float2(f[1], f[1]), f2 = make_float2(f[2], f[2]),
+               f3 = make_float2(f[3], f[3]);
+#pragma unroll
+  for (int c = 0; c < MLP_H; c += 8) {
+    float h[8];
+#pragma unroll
+    for (int u = 0; u < 8; u += 2) {
+      const int p = (c + u) >> 1;
+      float2 z = b1p[p];
+      z = fma2(w1p[4 * p + 0], f0, z);
+      z = fma2(w1p[4 * p + 1], f1, z);
+      z = fma2(w1p[4 * p + 2], f2, z);
+      z = fma2(w1p[4 * p + 3], f3, z);
+      const float2 g = gelu2(z);
+      h[u] = g.x;
+      h[u + 1] = g.y;
+    }
+    st_row8(tile, row, c, cols, h);
+  }
+}
+
 // ------------------------------------------------------------------ inference
 // Persistent over tiles of 128 particles: one thread per particle row. Shared memory:
 // W2 image 8 KB, the H1 tile 16 KB, small weights, one mbarrier; TMEM: 64 columns.
@@ -135,7 +210,7 @@ static __global__ void __launch_bounds__(MLP_THREADS) k_mlp_infer(MlpView mv, IO
 
   for (int k = tid; k < 8192 / 16; k += MLP_THREADS)
     reinterpret_cast<uint4 *>(sW2)[k] = reinterpret_cast<const uint4 *>(mv.w2img)[k];
-  mlp_stage_small(mv.wuse, sw);
+  mlp_stage_small_paired(mv.wuse, sw);
   if (tid == 0) {
     tc::mbar_init(bar, 1);
     tc::fence_mbar_init();
@@ -165,7 +240,7 @@ static __global__ void __launch_bounds__(MLP_THREADS) k_mlp_infer(MlpView mv, IO
     if (i < n) want = io.load(i, f);
 #pragma unroll
     for (int k = 0; k < 4; k++) f[k] = (f[k] - xm[k]) * xi[k];
-    mlp_layer1<false>(sw, f, sH1, tid, 64, nullptr);
+    mlp_layer1_paired(sw, f, sH1, tid, 64);
     tc::fence_async_smem();
     tc::fence_before_sync();
     __syncthreads();
@@ -188,15 +263,22 @@ static __global__ void __launch_bounds__(MLP_THREADS) k_mlp_infer(MlpView mv, IO
     pending = false;
     phase ^= 1u;
     tc::fence_after_sync();
-    float out = sw[MLP_SW_B3];
+    // output layer: the even and odd hidden units summed in two packed partial sums
+    float2 acc = make_float2(0.f, 0.f);
+    const float2 *b2p = reinterpret_cast<const float2 *>(sw + MLP_SW_B2);
+    const float2 *w3p = reinterpret_cast<const float2 *>(sw + MLP_SW_W3);
 #pragma unroll
     for (int c = 0; c < 64; c += 16) {
       float z[16];
       tc::tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c, z);
       tc::tmem_wait_ld();
 #pragma unroll
-      for (int u = 0; u < 16; u++) out += sw[MLP_SW_W3 + c + u] * gelu_f(z[u] + sw[MLP_SW_B2 + c + u]);
+      for (int u = 0; u < 16; u += 2) {
+        const int p = (c + u) >> 1;
+        acc = fma2(w3p[p], gelu2(add2(make_float2(z[u], z[u + 1]), b2p[p])), acc);
+      }
     }
+    const float out = sw[MLP_SW_B3] + (acc.x + acc.y);
     if (want) io.store(i, out * ys + ym);
     tc::fence_before_sync();
   }

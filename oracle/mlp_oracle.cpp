@@ -27,13 +27,14 @@ float bf16r(float v) {
   return v;
 }
 
+// GELU of the kernels (tanh form): g = h + h t, h = x / 2, t = tanh(x (c + c a x^2)); d = g'(x).
+constexpr float GC = 0.7978845608028654f, GA = 0.044715f, GCA = 0.7978845608028654f * 0.044715f;
 float gelu_d(float x, float &d) {
-  const float c = 0.7978845608028654f, a = 0.044715f;
   const float x2 = x * x;
-  const float u = c * (x + a * x2 * x);
-  const float t = std::tanh(u);
-  d = 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * c * (1.0f + 3.0f * a * x2);
-  return 0.5f * x * (1.0f + t);
+  const float t = std::tanh(x * std::fma(GCA, x2, GC));
+  const float h = 0.5f * x;
+  d = 0.5f * (1.0f + t) + h * (1.0f - t * t) * GC * (1.0f + 3.0f * GA * x2);
+  return std::fma(h, t, h);
 }
 
 }  // namespace
