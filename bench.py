@@ -478,6 +478,105 @@ def run_ours(args):
     return 0
 
 
+def roofline_of(sim, prof, peak, peak_kind):
+    """The dominant kernel class's achieved algorithmic bandwidth against the measured peak."""
+    from difffr_gb300._abi import KERNEL_CLASSES
+    dom = max(KERNEL_CLASSES, key=lambda k: prof[k]["ms"])
+    d = prof[dom]
+    avg_launch_s = d["ms"] / max(d["launches"], 1) / 1000.0
+    units = d["units"] / max(d["launches"], 1)
+    achieved = ALGO_BYTES.get(dom, 32) * units / avg_launch_s / 1e9
+    traffic = MEASURED_TRAFFIC[dom] * units if dom in MEASURED_TRAFFIC else None
+    return {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": traffic, "peak_kind": peak_kind, "algo_bytes_per_particle": ALGO_BYTES.get(dom, 32),
+            "avg_launch_us": avg_launch_s * 1e6}
+
+
+def run_basin(args):
+    """The full pipeline at 4M particles (200 x 100 x 200 lattice at r = 0.0025 m in a
+    1.2 x 0.8 x 1.2 m box, two R 0.03 m spheres colliding on the water, a static box): the
+    learned warm start is trained on the scene's own plain-solver samples (steps 40-59 of
+    seed 0), then K forward + adjoint steps with it (the leg's value: the gradient with
+    respect to the 12 initial velocities), K forward-only steps with it, and K forward +
+    adjoint steps with the reference warm start, all after W warm-up steps, CUDA events on
+    the context's stream; the dominant kernel's roofline from a profiled repeat."""
+    import numpy as np
+    from difffr_gb300 import _abi
+    from difffr_gb300 import scene as scn
+    from difffr_gb300.sim import DiffDFSPH
+    from difffr_gb300.warmstart import WarmStartModel, collect_samples, train
+    lib = _abi.load_library()
+    _abi.check(lib, lib.dfsph_set_device(0))
+    peak, peak_kind = load_peaks()
+    t0 = time.perf_counter()
+    sc0 = scn.billiards_on_water(seed=0, enable_gradient=0)
+    sim = DiffDFSPH(sc0)
+    sim.step(40)
+    x, y = collect_samples(sim, 20)
+    sim.close()
+    model = WarmStartModel(seed=0)
+    losses = train(model, x, y, epochs=2, batch=65536, lr=2e-3, lr_final=1e-4, seed=0)
+    training = {"samples": int(x.shape[0]), "epochs": 2, "final_loss": float(losses[-1]) if losses else None,
+                "wall_s": time.perf_counter() - t0}
+    del x, y
+
+    def leg(model_on, gradient):
+        s = DiffDFSPH(scn.billiards_on_water(seed=0, enable_gradient=1 if gradient else 0))
+        s.set_warmstart_model(model if model_on else None)
+        nb = s.n_bodies
+        dL = np.zeros((nb, 13))
+        dL[:, 0:3] = 1.0
+        for _ in range(args.warmup):
+            s.step(1)
+        s.reset_gradient()
+        s.synchronize()
+        s.record_event(0)
+        st = s.step(args.steps)
+        if gradient:
+            g = s.backward(dL)
+        s.record_event(1)
+        ms = s.event_elapsed_ms(0, 1)
+        out = {"steps_per_s": args.steps / (ms / 1000.0), "ms_per_step": ms / args.steps,
+               "pressure_iterations_per_step": st["total_pressure_iterations"] / args.steps}
+        if gradient:
+            out["gradient_finite"] = bool(np.all(np.isfinite(g)))
+            s.profile_enable(True)
+            s.step(args.steps)
+            prof = s.profile()
+            s.profile_enable(False)
+            out["roofline"] = roofline_of(s, prof, peak, peak_kind)
+            out["kernel_ms_per_step"] = {k: v["ms"] / args.steps for k, v in prof.items()}
+        s.set_warmstart_model(None)
+        s.close()
+        return out
+
+    clocks = ClockSampler(0)
+    clocks.start()
+    learned = leg(True, True)
+    clk = clocks.stop()
+    fwd = leg(True, False)
+    plain = leg(False, True)
+    model.close()
+    line = {
+        "metric": METRIC, "value": learned["steps_per_s"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": learned["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lattice + sampled boundaries)",
+        "config": {"workload": args.config_name, "n_fluid": sc0.n_fluid, "n_boundary": sc0.n_boundary,
+                   "dt": sc0.params.time_step, "gradient": "12 initial velocity variables (2 spheres x (v, omega))",
+                   "warm_start": "learned, trained on this scene's steps 40-59 (seed 0)",
+                   "l2": "inputs larger than L2", "parallelism": "single GPU"},
+        "pressure_iterations_per_step": learned["pressure_iterations_per_step"],
+        "gradient_finite": learned["gradient_finite"],
+        "fwd_only_steps_per_s": fwd["steps_per_s"],
+        "plain_warm_start": {"fwd_adjoint_steps_per_s": plain["steps_per_s"],
+                             "pressure_iterations_per_step": plain["pressure_iterations_per_step"]},
+        "roofline": learned["roofline"], "kernel_ms_per_step": learned["kernel_ms_per_step"],
+        "warm_start_training": training, "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def contact_leg(args):
     """Forward + adjoint steps/s of the 1M dam break with two spheres in contact (the rigid
     contact solver and the gradient manager on), and the rigid-stream time that includes the
@@ -556,6 +655,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.config == 4:
+        return run_basin(args)
     return run_ours(args)
 
 

@@ -162,24 +162,31 @@ static __device__ __forceinline__ void mlp_layer1(const float *sw, const float f
 // staged by mlp_stage_small_paired)
 static __device__ __forceinline__ void mlp_layer1_paired(const float *sw, const float f[4], uint8_t *tile, int row,
                                                          int cols) {
-  const float2 *w1p = reinterpret_cast<const float2 *>(sw + MLP_SW_W1);
-  const float2 *b1p = reinterpret_cast<const float2 *>(sw + MLP_SW_B1);
+  // 16-byte shared-memory reads (the weights are the same for every thread: each read is
+  // one broadcast wavefront, four weights at a time)
+  const float4 *w1q = reinterpret_cast<const float4 *>(sw + MLP_SW_W1);
+  const float4 *b1q = reinterpret_cast<const float4 *>(sw + MLP_SW_B1);
   const float2 f0 = make_float2(f[0], f[0]), f1 = make_float2(f[1], f[1]), f2 = make_float2(f[2], f[2]),
                f3 = make_float2(f[3], f[3]);
 #pragma unroll
   for (int c = 0; c < MLP_H; c += 8) {
     float h[8];
 #pragma unroll
-    for (int u = 0; u < 8; u += 2) {
-      const int p = (c + u) >> 1;
-      float2 z = b1p[p];
-      z = fma2(w1p[4 * p + 0], f0, z);
-      z = fma2(w1p[4 * p + 1], f1, z);
-      z = fma2(w1p[4 * p + 2], f2, z);
-      z = fma2(w1p[4 * p + 3], f3, z);
-      const float2 g = gelu2(z);
-      h[u] = g.x;
-      h[u + 1] = g.y;
+    for (int u = 0; u < 8; u += 4) {
+      const int p = (c + u) >> 1;  // even: pairs p and p + 1
+      const float4 bb = b1q[p >> 1];
+#pragma unroll
+      for (int e = 0; e < 2; e++) {
+        const float4 wa = w1q[2 * (p + e)], wb = w1q[2 * (p + e) + 1];
+        float2 z = e ? make_float2(bb.z, bb.w) : make_float2(bb.x, bb.y);
+        z = fma2(make_float2(wa.x, wa.y), f0, z);
+        z = fma2(make_float2(wa.z, wa.w), f1, z);
+        z = fma2(make_float2(wb.x, wb.y), f2, z);
+        z = fma2(make_float2(wb.z, wb.w), f3, z);
+        const float2 g = gelu2(z);
+        h[u + 2 * e] = g.x;
+        h[u + 2 * e + 1] = g.y;
+      }
     }
     st_row8(tile, row, c, cols, h);
   }
@@ -265,17 +272,18 @@ static __global__ void __launch_bounds__(MLP_THREADS) k_mlp_infer(MlpView mv, IO
     tc::fence_after_sync();
     // output layer: the even and odd hidden units summed in two packed partial sums
     float2 acc = make_float2(0.f, 0.f);
-    const float2 *b2p = reinterpret_cast<const float2 *>(sw + MLP_SW_B2);
-    const float2 *w3p = reinterpret_cast<const float2 *>(sw + MLP_SW_W3);
+    const float4 *b2q = reinterpret_cast<const float4 *>(sw + MLP_SW_B2);
+    const float4 *w3q = reinterpret_cast<const float4 *>(sw + MLP_SW_W3);
 #pragma unroll
     for (int c = 0; c < 64; c += 16) {
       float z[16];
       tc::tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c, z);
       tc::tmem_wait_ld();
 #pragma unroll
-      for (int u = 0; u < 16; u += 2) {
-        const int p = (c + u) >> 1;
-        acc = fma2(w3p[p], gelu2(add2(make_float2(z[u], z[u + 1]), b2p[p])), acc);
+      for (int u = 0; u < 16; u += 4) {
+        const float4 bb = b2q[(c + u) >> 2], ww = w3q[(c + u) >> 2];
+        acc = fma2(make_float2(ww.x, ww.y), gelu2(add2(make_float2(z[u], z[u + 1]), make_float2(bb.x, bb.y))), acc);
+        acc = fma2(make_float2(ww.z, ww.w), gelu2(add2(make_float2(z[u + 2], z[u + 3]), make_float2(bb.z, bb.w))), acc);
       }
     }
     const float out = sw[MLP_SW_B3] + (acc.x + acc.y);
