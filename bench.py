@@ -291,6 +291,19 @@ def run_reference(args):
     return 0
 
 
+def nvtx(name=None):
+    """Pushes (name given) or pops an NVTX range; a profiler's launch list can then select the
+    timed window (``ncu --nvtx --nvtx-include "timed_window/"``). Does nothing without NVTX."""
+    try:
+        import torch
+        if name is None:
+            torch.cuda.nvtx.range_pop()
+        else:
+            torch.cuda.nvtx.range_push(name)
+    except Exception:
+        pass
+
+
 def timed_fwd_adjoint(sim, steps, dL):
     """K forward steps with the pair Jacobians recorded, then the reverse sweep once; CUDA
     events on the context's stream. Returns (ms, step stats)."""
@@ -340,7 +353,9 @@ def run_ours(args):
     l0 = sim.launch_count()
     sim.synchronize()
     barrier(pg)
+    nvtx("timed_window")
     ms, st = timed_fwd_adjoint(sim, args.steps, dL)
+    nvtx()
     launches = sim.launch_count() - l0
     clk = clocks.stop()
     ms_max = allmax(pg, ms)

@@ -11,6 +11,7 @@ using dfsph::DfsphException;
 using dfsph::EngineBase;
 using dfsph::MlpView;
 using dfsph::mlp_view;
+using dfsph::mlp_sync_small;
 
 struct dfsph_ctx {
   EngineBase *engine;
@@ -150,6 +151,7 @@ int dfsph_step(dfsph_ctx *ctx, int32_t nsteps, dfsph_step_stats *stats) {
   return guard([&] {
     valid(ctx);
     if (ctx->mlp) {
+      mlp_sync_small(ctx->mlp);
       const MlpView v = mlp_view(ctx->mlp);  // the model's current weights and normalisation
       ctx->engine->set_warmstart_model(&v);
     }
@@ -397,6 +399,7 @@ int dfsph_set_warmstart_model(dfsph_ctx *ctx, dfsph_mlp *m) {
   return guard([&] {
     valid(ctx);
     if (m) {
+      mlp_sync_small(m);
       const MlpView v = mlp_view(m);
       ctx->engine->set_warmstart_model(&v);
     } else {

@@ -77,18 +77,21 @@ static __device__ __forceinline__ float2 add2(float2 a, float2 b) {
   asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
   return f2_of(d);
 }
-// gelu_f on a pair
-static __device__ __forceinline__ float2 gelu2(float2 x) {
-  const float2 u = mul2(x, fma2(make_float2(GELU_CA, GELU_CA), mul2(x, x), make_float2(GELU_C, GELU_C)));
+// gelu_f on a pair, from h = x / 2 (the inference kernel carries the halved pre-activations:
+// its W1, b1 and b2 are stored halved, which is exact). Every intermediate is an exact power-
+// of-two multiple of gelu_f's, so the result is bit-identical to gelu_f(x):
+// h^2 = x^2 / 4, 8 c a h^2 + 2 c = 2 (c a x^2 + c), u = h (2 (c + c a x^2)), g = h + h t.
+static __device__ __forceinline__ float2 gelu2_half(float2 h) {
+  const float2 u = mul2(h, fma2(make_float2(8.f * GELU_CA, 8.f * GELU_CA), mul2(h, h),
+                                make_float2(2.f * GELU_C, 2.f * GELU_C)));
   const float2 t = make_float2(tanh_approx(u.x), tanh_approx(u.y));
-  const float2 h = mul2(make_float2(0.5f, 0.5f), x);
   return fma2(h, t, h);
 }
 
+// two round-to-nearest BF16 conversions in one packed instruction (lo in the low half)
 static __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
-  const uint32_t l = __bfloat16_as_ushort(__float2bfloat16_rn(lo));
-  const uint32_t h = __bfloat16_as_ushort(__float2bfloat16_rn(hi));
-  return l | (h << 16);
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t *>(&v);
 }
 // store 8 consecutive columns (c0 multiple of 8) of row `row` of a core-matrix tile
 static __device__ __forceinline__ void st_row8(uint8_t *tile, int row, int c0, int cols, const float *v) {
@@ -104,23 +107,9 @@ static __device__ __forceinline__ uint8_t *align1024(uint8_t *p) {
   return reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
 }
 
-// Small weights in shared memory: W1 (256), b1 (64), b2 (64), w3 (64), b3 (1). The inference
-// kernel keeps W1 in unit pairs instead: float2 {W1[2p][k], W1[2p+1][k]} at 8 p + 2 k.
+// Small weights of the training kernel in shared memory: W1 (256), b1 (64), b2 (64), w3 (64),
+// b3 (1). (The inference kernel reads them from its parameter block, MlpView::small.)
 constexpr int MLP_SW_W1 = 0, MLP_SW_B1 = 256, MLP_SW_B2 = 320, MLP_SW_W3 = 384, MLP_SW_B3 = 448, MLP_SW_N = 452;
-
-static __device__ __forceinline__ void mlp_stage_small_paired(const float *wuse, float *sw) {
-  for (int k = threadIdx.x; k < MLP_SW_N; k += blockDim.x) {
-    float v = 0.f;
-    if (k < MLP_SW_B1) {
-      const int p = k >> 3, kk = (k >> 1) & 3, odd = k & 1;  // W1 pair p, input kk, unit 2p + odd
-      v = wuse[MLP_OFF_W1 + 4 * (2 * p + odd) + kk];
-    } else if (k < MLP_SW_B2) v = wuse[k];                          // b1
-    else if (k < MLP_SW_W3) v = wuse[MLP_OFF_B2 + (k - MLP_SW_B2)];  // b2
-    else if (k < MLP_SW_B3) v = wuse[MLP_OFF_W3 + (k - MLP_SW_W3)];  // w3
-    else if (k == MLP_SW_B3) v = wuse[MLP_OFF_B3];
-    sw[k] = v;
-  }
-}
 
 static __device__ __forceinline__ void mlp_stage_small(const float *wuse, float *sw) {
   for (int k = threadIdx.x; k < MLP_SW_N; k += blockDim.x) {
@@ -133,60 +122,28 @@ static __device__ __forceinline__ void mlp_stage_small(const float *wuse, float 
   }
 }
 
-// hidden layer 1 for one particle: h1 (64, to the tile row as BF16) and optionally
-// gelu'(z1) into g1d
-template <bool DERIV>
-static __device__ __forceinline__ void mlp_layer1(const float *sw, const float f[4], uint8_t *tile, int row, int cols,
-                                                  float *g1d) {
-#pragma unroll
-  for (int c = 0; c < MLP_H; c += 8) {
-    float h[8];
-#pragma unroll
-    for (int u = 0; u < 8; u++) {
-      const int j = c + u;
-      const float *w = sw + MLP_SW_W1 + 4 * j;
-      const float z = sw[MLP_SW_B1 + j] + w[0] * f[0] + w[1] * f[1] + w[2] * f[2] + w[3] * f[3];
-      if (DERIV) {
-        float d;
-        h[u] = gelu_d(z, d);
-        g1d[j] = d;
-      } else {
-        h[u] = gelu_f(z);
-      }
-    }
-    st_row8(tile, row, c, cols, h);
-  }
-}
-
-// hidden layer 1 of the inference kernel, two units per packed operation (W1 paired as
-// staged by mlp_stage_small_paired)
-static __device__ __forceinline__ void mlp_layer1_paired(const float *sw, const float f[4], uint8_t *tile, int row,
+// hidden layer 1 of the inference kernel, two units per packed operation; the weights come
+// from the kernel's parameter block (every index is a compile-time constant after
+// unrolling, so each read is a constant-bank operand), W1 and b1 halved, so z holds the
+// halved pre-activations gelu2_half takes
+static __device__ __forceinline__ void mlp_layer1_paired(const MlpView &mv, const float f[4], uint8_t *tile, int row,
                                                          int cols) {
-  // 16-byte shared-memory reads (the weights are the same for every thread: each read is
-  // one broadcast wavefront, four weights at a time)
-  const float4 *w1q = reinterpret_cast<const float4 *>(sw + MLP_SW_W1);
-  const float4 *b1q = reinterpret_cast<const float4 *>(sw + MLP_SW_B1);
   const float2 f0 = make_float2(f[0], f[0]), f1 = make_float2(f[1], f[1]), f2 = make_float2(f[2], f[2]),
                f3 = make_float2(f[3], f[3]);
 #pragma unroll
   for (int c = 0; c < MLP_H; c += 8) {
     float h[8];
 #pragma unroll
-    for (int u = 0; u < 8; u += 4) {
-      const int p = (c + u) >> 1;  // even: pairs p and p + 1
-      const float4 bb = b1q[p >> 1];
-#pragma unroll
-      for (int e = 0; e < 2; e++) {
-        const float4 wa = w1q[2 * (p + e)], wb = w1q[2 * (p + e) + 1];
-        float2 z = e ? make_float2(bb.z, bb.w) : make_float2(bb.x, bb.y);
-        z = fma2(make_float2(wa.x, wa.y), f0, z);
-        z = fma2(make_float2(wa.z, wa.w), f1, z);
-        z = fma2(make_float2(wb.x, wb.y), f2, z);
-        z = fma2(make_float2(wb.z, wb.w), f3, z);
-        const float2 g = gelu2(z);
-        h[u + 2 * e] = g.x;
-        h[u + 2 * e + 1] = g.y;
-      }
+    for (int u = 0; u < 8; u += 2) {
+      const int p = (c + u) >> 1, w = MLP_SMALL_W1 + 8 * p;
+      float2 z = make_float2(mv.small[MLP_SMALL_B1 + c + u], mv.small[MLP_SMALL_B1 + c + u + 1]);
+      z = fma2(make_float2(mv.small[w + 0], mv.small[w + 1]), f0, z);
+      z = fma2(make_float2(mv.small[w + 2], mv.small[w + 3]), f1, z);
+      z = fma2(make_float2(mv.small[w + 4], mv.small[w + 5]), f2, z);
+      z = fma2(make_float2(mv.small[w + 6], mv.small[w + 7]), f3, z);
+      const float2 g = gelu2_half(z);
+      h[u] = g.x;
+      h[u + 1] = g.y;
     }
     st_row8(tile, row, c, cols, h);
   }
@@ -194,14 +151,15 @@ static __device__ __forceinline__ void mlp_layer1_paired(const float *sw, const 
 
 // ------------------------------------------------------------------ inference
 // Persistent over tiles of 128 particles: one thread per particle row. Shared memory:
-// W2 image 8 KB, the H1 tile 16 KB, small weights, one mbarrier; TMEM: 64 columns.
+// W2 image 8 KB, the H1 tile 16 KB, one mbarrier; TMEM: 64 columns. The small weights are
+// read from the parameter block.
 // IO supplies `bool load(int i, float f[4])` (false: no prediction wanted for i) and
 // `void store(int i, float y)`.
-// 8192 (W2) + 16384 (H1 tile) + 1808 (small weights) + 16 (barrier, TMEM address) + 1008
-// (alignment) bytes. At 27 KB at most 8 CTAs fit on an SM, and 8 x 64 TMEM columns is
-// exactly the SM's 512, so no CTA waits in tcgen05.alloc.
+// 8192 (W2) + 16384 (H1 tile) + 16 (barrier, TMEM address) + 1008 (alignment) bytes, rounded
+// up to 27 KB: at most 8 CTAs fit on an SM, and 8 x 64 TMEM columns is exactly the SM's 512,
+// so no CTA waits in tcgen05.alloc.
 constexpr int MLP_INFER_SMEM = 27 * 1024;
-static_assert(8192 + 16384 + MLP_SW_N * 4 + 16 + 1008 <= MLP_INFER_SMEM, "inference tile layout fits");
+static_assert(8192 + 16384 + 16 + 1008 <= MLP_INFER_SMEM, "inference tile layout fits");
 static_assert((228 * 1024) / (MLP_INFER_SMEM + 1024) <= 8, "at most 8 CTAs (512 TMEM columns) per SM");
 
 template <class IO>
@@ -210,14 +168,18 @@ static __global__ void __launch_bounds__(MLP_THREADS) k_mlp_infer(MlpView mv, IO
   uint8_t *base = align1024(mlp_smem_raw);
   uint8_t *sW2 = base;                   // 8192 B
   uint8_t *sH1 = base + 8192;            // 16384 B: 128 rows x 64 cols
-  float *sw = reinterpret_cast<float *>(base + 8192 + 16384);
-  uint64_t *bar = reinterpret_cast<uint64_t *>(sw + MLP_SW_N);
+  uint64_t *bar = reinterpret_cast<uint64_t *>(base + 8192 + 16384);
   uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 1);
   const int tid = threadIdx.x, warp = tid >> 5;
 
-  for (int k = tid; k < 8192 / 16; k += MLP_THREADS)
-    reinterpret_cast<uint4 *>(sW2)[k] = reinterpret_cast<const uint4 *>(mv.w2img)[k];
-  mlp_stage_small_paired(mv.wuse, sw);
+  {
+    static_assert(MLP_THREADS == 128, "staging assumes 128 threads");
+    uint4 t[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) t[j] = reinterpret_cast<const uint4 *>(mv.w2img)[tid + 128 * j];
+#pragma unroll
+    for (int j = 0; j < 4; j++) reinterpret_cast<uint4 *>(sW2)[tid + 128 * j] = t[j];
+  }
   if (tid == 0) {
     tc::mbar_init(bar, 1);
     tc::fence_mbar_init();
@@ -240,14 +202,17 @@ static __global__ void __launch_bounds__(MLP_THREADS) k_mlp_infer(MlpView mv, IO
   const int ntiles = (n + MLP_TILE - 1) / MLP_TILE;
   uint32_t phase = 0;
   bool pending = false;
+  // the features of the CTA's next tile are loaded while the current tile's product runs
+  float fn[4] = {0.f, 0.f, 0.f, 0.f};
+  bool wantn = false;
+  if (blockIdx.x < ntiles && (int)blockIdx.x * MLP_TILE + tid < n) wantn = io.load(blockIdx.x * MLP_TILE + tid, fn);
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int i = tile * MLP_TILE + tid;
-    float f[4] = {0.f, 0.f, 0.f, 0.f};
-    bool want = false;
-    if (i < n) want = io.load(i, f);
+    float f[4];
+    const bool want = wantn;
 #pragma unroll
-    for (int k = 0; k < 4; k++) f[k] = (f[k] - xm[k]) * xi[k];
-    mlp_layer1_paired(sw, f, sH1, tid, 64);
+    for (int k = 0; k < 4; k++) f[k] = (fn[k] - xm[k]) * xi[k];
+    mlp_layer1_paired(mv, f, sH1, tid, 64);
     tc::fence_async_smem();
     tc::fence_before_sync();
     __syncthreads();
@@ -260,40 +225,49 @@ static __global__ void __launch_bounds__(MLP_THREADS) k_mlp_infer(MlpView mv, IO
       tc::mma_commit(bar);
     }
     pending = true;
+    {
+      const int64_t inext = (int64_t)(tile + (int)gridDim.x) * MLP_TILE + tid;
+      wantn = false;
+#pragma unroll
+      for (int k = 0; k < 4; k++) fn[k] = 0.f;
+      if (inext < n) wantn = io.load((int)inext, fn);
+    }
     // the first wait may be given fewer polls (a test of the failure path below); the wait
     // for the product still in flight after a failure always has the regular limit
     const uint32_t lim = (tile == (int)blockIdx.x && mv.first_wait_polls >= 0) ? (uint32_t)mv.first_wait_polls
                                                                               : MLP_WAIT_LIMIT;
-    bool ok = tc::mbar_wait(bar, phase, lim);
-    ok = __syncthreads_and(ok) != 0;
+    // one thread polls the barrier (every poll is a shared-memory access), the block follows
+    const bool ok = __syncthreads_and(tid == 0 ? tc::mbar_wait(bar, phase, lim) : true) != 0;
     if (!ok) break;
     pending = false;
     phase ^= 1u;
     tc::fence_after_sync();
     // output layer: the even and odd hidden units summed in two packed partial sums
     float2 acc = make_float2(0.f, 0.f);
-    const float4 *b2q = reinterpret_cast<const float4 *>(sw + MLP_SW_B2);
-    const float4 *w3q = reinterpret_cast<const float4 *>(sw + MLP_SW_W3);
 #pragma unroll
     for (int c = 0; c < 64; c += 16) {
       float z[16];
       tc::tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c, z);
       tc::tmem_wait_ld();
 #pragma unroll
-      for (int u = 0; u < 16; u += 4) {
-        const float4 bb = b2q[(c + u) >> 2], ww = w3q[(c + u) >> 2];
-        acc = fma2(make_float2(ww.x, ww.y), gelu2(add2(make_float2(z[u], z[u + 1]), make_float2(bb.x, bb.y))), acc);
-        acc = fma2(make_float2(ww.z, ww.w), gelu2(add2(make_float2(z[u + 2], z[u + 3]), make_float2(bb.z, bb.w))), acc);
+      for (int u = 0; u < 16; u += 2) {
+        const int j = c + u;
+        // (z + b2) / 2 in one rounding: fma(1/2, z, b2 / 2) with b2 stored halved
+        const float2 b = make_float2(mv.small[MLP_SMALL_B2 + j], mv.small[MLP_SMALL_B2 + j + 1]);
+        const float2 w = make_float2(mv.small[MLP_SMALL_W3 + j], mv.small[MLP_SMALL_W3 + j + 1]);
+        acc = fma2(w, gelu2_half(fma2(make_float2(0.5f, 0.5f), make_float2(z[u], z[u + 1]), b)), acc);
       }
     }
-    const float out = sw[MLP_SW_B3] + (acc.x + acc.y);
+    const float out = mv.small[MLP_SMALL_B3] + (acc.x + acc.y);
     if (want) io.store(i, out * ys + ym);
     tc::fence_before_sync();
   }
   if (pending) {
     // an MMA may still be in flight: record the failure, give it a bounded wait, then free TMEM
-    if (tid == 0) atomicOr(err, errbit);
-    tc::mbar_wait(bar, phase, MLP_WAIT_LIMIT);
+    if (tid == 0) {
+      atomicOr(err, errbit);
+      tc::mbar_wait(bar, phase, MLP_WAIT_LIMIT);
+    }
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -314,20 +288,28 @@ struct MlpArrayIO {
 };
 
 // ------------------------------------------------------------------ training
-// One CTA per SM, persistent over the batch's tiles. Per tile (thread p = particle row):
-//   forward:   z1 = W1 f + b1, h1 = gelu(z1)           (per thread, FP32)
+// One CTA of 1024 threads per SM, persistent over the batch's tiles of 128 samples. Warp w
+// reaches TMEM lanes 32 (w % 4) .. + 31, so the sample row is r = 32 (w % 4) + lane and the
+// CTA's 32 warps form 8 column groups g = w / 4: the 8 threads of a row each take 8 of the
+// 64 hidden units, [8 g, 8 g + 8). Per tile:
+//   forward:   z1 = W1 f + b1, h1 = gelu(z1)           (per thread, its 8 units, FP32)
 //              Z2 = H1 W2^T                             (MMA1, M=128 N=64 K=64)
-//              h2 = gelu(z2 + b2), y = w3 . h2 + b3     (per thread)
+//              h2 = gelu(z2 + b2), y = w3 . h2 + b3     (per thread its 8 units; the 8
+//                                                        partial dot products summed per row
+//                                                        through shared memory, fixed order)
 //   backward:  e = y - target, dz2 = e w3 gelu'(z2)
 //              DH1 = DZ2 W2                             (MMA2, M=128 N=64 K=64)
 //              GW2 += DZ2^T [H1 | 1]                    (MMA3, M=128 N=80 K=128: dW2 and db2)
 //              GW3 += [H2 | 1]^T e                      (MMA5, M=128 N=16 K=128: dw3 and db3)
 //              dz1 = dh1 gelu'(z1)
 //              GW1 += DZ1^T [F | 1]                     (MMA4, M=128 N=16 K=128: dW1 and db1)
-// The weight-gradient products read the per-particle tiles as MN-major operands, so every
-// thread writes only its own row. Rows 64..127 of the M dimension are zero padding
+// The weight-gradient products read the per-sample tiles as MN-major operands, so every
+// thread writes only its own row segment. Rows 64..127 of the M dimension are zero padding
 // (M = 128 keeps row r of D in TMEM lane r). At the end the CTA writes its gradient
 // partial sums (unscaled) and its loss partial; k_mlp_adam reduces them in fixed order.
+constexpr int MLP_TRAIN_THREADS = 1024;
+constexpr int MLP_TRAIN_GROUPS = MLP_TRAIN_THREADS / MLP_TILE;  // 8 column groups of 8 units
+static_assert(MLP_TRAIN_GROUPS * 8 == MLP_H, "8 units per column group");
 namespace mlptrain {
 constexpr int SW2 = 0;                      // W2 image, 64 x 64
 constexpr int SH1 = SW2 + 8192;             // 128 x 80  (col 64 = 1)
@@ -337,7 +319,8 @@ constexpr int SDZ1 = SH2 + 128 * 128 * 2;   // 128 x 128 (cols 64.. = 0)
 constexpr int SFX = SDZ1 + 128 * 128 * 2;   // 128 x 16  (cols 0..3 features, col 4 = 1)
 constexpr int SDO = SFX + 128 * 16 * 2;     // 128 x 16  (col 0 = error)
 constexpr int SSW = SDO + 128 * 16 * 2;     // small weights
-constexpr int SBAR = SSW + MLP_SW_N * 4;    // mbarrier
+constexpr int SRED = SSW + MLP_SW_N * 4;    // output-layer partial sums [group][row], FP32
+constexpr int SBAR = SRED + MLP_TRAIN_GROUPS * MLP_TILE * 4;  // mbarrier, TMEM address
 constexpr int SEND = SBAR + 16;
 // The dynamic allocation is padded far beyond SEND so that every operand read of every
 // MMA stays inside it even if the descriptor's two byte offsets were read the other way
@@ -345,32 +328,54 @@ constexpr int SEND = SBAR + 16;
 constexpr int SMEM = 225 * 1024;
 static_assert(SDZ1 + 15 * 2048 + 7 * 4096 + 128 * 2 + 128 < SMEM - 1024, "operand reads stay in the allocation");
 static_assert(SEND < SMEM - 1024, "layout fits");
+static_assert(SRED % 16 == 0 && SBAR % 8 == 0, "aligned regions");
 // TMEM columns
 constexpr uint32_t TZ2 = 0, TDH1 = 64, TGW2 = 128, TGW1 = 208, TGW3 = 224, TCOLS = 256;
 }  // namespace mlptrain
 
-static __global__ void __launch_bounds__(MLP_THREADS, 1)
+// hidden layer 1 for one sample row, units [c0, c0 + 8): h1 to the tile row as BF16,
+// gelu'(z1) into g1d
+static __device__ __forceinline__ void mlp_layer1_cols8(const float *sw, const float f[4], uint8_t *tile, int row,
+                                                        int cols, int c0, float g1d[8]) {
+  float h[8];
+#pragma unroll
+  for (int u = 0; u < 8; u++) {
+    const int j = c0 + u;
+    const float *w = sw + MLP_SW_W1 + 4 * j;
+    const float z = sw[MLP_SW_B1 + j] + w[0] * f[0] + w[1] * f[1] + w[2] * f[2] + w[3] * f[3];
+    float d;
+    h[u] = gelu_d(z, d);
+    g1d[u] = d;
+  }
+  st_row8(tile, row, c0, cols, h);
+}
+
+static __global__ void __launch_bounds__(MLP_TRAIN_THREADS, 1)
     k_mlp_train(MlpView mv, const float *__restrict__ x, const float *__restrict__ y, const int *__restrict__ idx, int n,
                 int nsrc, float *__restrict__ gpart, double *__restrict__ lpart, int *err) {
   using namespace mlptrain;
   extern __shared__ uint8_t mlp_smem_raw[];
   uint8_t *base = align1024(mlp_smem_raw);
   float *sw = reinterpret_cast<float *>(base + SSW);
+  float *red = reinterpret_cast<float *>(base + SRED);
   uint64_t *bar = reinterpret_cast<uint64_t *>(base + SBAR);
   uint32_t *tslot = reinterpret_cast<uint32_t *>(base + SBAR + 8);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int row = 32 * (warp & 3) + lane;  // the sample row (TMEM lane) of this thread
+  const int grp = warp >> 2, c0 = 8 * grp;  // its column group and first hidden unit
 
   // constant parts of the tiles: zeros, and the constant-1 columns
-  for (int k = tid; k < (SSW - SH1) / 16; k += MLP_THREADS) reinterpret_cast<uint4 *>(base + SH1)[k] = make_uint4(0, 0, 0, 0);
-  for (int k = tid; k < 8192 / 16; k += MLP_THREADS)
+  for (int k = tid; k < (SSW - SH1) / 16; k += MLP_TRAIN_THREADS)
+    reinterpret_cast<uint4 *>(base + SH1)[k] = make_uint4(0, 0, 0, 0);
+  for (int k = tid; k < 8192 / 16; k += MLP_TRAIN_THREADS)
     reinterpret_cast<uint4 *>(base + SW2)[k] = reinterpret_cast<const uint4 *>(mv.w2img)[k];
   mlp_stage_small(mv.wuse, sw);
   __syncthreads();
-  {
+  if (grp == 0) {
     const uint16_t one = __bfloat16_as_ushort(__float2bfloat16_rn(1.0f));
-    *reinterpret_cast<uint16_t *>(base + SH1 + tc::cm_offset(tid, 64, 80)) = one;
-    *reinterpret_cast<uint16_t *>(base + SH2 + tc::cm_offset(tid, 64, 128)) = one;
-    *reinterpret_cast<uint16_t *>(base + SFX + tc::cm_offset(tid, 4, 16)) = one;
+    *reinterpret_cast<uint16_t *>(base + SH1 + tc::cm_offset(row, 64, 80)) = one;
+    *reinterpret_cast<uint16_t *>(base + SH2 + tc::cm_offset(row, 64, 128)) = one;
+    *reinterpret_cast<uint16_t *>(base + SFX + tc::cm_offset(row, 4, 16)) = one;
   }
   if (tid == 0) {
     tc::mbar_init(bar, 1);
@@ -385,7 +390,7 @@ static __global__ void __launch_bounds__(MLP_THREADS, 1)
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = *tslot;
-  const uint32_t lane_off = (uint32_t)(32 * warp) << 16;
+  const uint32_t lane_off = (uint32_t)(32 * (warp & 3)) << 16;
   const uint32_t sb = tc::smem_u32(base);
   float xm[4], xi[4];
 #pragma unroll
@@ -398,14 +403,14 @@ static __global__ void __launch_bounds__(MLP_THREADS, 1)
   int it = 0;
   double loss = 0.0;
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
-    const int r = tile * MLP_TILE + tid;
+    const int r = tile * MLP_TILE + row;
     bool valid = r < n;
     float f[4] = {0.f, 0.f, 0.f, 0.f}, yn = 0.f;
     int s = r;
     if (valid && idx) {
       s = idx[r];
       if (s < 0 || s >= nsrc) {  // an index outside the sample arrays: flag it, skip the sample
-        atomicOr(err, 2);
+        if (grp == 0) atomicOr(err, 2);
         valid = false;
       }
     }
@@ -415,11 +420,11 @@ static __global__ void __launch_bounds__(MLP_THREADS, 1)
       f[2] = (v.z - xm[2]) * xi[2]; f[3] = (v.w - xm[3]) * xi[3];
       yn = (y[s] - ym) * yi;
     }
-    float g1d[MLP_H];
-    mlp_layer1<true>(sw, f, base + SH1, tid, 80, g1d);
-    {
+    float g1d[8];
+    mlp_layer1_cols8(sw, f, base + SH1, row, 80, c0, g1d);
+    if (grp == 0) {
       const float fr[8] = {f[0], f[1], f[2], f[3], 1.0f, 0.f, 0.f, 0.f};
-      st_row8(base + SFX, tid, 0, 16, fr);
+      st_row8(base + SFX, row, 0, 16, fr);
     }
     // ---- MMA1: Z2 = H1 W2^T
     tc::fence_async_smem();
@@ -435,45 +440,40 @@ static __global__ void __launch_bounds__(MLP_THREADS, 1)
       tc::mma_commit(bar);
     }
     pending = true;
-    if (!__syncthreads_and(tc::mbar_wait(bar, phase, MLP_WAIT_LIMIT))) { failed = true; break; }
+    if (!__syncthreads_and(tid == 0 ? tc::mbar_wait(bar, phase, MLP_WAIT_LIMIT) : true)) { failed = true; break; }
     pending = false;
     phase ^= 1u;
     tc::fence_after_sync();
-    // ---- output layer, error, dz2
-    float z2[MLP_H];
-#pragma unroll
-    for (int c = 0; c < MLP_H; c += 16) {
-      float t[16];
-      tc::tmem_ld16(tmem + lane_off + TZ2 + (uint32_t)c, t);
+    // ---- output layer (this thread's 8 units), error, dz2
+    float d2[8];
+    {
+      float t[8];
+      tc::tmem_ld8(tmem + lane_off + TZ2 + (uint32_t)c0, t);
       tc::tmem_wait_ld();
-#pragma unroll
-      for (int u = 0; u < 16; u++) z2[c + u] = t[u];
-    }
-    float out = sw[MLP_SW_B3];
-#pragma unroll
-    for (int c = 0; c < MLP_H; c += 8) {
-      float h[8];
+      float h[8], part = 0.f;
 #pragma unroll
       for (int u = 0; u < 8; u++) {
-        float d;
-        h[u] = gelu_d(z2[c + u] + sw[MLP_SW_B2 + c + u], d);
-        out += sw[MLP_SW_W3 + c + u] * h[u];
-        z2[c + u] = d;  // keep gelu'(z2)
+        h[u] = gelu_d(t[u] + sw[MLP_SW_B2 + c0 + u], d2[u]);
+        part += sw[MLP_SW_W3 + c0 + u] * h[u];
       }
-      st_row8(base + SH2, tid, c, 128, h);
+      st_row8(base + SH2, row, c0, 128, h);
+      red[grp * MLP_TILE + row] = part;
     }
-    const float e = valid ? out - yn : 0.f;
-    loss += (double)e * (double)e;
-    {
-      const float er[8] = {e, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-      st_row8(base + SDO, tid, 0, 16, er);
-    }
+    __syncthreads();
+    float out = sw[MLP_SW_B3];
 #pragma unroll
-    for (int c = 0; c < MLP_H; c += 8) {
+    for (int g = 0; g < MLP_TRAIN_GROUPS; g++) out += red[g * MLP_TILE + row];
+    const float e = valid ? out - yn : 0.f;
+    if (grp == 0) {
+      loss += (double)e * (double)e;
+      const float er[8] = {e, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      st_row8(base + SDO, row, 0, 16, er);
+    }
+    {
       float d[8];
 #pragma unroll
-      for (int u = 0; u < 8; u++) d[u] = e * sw[MLP_SW_W3 + c + u] * z2[c + u];
-      st_row8(base + SDZ2, tid, c, 128, d);
+      for (int u = 0; u < 8; u++) d[u] = e * sw[MLP_SW_W3 + c0 + u] * d2[u];
+      st_row8(base + SDZ2, row, c0, 128, d);
     }
     // ---- MMA2 (DH1 = DZ2 W2), MMA3 (GW2 += DZ2^T [H1|1]), MMA5 (GW3 += [H2|1]^T e)
     tc::fence_async_smem();
@@ -499,24 +499,18 @@ static __global__ void __launch_bounds__(MLP_THREADS, 1)
       tc::mma_commit(bar);
     }
     pending = true;
-    if (!__syncthreads_and(tc::mbar_wait(bar, phase, MLP_WAIT_LIMIT))) { failed = true; break; }
+    if (!__syncthreads_and(tid == 0 ? tc::mbar_wait(bar, phase, MLP_WAIT_LIMIT) : true)) { failed = true; break; }
     pending = false;
     phase ^= 1u;
     tc::fence_after_sync();
-    // ---- dz1 = dh1 gelu'(z1)
-#pragma unroll
-    for (int c = 0; c < MLP_H; c += 16) {
-      float t[16];
-      tc::tmem_ld16(tmem + lane_off + TDH1 + (uint32_t)c, t);
+    // ---- dz1 = dh1 gelu'(z1) (this thread's 8 units)
+    {
+      float t[8], a[8];
+      tc::tmem_ld8(tmem + lane_off + TDH1 + (uint32_t)c0, t);
       tc::tmem_wait_ld();
-      float a[8], b[8];
 #pragma unroll
-      for (int u = 0; u < 8; u++) {
-        a[u] = valid ? t[u] * g1d[c + u] : 0.f;
-        b[u] = valid ? t[8 + u] * g1d[c + 8 + u] : 0.f;
-      }
-      st_row8(base + SDZ1, tid, c, 128, a);
-      st_row8(base + SDZ1, tid, c + 8, 128, b);
+      for (int u = 0; u < 8; u++) a[u] = valid ? t[u] * g1d[u] : 0.f;
+      st_row8(base + SDZ1, row, c0, 128, a);
     }
     // ---- MMA4: GW1 += DZ1^T [F|1]
     tc::fence_async_smem();
@@ -532,48 +526,48 @@ static __global__ void __launch_bounds__(MLP_THREADS, 1)
       tc::mma_commit(bar);
     }
     pending = true;
-    if (!__syncthreads_and(tc::mbar_wait(bar, phase, MLP_WAIT_LIMIT))) { failed = true; break; }
+    if (!__syncthreads_and(tid == 0 ? tc::mbar_wait(bar, phase, MLP_WAIT_LIMIT) : true)) { failed = true; break; }
     pending = false;
     phase ^= 1u;
     tc::fence_after_sync();
   }
   if (failed) {
     if (tid == 0) atomicOr(err, 1);
-    if (pending) tc::mbar_wait(bar, phase, MLP_WAIT_LIMIT);
+    if (pending && tid == 0) tc::mbar_wait(bar, phase, MLP_WAIT_LIMIT);
   }
-  // ---- gradient partials of this CTA
+  // ---- gradient partials of this CTA: D rows 0..64 sit in TMEM lanes 0..64 (warps with
+  // w % 4 = 0, 1 and lane 0 of w % 4 = 2); the column groups split the columns
   float *gp = gpart + (size_t)blockIdx.x * MLP_NPARAMS;
+  const int q = warp & 3;
   if (it == 0 || failed) {
-    for (int k = tid; k < MLP_NPARAMS; k += MLP_THREADS) gp[k] = 0.f;
-  } else if (warp < 3) {
-    const int row = 32 * warp + lane;
-    if (warp < 2) {
-      for (int c = 0; c < 80; c += 16) {
-        float t[16];
-        tc::tmem_ld16(tmem + lane_off + TGW2 + (uint32_t)c, t);
-        tc::tmem_wait_ld();
-#pragma unroll
-        for (int u = 0; u < 16; u++) {
-          const int col = c + u;
-          if (col < 64) gp[MLP_OFF_W2 + row * 64 + col] = t[u];
-          else if (col == 64) gp[MLP_OFF_B2 + row] = t[u];
-        }
-      }
-      float t[16];
-      tc::tmem_ld16(tmem + lane_off + TGW1, t);
-      tc::tmem_wait_ld();
-#pragma unroll
-      for (int k = 0; k < 4; k++) gp[MLP_OFF_W1 + row * 4 + k] = t[k];
-      gp[MLP_OFF_B1 + row] = t[4];
-    }
+    for (int k = tid; k < MLP_NPARAMS; k += MLP_TRAIN_THREADS) gp[k] = 0.f;
+  } else if (q < 2 && grp < 5) {
+    // GW2: 80 columns (W2 row `row`, then b2 in column 64), 16 per group
     float t[16];
-    tc::tmem_ld16(tmem + lane_off + TGW3, t);
+    tc::tmem_ld16(tmem + lane_off + TGW2 + (uint32_t)(16 * grp), t);
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int u = 0; u < 16; u++) {
+      const int col = 16 * grp + u;
+      if (col < 64) gp[MLP_OFF_W2 + row * 64 + col] = t[u];
+      else if (col == 64) gp[MLP_OFF_B2 + row] = t[u];
+    }
+  } else if (q < 2 && grp == 5) {
+    float t[8];
+    tc::tmem_ld8(tmem + lane_off + TGW1, t);
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int k = 0; k < 4; k++) gp[MLP_OFF_W1 + row * 4 + k] = t[k];
+    gp[MLP_OFF_B1 + row] = t[4];
+  } else if (q < 3 && grp == 6) {
+    float t[8];
+    tc::tmem_ld8(tmem + lane_off + TGW3, t);
     tc::tmem_wait_ld();
     if (row < 64) gp[MLP_OFF_W3 + row] = t[0];
     else if (row == 64) gp[MLP_OFF_B3] = t[0];
   }
-  // ---- loss partial (fixed order)
-  __shared__ double lred[MLP_THREADS / 32];
+  // ---- loss partial (fixed order; only column group 0 holds the rows' losses)
+  __shared__ double lred[MLP_TRAIN_THREADS / 32];
   for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
   if (lane == 0) lred[warp] = loss;
   tc::fence_before_sync();
@@ -581,7 +575,7 @@ static __global__ void __launch_bounds__(MLP_THREADS, 1)
   tc::fence_after_sync();
   if (tid == 0) {
     double s = 0.0;
-    for (int w = 0; w < MLP_THREADS / 32; w++) s += lred[w];
+    for (int w = 0; w < MLP_TRAIN_THREADS / 32; w++) s += lred[w];
     lpart[blockIdx.x] = s;
   }
   if (warp == 0) tc::tmem_dealloc(tmem, TCOLS);

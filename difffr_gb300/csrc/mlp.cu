@@ -27,6 +27,8 @@ struct dfsph_mlp {
   float norm[dfsph::MLP_NNORM] = {0, 0, 0, 0, 1, 1, 1, 1, 0, 1};
   int64_t adam_t = 0;
   int first_wait_polls = -1;
+  float small[dfsph::MLP_SMALL_N] = {};  // host copy of the inference kernel's small weights
+  bool small_stale = true;               // set whenever the device weights change
 };
 
 namespace dfsph {
@@ -38,6 +40,7 @@ MlpView mlp_view(const dfsph_mlp *m) {
   std::memcpy(v.norm, m->norm, sizeof(v.norm));
   v.device = m->device;
   v.first_wait_polls = m->first_wait_polls;
+  std::memcpy(v.small, m->small, sizeof(v.small));
   return v;
 }
 
@@ -96,6 +99,7 @@ void refresh(dfsph_mlp *m, float lr, bool with_grad, float scale, int nparts) {
   k_mlp_adam<<<(MLP_NPARAMS + 255) / 256, 256, 0, m->stream>>>(nparts, m->gpart, scale, with_grad ? m->grad : nullptr,
                                                               m->master, m->m1, m->m2, m->wuse, m->w2img, lr, b1c, b2c);
   DF_CK(cudaGetLastError());
+  m->small_stale = true;
 }
 
 void upload_params(dfsph_mlp *m, const float *params) {
@@ -117,7 +121,7 @@ double run_train_kernel(dfsph_mlp *m, const float *x, const float *y, const int 
   const int ntiles = (int)((n + MLP_TILE - 1) / MLP_TILE);
   const int grid = std::min(ntiles, m->nparts);
   DF_CK(cudaMemsetAsync(m->err, 0, sizeof(int), m->stream));
-  k_mlp_train<<<grid, MLP_THREADS, mlptrain::SMEM, m->stream>>>(mlp_view(m), x, y, idx, (int)n, (int)nsrc, m->gpart,
+  k_mlp_train<<<grid, MLP_TRAIN_THREADS, mlptrain::SMEM, m->stream>>>(mlp_view(m), x, y, idx, (int)n, (int)nsrc, m->gpart,
                                                                  m->lpart, m->err);
   DF_CK(cudaGetLastError());
   std::vector<double> lp(grid);
@@ -133,6 +137,26 @@ double run_train_kernel(dfsph_mlp *m, const float *x, const float *y, const int 
 }
 
 }  // namespace
+
+void mlp_sync_small(dfsph_mlp *m) {
+  if (!m->small_stale) return;
+  DeviceScope ds(m->device);
+  std::vector<float> w(MLP_NPARAMS);
+  DF_CK(cudaMemcpyAsync(w.data(), m->wuse, MLP_NPARAMS * sizeof(float), cudaMemcpyDeviceToHost, m->stream));
+  DF_CK(cudaStreamSynchronize(m->stream));
+  for (int p = 0; p < MLP_H / 2; p++)
+    for (int k = 0; k < MLP_IN; k++)
+      for (int odd = 0; odd < 2; odd++)
+        m->small[MLP_SMALL_W1 + 8 * p + 2 * k + odd] = 0.5f * w[MLP_OFF_W1 + MLP_IN * (2 * p + odd) + k];
+  for (int j = 0; j < MLP_H; j++) {
+    m->small[MLP_SMALL_B1 + j] = 0.5f * w[MLP_OFF_B1 + j];
+    m->small[MLP_SMALL_B2 + j] = 0.5f * w[MLP_OFF_B2 + j];
+    m->small[MLP_SMALL_W3 + j] = w[MLP_OFF_W3 + j];
+  }
+  m->small[MLP_SMALL_B3] = w[MLP_OFF_B3];
+  m->small_stale = false;
+}
+
 }  // namespace dfsph
 
 using namespace dfsph;
@@ -293,11 +317,18 @@ int dfsph_mlp_gradient(dfsph_mlp *m, const float *x, const float *y, int64_t n, 
 int dfsph_mlp_predict(dfsph_mlp *m, const float *x, float *y, int64_t n) {
   return guard_mlp([&] {
     if (!m) throw DfsphException(DFSPH_ERR_INVALID_ARG, "model is NULL");
-    if (n < 0 || n > (int64_t)1 << 31) throw DfsphException(DFSPH_ERR_INVALID_ARG, "n");
+    if (n < 0 || n > (int64_t)INT32_MAX - MLP_TILE) throw DfsphException(DFSPH_ERR_INVALID_ARG, "n");
     if (n == 0) return DFSPH_OK;
     DeviceScope ds(m->device);
     check_device_ptr(x, "x");
     check_device_ptr(y, "y");
+    {
+      // the kernel reads the next tile's features before it writes the current tile's outputs
+      const auto xb = reinterpret_cast<uintptr_t>(x), yb = reinterpret_cast<uintptr_t>(y);
+      const auto xe = xb + (uintptr_t)n * 4 * sizeof(float), ye = yb + (uintptr_t)n * sizeof(float);
+      if (xb < ye && yb < xe) throw DfsphException(DFSPH_ERR_INVALID_ARG, "x and y overlap");
+    }
+    mlp_sync_small(m);
     const int ntiles = (int)((n + MLP_TILE - 1) / MLP_TILE);
     const int grid = std::min(ntiles, m->nparts * 8);
     DF_CK(cudaMemsetAsync(m->err, 0, sizeof(int), m->stream));

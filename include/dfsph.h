@@ -404,7 +404,8 @@ int dfsph_mlp_train_step(dfsph_mlp *m, const float *x, const float *y, int64_t n
 /* Gradient of that loss over samples 0..n (DFSPH_MLP_NPARAMS doubles, host) without
    updating the parameters. */
 int dfsph_mlp_gradient(dfsph_mlp *m, const float *x, const float *y, int64_t n, double *grad, double *loss);
-/* Predicted targets (denormalised) for n samples. */
+/* Predicted targets (denormalised) for n samples: x[n][4] -> y[n] (device pointers; the
+   two ranges may not overlap). */
 int dfsph_mlp_predict(dfsph_mlp *m, const float *x, float *y, int64_t n);
 /* Failure-path test hook (no counterpart in the reference, whose CPU path has no device
    waits): the number of polls the first tensor-core wait of each inference CTA may take
