@@ -346,6 +346,7 @@ def run_ours(args):
     # ---- headline: forward + adjoint over the window (collapse phase)
     for _ in range(args.warmup):
         sim.step(1)
+    slot_w = sim.checkpoint_save()  # the window's first state, for the end-to-end leg
     sim.reset_gradient()
     barrier(pg)
     clocks = ClockSampler(local)
@@ -404,15 +405,17 @@ def run_ours(args):
     sim.set_gradient_enabled(True)
 
     # ---- end to end through the public API with host buffers: one optimisation-loop
-    # trajectory over the window. The fluid state comes from the device checkpoint (the
-    # trajectory's saved starting state, as the reference's scripts load theirs), the
-    # bodies' states are uploaded from host memory, K single-step calls each followed by a
-    # read-back of every body's state, then the adjoint with its host input and output.
+    # trajectory over the headline's window. The fluid state comes from the device
+    # checkpoint of the window's first state (the trajectory's saved starting state, as the
+    # reference's scripts load theirs), the bodies' states are uploaded from host memory,
+    # K single-step calls each followed by a read-back of every body's state, then the
+    # adjoint with its host input and output.
     n = sim.n_fluid
+    sim.checkpoint_restore(slot_w)
     host_bodies = [sim.rigid_state(b) for b in range(nb)]
     sim.synchronize()
     t0 = time.perf_counter()
-    sim.checkpoint_restore(slot)
+    sim.checkpoint_restore(slot_w)
     sim.reset_gradient()
     for b in range(nb):
         sim.set_rigid_state(b, *host_bodies[b])
@@ -432,9 +435,7 @@ def run_ours(args):
     # ---- the CPU oracle over the same window, from the same device state
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        sim.checkpoint_restore(slot)
-        for _ in range(args.warmup):
-            sim.step(1)
+        sim.checkpoint_restore(slot_w)
         threads = os.cpu_count() or 1
         cpu_steps = args.cpu_steps
         cval, cdt, cip = cpu_baseline(args, sim, cpu_steps, threads)
@@ -444,6 +445,7 @@ def run_ours(args):
                          f"{sc_start} of the full {args.config_name} workload ({cip:.2f} pressure sweeps per "
                          f"step), oracle port with FP32 fluid / FP64 rigid, gradient on, {threads} OpenMP threads"}
     sim.checkpoint_free(slot)
+    sim.checkpoint_free(slot_w)
 
     # ---- learned warm start vs the reference warm start (collapse phase of a held-out seed)
     ws = None
