@@ -1,6 +1,7 @@
-// engine.cuh — host orchestration of the DiffDFSPH step on one GPU (one CUDA stream
-// per context). Engine<T> is instantiated for float and double fluid arithmetic in
-// engine_fp32.cu / engine_fp64.cu; the C ABI (abi.cu) only sees EngineBase.
+// engine.cuh — host orchestration of the DiffDFSPH step on one GPU (three CUDA streams per
+// context: fluid, rigid bodies, per-body chain rule). Engine<T> is instantiated for float
+// and double fluid arithmetic in engine_fp32.cu / engine_fp64.cu; the C ABI (abi.cu) only
+// sees EngineBase.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -212,7 +213,7 @@ class Engine : public EngineBase {
   dfsph_params P_;
   FluidConsts<T> fc_;
   RigidConsts rc_;
-  PairConsts<T> pcP_, pcD_;
+  PairConsts<T> pcP_{}, pcD_{};
   int n_ = 0, ns_ = 0, nd_ = 0, nb_ = 0, kbf_ = 128;
   int ncell_ = 0;
   cudaStream_t stream_ = nullptr;

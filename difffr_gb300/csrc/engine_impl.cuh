@@ -742,8 +742,8 @@ void Engine<T>::solve_impl(bool pressure) {
     const bool need = (it + 1 >= minIt) || (it + 1 >= maxIt);
     launch_density(im, nullptr, need);
     if (need) {
-      k_final_sum<<<1, 256, 0, stream_>>>(nbk, partials_.p, 1.0 / (double)std::max(n_, 1), resid_.p,
-                                          resid_host_dev_, err_.p);
+      k_final_sum<<<1, FINAL_SUM_THREADS, 0, stream_>>>(nbk, partials_.p, 1.0 / (double)std::max(n_, 1), resid_.p,
+                                                        resid_host_dev_, err_.p);
       launched();
       check_launch();
       avg = read_residual();

@@ -809,21 +809,34 @@ static __global__ void k_integrate(FluidConsts<T> c, Rec<T> *__restrict__ R, T *
   if (scale_kappa) kappa[i] *= c.dt * c.dt;
 }
 
-// Final residual sum (one block of 256 threads, fixed order); also publishes the
-// device error word next to it in mapped host memory, so one stream synchronisation
-// reads both.
-static __global__ void __launch_bounds__(256) k_final_sum(int nparts, const double *__restrict__ partials,
-                                                          double scale, double *__restrict__ out,
-                                                          double *__restrict__ out_host, const int *__restrict__ err) {
-  __shared__ double ws[8];
+// Final residual sum (one block of FINAL_SUM_THREADS threads, fixed order); also publishes
+// the device error word next to it in mapped host memory, so one stream synchronisation
+// reads both. Thread t adds partials t, t + 1024, t + 2048, ... in index order, with eight
+// loads in flight at a time (one memory latency per 8192 partials instead of one per
+// partial); then a shuffle tree per warp and the 32 warp sums in warp order.
+constexpr int FINAL_SUM_THREADS = 1024;
+static __global__ void __launch_bounds__(FINAL_SUM_THREADS) k_final_sum(int nparts, const double *__restrict__ partials,
+                                                                        double scale, double *__restrict__ out,
+                                                                        double *__restrict__ out_host,
+                                                                        const int *__restrict__ err) {
+  __shared__ double ws[FINAL_SUM_THREADS / 32];
   double s = 0.0;
-  for (int k = threadIdx.x; k < nparts; k += blockDim.x) s += partials[k];
+  for (int k0 = threadIdx.x; k0 < nparts; k0 += 8 * FINAL_SUM_THREADS) {
+    double v[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      const int k = k0 + u * FINAL_SUM_THREADS;
+      v[u] = k < nparts ? partials[k] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; u++) s += v[u];
+  }
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
   __syncthreads();
   if (threadIdx.x == 0) {
     double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += ws[w];
+    for (int w = 0; w < FINAL_SUM_THREADS / 32; w++) t += ws[w];
     *out = t * scale;
     if (out_host) {
       out_host[0] = t * scale;
