@@ -21,6 +21,7 @@
 
 #include <cstdint>
 
+#include "f32x2.cuh"
 #include "mlp_view.h"
 #include "tc.cuh"
 
@@ -54,33 +55,12 @@ static __device__ __forceinline__ float gelu_f(float x) {
   return fmaf(h, t, h);
 }
 
-// ---- packed FP32 pairs (Blackwell f32x2 arithmetic: two IEEE FP32 operations per
-// instruction, each rounded as its scalar form)
-static __device__ __forceinline__ unsigned long long f2_bits(float2 v) {
-  return (unsigned long long)__float_as_uint(v.x) | ((unsigned long long)__float_as_uint(v.y) << 32);
-}
-static __device__ __forceinline__ float2 f2_of(unsigned long long u) {
-  return make_float2(__uint_as_float((unsigned)u), __uint_as_float((unsigned)(u >> 32)));
-}
-static __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
-  unsigned long long d;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)), "l"(f2_bits(c)));
-  return f2_of(d);
-}
-static __device__ __forceinline__ float2 mul2(float2 a, float2 b) {
-  unsigned long long d;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
-  return f2_of(d);
-}
-static __device__ __forceinline__ float2 add2(float2 a, float2 b) {
-  unsigned long long d;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
-  return f2_of(d);
-}
 // gelu_f on a pair, from h = x / 2 (the inference kernel carries the halved pre-activations:
-// its W1, b1 and b2 are stored halved, which is exact). Every intermediate is an exact power-
-// of-two multiple of gelu_f's, so the result is bit-identical to gelu_f(x):
-// h^2 = x^2 / 4, 8 c a h^2 + 2 c = 2 (c a x^2 + c), u = h (2 (c + c a x^2)), g = h + h t.
+// its W1, b1 and b2 are stored halved, which is exact). Every intermediate is a power-of-two
+// multiple of gelu_f's, so in exact arithmetic the result is gelu_f(x), with one multiply
+// fewer: h^2 = x^2 / 4, 8 c a h^2 + 2 c = 2 (c a x^2 + c), u = h (2 (c + c a x^2)),
+// g = h + h t. (The packed operations may round differently from the scalar form in the
+// last bit; the tolerance against the oracle covers it.)
 static __device__ __forceinline__ float2 gelu2_half(float2 h) {
   const float2 u = mul2(h, fma2(make_float2(8.f * GELU_CA, 8.f * GELU_CA), mul2(h, h),
                                 make_float2(2.f * GELU_C, 2.f * GELU_C)));
