@@ -44,6 +44,40 @@ def test_mlp_predict_matches_oracle(gpu_lib, oracle_lib):
     assert np.max(np.abs(got - ref)) <= 2e-3 * scale, np.max(np.abs(got - ref)) / scale
 
 
+def test_mlp_predict_after_training_matches_oracle(gpu_lib, oracle_lib):
+    """Inference reads the small weights from its parameter block, a host copy refreshed
+    after every parameter change: predictions after Adam steps follow the new weights."""
+    m = _model(seed=9)
+    x, y, xt, yt = _data(3000, seed=4)
+    m.fit_normalization(xt, yt)
+    p0, _ = m.params()
+    m.predict(xt)                       # the host copy is current for p0
+    for _ in range(3):
+        m.train_step(xt, yt, lr=1e-2)
+    p, norm = m.params()
+    assert np.max(np.abs(p - p0)) > 1e-3
+    got = m.predict(xt).cpu().numpy()
+    ref, _, _ = oracle_lib.mlp_eval(p, norm, x)
+    scale = float(norm[9])
+    assert np.max(np.abs(got - ref)) <= 2e-3 * scale, np.max(np.abs(got - ref)) / scale
+
+
+def test_mlp_predict_rejects_overlapping_buffers(gpu_lib):
+    import torch
+    lib = gpu_lib
+    m = _model()
+    n = 1000
+    buf = torch.zeros(5 * n, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    x = buf.data_ptr()
+    rc = lib.dfsph_mlp_predict(m.h, x, x + 4 * (4 * n - 1), n)   # y starts inside x
+    assert rc == _abi.DFSPH_ERR_INVALID_ARG
+    assert "overlap" in lib.dfsph_last_error().decode()
+    _abi.check(lib, lib.dfsph_mlp_predict(m.h, x, x + 4 * (4 * n), n))   # y right after x
+    torch.cuda.synchronize()
+    assert torch.isfinite(buf[4 * n:]).all()
+
+
 def test_mlp_gradient_matches_oracle(gpu_lib, oracle_lib):
     m = _model(seed=5)
     x, y, xt, yt = _data(2000, seed=1)
