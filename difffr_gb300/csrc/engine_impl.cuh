@@ -962,9 +962,11 @@ int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
       rc = DFSPH_ERR_NOT_CONVERGED;
   }
   // the error word and the body states come back with the step's final synchronisation
-  // (the host mirror of the bodies is then current without another round trip)
-  // (the per-body chain rule may still run: the mirror's G is refreshed by get_rigid_grad)
-  wait_rigid_except_chain();
+  // (the host mirror of the bodies is then current without another round trip). The bodies
+  // are final after k_rigid_step: the per-body chain rule (the mirror's G is refreshed by
+  // get_rigid_grad) and the gradient manager's kernels may still run; what reads their
+  // results (gradient getters, checkpoints, the adjoint, body uploads, reset) waits for them.
+  wait_rigid_state();
   if (nb_ > 0)
     DF_CK(cudaMemcpyAsync(hbs_pin_, bs_.p, nb_ * sizeof(BodyState), cudaMemcpyDeviceToHost, stream_));
   DF_CK(cudaMemcpyAsync(err_host_, err_.p, sizeof(int), cudaMemcpyDeviceToHost, stream_));
