@@ -39,8 +39,12 @@ ALGO_BYTES = {
 
 # DRAM bytes per particle and launch (dram__bytes_read.sum + dram__bytes_write.sum) from an
 # ncu capture of the same passes on the 262,144-particle copy of the dam break (L2 flushed
-# by ncu before each launch), scaled by the launch's particle count.
+# by ncu before each launch), scaled by the launch's particle count; a capture of one
+# launch of each at 1M particles measured 179 and 183 B per particle.
 MEASURED_TRAFFIC = {"density_pass": 178.3, "velocity_pass": 179.5}
+# The passes' binding resource as ncu measured it on one launch of each at 1M particles:
+# L1 data-pipe wavefronts (l1tex__data_pipe_lsu_wavefronts) as a fraction of their peak.
+MEASURED_L1_WAVEFRONT_FRAC = {"density_pass": 0.777, "velocity_pass": 0.696}
 
 
 def load_sm_max_mhz():
@@ -390,7 +394,9 @@ def run_ours(args):
         l1_achieved = nbar * (rec + 4) * units_per_launch / avg_launch_s / 1e9
         l1 = {"fluid_neighbours_per_particle": nbar, "bytes_per_particle": nbar * (rec + 4),
               "achieved": l1_achieved, "peak": l1_peak, "unit": "GB/s", "frac": l1_achieved / l1_peak,
-              "peak_basis": "128 B per clock per SM at the maximum SM clock"}
+              "peak_basis": "128 B per clock per SM at the maximum SM clock",
+              # the used record bytes fill fewer wavefronts than a scattered gather costs
+              "ncu_wavefront_frac": MEASURED_L1_WAVEFRONT_FRAC.get(dom)}
 
     # ---- forward-only steps/s over the same window (no pair Jacobians, no tape)
     sim.checkpoint_restore(slot)
