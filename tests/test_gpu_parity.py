@@ -163,6 +163,27 @@ def test_edge_cases_empty_and_no_bodies(gpu_lib, oracle_lib):
     assert np.all(np.isfinite(x))
 
 
+@pytest.mark.parametrize("precision", [_abi.DFSPH_FP64, _abi.DFSPH_FP32])
+def test_edge_cases_lone_particles(gpu_lib, oracle_lib, precision):
+    """One fluid particle, then three far apart (empty neighbour lists: density from the
+    particle itself, a zero DFSPH factor, fewer than 20 neighbours), falling in the scene's
+    container beside its bodies; every field and the rigid state against the oracle."""
+    sc = scn.small_contact_scene(precision=precision)
+    lo, hi = sc.fluid_x.min(axis=0), sc.fluid_x.max(axis=0)
+    mid = 0.5 * (lo + hi)
+    for pts in ([mid], [lo, mid, hi]):
+        x = np.asarray(pts, np.float64).reshape(-1, 3)
+        lone = scn.Scene(params=sc.params, fluid_x=x, fluid_v=np.zeros_like(x), bodies=sc.bodies)
+        g, r = make(lone), oracle_lib.Oracle(lone)
+        g.step(3)
+        r.step(3)
+        tol = 1e-9 if precision == _abi.DFSPH_FP64 else 1e-5
+        for f in (_abi.FIELD_X, _abi.FIELD_V, _abi.FIELD_DENSITY, _abi.FIELD_FACTOR):
+            assert rel(g.field(f), r.field(f)) < tol, (len(pts), f)
+        assert np.allclose(g.rigid_state(1)[0], r.rigid_state(1)[0], rtol=tol, atol=1e-12)
+        assert g.neighbor_total(_abi.NB_FLUID_FLUID) == 0
+
+
 def test_neighbor_overflow_reports_device_error(gpu_lib):
     sc = scn.small_contact_scene(precision=_abi.DFSPH_FP32, max_fluid_neighbors=4)
     g = make(sc)
