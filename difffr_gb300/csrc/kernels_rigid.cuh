@@ -729,21 +729,8 @@ static __global__ void __launch_bounds__(RIGID_THREADS) k_rigid_step(BodyState *
         for (int e = 0; e < 3; e++) { sft[k][e] = cr.f[e]; sft[k][3 + e] = cr.tau[e]; }
       }
       __syncthreads();
-      if (t == 0) {
-        // the body's velocities and inertia in registers for the sequential part (the same
-        // operations on the same values as on the shared record, without a shared-memory
-        // round trip in every link of the chain)
-        double v[3], w[3], I[9], Ii[9];
-        for (int e = 0; e < 3; e++) { v[e] = B.v[e]; w[e] = B.w[e]; }
-        for (int e = 0; e < 9; e++) { I[e] = B.I[e]; Ii[e] = B.Iinv[e]; }
-        const double im = B.invMass;
-        const bool gyro = rc.gyroscopic;
-        for (int k = 0; k < m; k++) {
-          body_add_force(v, im, sft[k], dt);
-          body_add_torque(w, I, Ii, sft[k] + 3, gyro, dt);
-        }
-        for (int e = 0; e < 3; e++) { B.v[e] = v[e]; B.w[e] = w[e]; }
-      }
+      if (t == 0)
+        for (int k = 0; k < m; k++) { add_force(sft[k]); add_torque(sft[k] + 3); }
       __syncthreads();
     }
   }
