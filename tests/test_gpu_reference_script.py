@@ -1,17 +1,20 @@
-"""The reference's own optimisation script, run unchanged against the GPU library.
+"""The reference's own optimisation scripts, run unchanged against the GPU library.
 
-experiments/rigid_body_trajectory_optimization/python/gradient-based-optimize.py is read
-from a DiffFR checkout (DIFFFR_REFERENCE, else ``reference`` beside this repository; the
-test skips without one) and executed as ``__main__`` with its own command line. Its
+experiments/rigid_body_trajectory_optimization/python/gradient-based-optimize.py and
+diff-rigid-contact-multi.py are read from a DiffFR checkout (DIFFFR_REFERENCE_SCRIPTS, else
+DIFFFR_REFERENCE, else ``reference`` beside this repository; the tests skip without one)
+and executed as ``__main__`` with their own command lines. Its
 ``import pysplishsplash as sph`` is answered by this repository's ``pysplishsplash``
 package. Its ``import quaternion`` (numpy-quaternion; the script imports it and never uses
 it) is answered by an empty module where the package is not installed.
 
-The scene is a small synthetic one in the reference's scene-JSON format: a fluid block in
-a closed box and a dynamic sphere released into it, a trajectory of 12 steps. The script
-runs the bottle-flip task (position and rotation losses, gradients from
-get_grad_x_to_v0 / get_grad_quaternion_to_omega0) for two optimisation iterations and
-then quits by itself (``--maxIter 1``).
+The scenes are small synthetic ones in the reference's scene-JSON format, trajectories of
+12 steps. gradient-based-optimize.py runs the bottle-flip task (a fluid block in a closed
+box and a dynamic sphere released into it; position and rotation losses, gradients from
+get_grad_x_to_v0 / get_grad_quaternion_to_omega0); diff-rigid-contact-multi.py runs its
+two-body task with the rigid contact solver and the gradient manager on (one sphere
+strikes another; the gradient is the manager's cross-body block). Each runs two
+optimisation iterations and then quits by itself (``--maxIter 1``).
 """
 import json
 import os
@@ -28,14 +31,35 @@ from oracle import reference_root
 pytestmark = pytest.mark.gpu
 
 SCRIPT = ("experiments", "rigid_body_trajectory_optimization", "python", "gradient-based-optimize.py")
+CONTACT_SCRIPT = ("experiments", "rigid_body_trajectory_optimization", "python", "diff-rigid-contact-multi.py")
 
 
-def _script():
+def _script(parts=SCRIPT):
     ref = os.environ.get("DIFFFR_REFERENCE_SCRIPTS") or reference_root()
     if ref is None:
         return None
-    p = os.path.join(ref, *SCRIPT)
+    p = os.path.join(ref, *parts)
     return p if os.path.exists(p) else None
+
+
+def _run_script(script, argv, tmp_path, monkeypatch):
+    """Runs a reference script as __main__ against this repository's pysplishsplash; returns
+    its standard output."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    monkeypatch.syspath_prepend(root)
+    monkeypatch.syspath_prepend(os.path.dirname(script))
+    try:
+        import quaternion  # noqa: F401
+    except ImportError:
+        monkeypatch.setitem(sys.modules, "quaternion", types.ModuleType("quaternion"))
+    for name in ("pysplishsplash", "utils"):
+        monkeypatch.delitem(sys.modules, name, raising=False)
+    monkeypatch.chdir(tmp_path)
+    monkeypatch.setattr(sys, "argv", [script, *argv])
+    with pytest.raises(SystemExit):
+        runpy.run_path(script, run_name="__main__")
+    import pysplishsplash
+    assert pysplishsplash.__file__.startswith(root)
 
 
 def test_gradient_based_optimize_runs_unchanged(gpu_lib, tmp_path, capsys, monkeypatch):
@@ -58,21 +82,9 @@ def test_gradient_based_optimize_runs_unchanged(gpu_lib, tmp_path, capsys, monke
     }
     f = tmp_path / "scene.json"
     f.write_text(json.dumps(scene))
-    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    monkeypatch.syspath_prepend(root)
-    monkeypatch.syspath_prepend(os.path.dirname(script))
-    try:
-        import quaternion  # noqa: F401
-    except ImportError:
-        monkeypatch.setitem(sys.modules, "quaternion", types.ModuleType("quaternion"))
-    for name in ("pysplishsplash", "utils"):
-        monkeypatch.delitem(sys.modules, name, raising=False)
-    monkeypatch.chdir(tmp_path)
-    monkeypatch.setattr(sys, "argv", [script, "--scene", str(f), "--no-gui", "--no-initial-pause",
-                                      "--taskType", "bottle-flip", "--maxIter", "1", "--lr-v", "0.1",
-                                      "--lr-omega", "0.1", "--output-dir", str(tmp_path)])
-    with pytest.raises(SystemExit):
-        runpy.run_path(script, run_name="__main__")
+    _run_script(script, ["--scene", str(f), "--no-gui", "--no-initial-pause", "--taskType", "bottle-flip",
+                         "--maxIter", "1", "--lr-v", "0.1", "--lr-omega", "0.1", "--output-dir", str(tmp_path)],
+                tmp_path, monkeypatch)
     out = capsys.readouterr().out
     losses = re.findall(r"===== iter (\d+), loss = \[tensor\(\[([-0-9.e+]+)\]", out)
     assert [int(i) for i, _ in losses] == [1, 2], out[-3000:]
@@ -83,5 +95,40 @@ def test_gradient_based_optimize_runs_unchanged(gpu_lib, tmp_path, capsys, monke
     assert len(grads) >= 2
     for g in grads:
         assert np.all(np.isfinite(np.array(g.split(), dtype=np.float64)))
-    import pysplishsplash
-    assert pysplishsplash.__file__.startswith(root)
+
+
+def test_rigid_contact_multi_runs_unchanged(gpu_lib, tmp_path, capsys, monkeypatch):
+    """experiments/rigid_body_trajectory_optimization/python/diff-rigid-contact-multi.py: the
+    billiards-style task (the active sphere's initial velocity optimised so that the
+    passive one it strikes reaches a target), with the rigid contact solver and the
+    gradient manager on; the gradient is the manager's cross-body block
+    get_grad_x_to_v0(passive, active). Two optimisation iterations on a small tank in which
+    sphere 1 moves at 1 m/s towards sphere 2, 0.01 m away."""
+    script = _script(CONTACT_SCRIPT)
+    if script is None:
+        pytest.skip("reference checkout not present")
+    scene = {
+        "Configuration": {"particleRadius": 0.025, "timeStepSize": 0.001, "targetTime": 0.012,
+                          "maxIterations": 100, "maxError": 0.01, "maxErrorV": 0.1, "gradientMode": 1,
+                          "useRigidContactSolver": True, "useRigidGradientManager": True},
+        "Materials": [{"id": "Fluid", "viscosity": 0.01}],
+        "FluidBlocks": [{"start": [-0.3, 0.0, -0.3], "end": [0.3, 0.2, 0.3]}],
+        "RigidBodies": [
+            {"geometryFile": "UnitBox.obj", "scale": [1.0, 1.0, 1.0], "translation": [0.0, 0.45, 0.0],
+             "isWall": True, "isDynamic": False},
+            {"geometryFile": "sphere", "scale": [0.1, 0.1, 0.1], "translation": [-0.105, 0.25, 0.0],
+             "isDynamic": True, "density": 700, "initVelocity": [1.0, 0.0, 0.0],
+             "initAngularVelocity": [0.0, 0.0, 0.0]},
+            {"geometryFile": "sphere", "scale": [0.1, 0.1, 0.1], "translation": [0.105, 0.25, 0.0],
+             "isDynamic": True, "density": 700, "initVelocity": [0.0, 0.0, 0.0],
+             "initAngularVelocity": [0.0, 0.0, 0.0], "targetX": [0.3, 0.25, 0.0]},
+        ],
+    }
+    f = tmp_path / "scene.json"
+    f.write_text(json.dumps(scene))
+    _run_script(script, ["--scene", str(f), "--no-gui", "--no-initial-pause", "--maxIter", "1",
+                         "--act", "1", "--passive", "2", "--output-dir", str(tmp_path)], tmp_path, monkeypatch)
+    out = capsys.readouterr().out
+    losses = re.findall(r"===== iter (\d+), loss = \[tensor\(\[([-0-9.e+]+)\]", out)
+    assert [int(i) for i, _ in losses] == [1, 2], out[-3000:]
+    assert np.all(np.isfinite([float(v) for _, v in losses]))
