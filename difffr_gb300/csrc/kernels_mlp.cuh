@@ -71,7 +71,9 @@ static __device__ __forceinline__ float2 gelu2_half(float2 h) {
 // two round-to-nearest BF16 conversions in one packed instruction (lo in the low half)
 static __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
   const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
-  return *reinterpret_cast<const uint32_t *>(&v);
+  uint32_t u;
+  memcpy(&u, &v, sizeof(u));
+  return u;
 }
 // store 8 consecutive columns (c0 multiple of 8) of row `row` of a core-matrix tile
 static __device__ __forceinline__ void st_row8(uint8_t *tile, int row, int c0, int cols, const float *v) {
