@@ -188,10 +188,21 @@ static __global__ void __launch_bounds__(MLP_THREADS) k_mlp_infer(MlpView mv, IO
   float fn[4] = {0.f, 0.f, 0.f, 0.f};
   bool wantn = false;
   if (blockIdx.x < ntiles && (int)blockIdx.x * MLP_TILE + tid < n) wantn = io.load(blockIdx.x * MLP_TILE + tid, fn);
+  bool first_wait = true;
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int i = tile * MLP_TILE + tid;
     float f[4];
     const bool want = wantn;
+    if (!__syncthreads_or(want)) {
+      // no particle of this tile wants a prediction (in the solver's warm start: none with
+      // rho_adv > 1): skip its arithmetic, load the next tile's features
+      const int64_t inext = (int64_t)(tile + (int)gridDim.x) * MLP_TILE + tid;
+      wantn = false;
+#pragma unroll
+      for (int k = 0; k < 4; k++) fn[k] = 0.f;
+      if (inext < n) wantn = io.load((int)inext, fn);
+      continue;
+    }
 #pragma unroll
     for (int k = 0; k < 4; k++) f[k] = (fn[k] - xm[k]) * xi[k];
     mlp_layer1_paired(mv, f, sH1, tid, 64);
@@ -214,10 +225,10 @@ static __global__ void __launch_bounds__(MLP_THREADS) k_mlp_infer(MlpView mv, IO
       for (int k = 0; k < 4; k++) fn[k] = 0.f;
       if (inext < n) wantn = io.load((int)inext, fn);
     }
-    // the first wait may be given fewer polls (a test of the failure path below); the wait
-    // for the product still in flight after a failure always has the regular limit
-    const uint32_t lim = (tile == (int)blockIdx.x && mv.first_wait_polls >= 0) ? (uint32_t)mv.first_wait_polls
-                                                                              : MLP_WAIT_LIMIT;
+    // the CTA's first wait may be given fewer polls (a test of the failure path below); the
+    // wait for the product still in flight after a failure always has the regular limit
+    const uint32_t lim = (first_wait && mv.first_wait_polls >= 0) ? (uint32_t)mv.first_wait_polls : MLP_WAIT_LIMIT;
+    first_wait = false;
     // one thread polls the barrier (every poll is a shared-memory access), the block follows
     const bool ok = __syncthreads_and(tid == 0 ? tc::mbar_wait(bar, phase, lim) : true) != 0;
     if (!ok) break;
