@@ -453,6 +453,24 @@ def run_ours(args):
     sim.checkpoint_free(slot)
     sim.checkpoint_free(slot_w)
 
+    # ---- the whole trajectory of the configuration (steps 0..T-1 in one call, gradient
+    # recorded, then the adjoint), the average over all its phases
+    traj = None
+    if rank == 0 and args.config == 1 and args.trajectory_steps > 0:
+        sim.reset()
+        sim.reset_gradient()
+        sim.synchronize()
+        sim.record_event(0)
+        st_t = sim.step(args.trajectory_steps)
+        sim.backward(dL)
+        sim.record_event(1)
+        t_ms = sim.event_elapsed_ms(0, 1)
+        traj = {"steps": args.trajectory_steps, "value": args.trajectory_steps / (t_ms / 1000.0), "unit": UNIT,
+                "ms_per_step": t_ms / args.trajectory_steps,
+                "pressure_iterations_per_step": st_t["total_pressure_iterations"] / args.trajectory_steps,
+                "divergence_iterations_per_step": st_t["total_divergence_iterations"] / args.trajectory_steps,
+                "window": f"steps 0-{args.trajectory_steps - 1} from rest, forward with gradient recording, then the adjoint"}
+
     # ---- learned warm start vs the reference warm start (collapse phase of a held-out seed)
     ws = None
     if rank == 0 and args.config == 1 and args.ws_steps > 0:
@@ -492,6 +510,7 @@ def run_ours(args):
             "kernel_ms_per_step": {k: v["ms"] / args.steps for k, v in prof.items()},
             "clocks": clk,
             "cpu_baseline": cpu,
+            "trajectory": traj,
             "warm_start": ws,
             "contact": contact,
         }
@@ -668,6 +687,7 @@ def main():
     ap.add_argument("--ws-steps", type=int, default=200)
     ap.add_argument("--train-warm-start", action="store_true")
     ap.add_argument("--contact-steps", type=int, default=20)
+    ap.add_argument("--trajectory-steps", type=int, default=500)
     args = ap.parse_args()
     args.config_name = {0: "tank_sphere_8k (20^3 lattice, r 0.025)",
                         1: "dam_break_sphere_1M (100^3 lattice, r 0.005, 2.4x1.2x1.2 box, R 0.05 sphere)",
