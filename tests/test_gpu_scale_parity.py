@@ -97,6 +97,37 @@ def test_bench_scene_1M_five_steps(bench_pair):
     assert sg["pressure_iterations"] == sr["pressure_iterations"]
 
 
+def test_bench_scene_1M_fifty_steps(bench_pair):
+    """Fifty more steps of the 1M scene on both sides from the state the previous test left
+    (the oracle took over the GPU's state there). Two FP32 runs that sum in different orders
+    separate slowly: each solve stops once the AVERAGE density error is below tolerance, so
+    runs that round differently stop at different Jacobi iterates whose per-particle
+    velocities differ by up to the per-particle residual, and those differences accumulate.
+    Measured on a GB300 after these 50 steps (56 from rest): positions within 3.8e-5 of the
+    domain for 99.9 % of the particles (1.0e-4 at most), velocities within 2.5e-2 of the
+    largest speed for 99 % (7.1e-2 at most), equal sweep counts in every step. Bounded here
+    at about twice that; the rigid state within 1e-3."""
+    sc, gpu, ref = bench_pair
+    differ = 0
+    for _ in range(50):
+        sg, sr = gpu.step(1), ref.step(1)
+        differ += (sg["pressure_iterations"], sg["divergence_iterations"]) != \
+            (sr["pressure_iterations"], sr["divergence_iterations"])
+    xg, xr = np.asarray(gpu.field(_abi.FIELD_X)), np.asarray(ref.field(_abi.FIELD_X))
+    vg, vr = np.asarray(gpu.field(_abi.FIELD_V)), np.asarray(ref.field(_abi.FIELD_V))
+    dx = np.linalg.norm((xg - xr).reshape(-1, 3), axis=1) / np.max(np.abs(xr))
+    dv = np.linalg.norm((vg - vr).reshape(-1, 3), axis=1) / np.max(np.abs(vr))
+    q = {"x99.9": float(np.quantile(dx, 0.999)), "xmax": float(dx.max()), "v99": float(np.quantile(dv, 0.99)),
+         "vmax": float(dv.max())}
+    print("1M, 50 further steps: relative differences", q, "steps with other sweep counts", differ)
+    assert q["x99.9"] < 1e-4 and q["xmax"] < 3e-4
+    assert q["v99"] < 5e-2 and q["vmax"] < 0.15
+    assert differ <= 5
+    for b in range(len(sc.bodies)):
+        for a, c in zip(gpu.rigid_state(b), ref.rigid_state(b)):
+            assert np.allclose(a, c, rtol=1e-3, atol=1e-6), (b, a, c)
+
+
 # The horizon of the pool gradient check: the longest over which the FP32 fluid of the GPU
 # and of the oracle stay close enough for the chain's blocks to agree. Measured on a GB300
 # (the ellipsoid flies free for its first 200 steps and is in the water from about step
