@@ -217,3 +217,35 @@ def test_step_force_jacobian_against_finite_differences(gpu_lib, size):
     print("finite-difference cosine", size, cos)
     assert cos > 0.9, cos
     sim.close()
+
+
+def test_basin_4M_neighbour_sets_sampled(gpu_lib):
+    """The 4M-particle basin (the largest configuration), second step: the fluid-fluid
+    neighbour lists of 4,000 randomly chosen particles against an exact search on the host
+    over the positions the lists were built from (those the step started with), with the
+    library's predicate ((dx^2 + dy^2) + dz^2 < h^2 in FP32, no fused multiply-add): equal
+    as sorted sets, particle by particle."""
+    spatial = pytest.importorskip("scipy.spatial")
+    from difffr_gb300.sim import DiffDFSPH
+    sc = scn.config4()
+    sim = DiffDFSPH(sc)
+    sim.step(1)
+    x = np.asarray(sim.field(_abi.FIELD_X), np.float64).reshape(-1, 3).astype(np.float32)
+    sim.step(1)   # its lists are built from x, before its position update
+    start, idx = sim.neighbors(_abi.NB_FLUID_FLUID)
+    sim.close()
+    assert x.shape[0] == 4_000_000
+    r = np.float32(sc.params.particle_radius)
+    h = np.float32(4) * r
+    h2 = h * h
+    tree = spatial.cKDTree(x.astype(np.float64))
+    pick = np.random.default_rng(3).choice(x.shape[0], 4000, replace=False)
+    for i in pick:
+        cand = np.asarray(tree.query_ball_point(x[i].astype(np.float64), float(h) * (1 + 1e-5)), np.int64)
+        cand = cand[cand != i]
+        d = x[i][None, :] - x[cand]
+        d2 = (d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]
+        want = np.sort(cand[d2 < h2])
+        got = np.sort(idx[start[i]:start[i + 1]])
+        assert np.array_equal(got, want), (int(i), got.size, want.size)
+
