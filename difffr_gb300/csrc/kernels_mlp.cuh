@@ -241,7 +241,6 @@ static __global__ void __launch_bounds__(MLP_THREADS) k_mlp_infer(MlpView mv, IO
     for (int c = 0; c < 64; c += 16) {
       float z[16];
       tc::tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c, z);
-      tc::tmem_wait_ld();
 #pragma unroll
       for (int u = 0; u < 16; u += 2) {
         const int j = c + u;
@@ -442,7 +441,6 @@ static __global__ void __launch_bounds__(MLP_TRAIN_THREADS, 1)
     {
       float t[8];
       tc::tmem_ld8(tmem + lane_off + TZ2 + (uint32_t)c0, t);
-      tc::tmem_wait_ld();
       float h[8], part = 0.f;
 #pragma unroll
       for (int u = 0; u < 8; u++) {
@@ -500,7 +498,6 @@ static __global__ void __launch_bounds__(MLP_TRAIN_THREADS, 1)
     {
       float t[8], a[8];
       tc::tmem_ld8(tmem + lane_off + TDH1 + (uint32_t)c0, t);
-      tc::tmem_wait_ld();
 #pragma unroll
       for (int u = 0; u < 8; u++) a[u] = valid ? t[u] * g1d[u] : 0.f;
       st_row8(base + SDZ1, row, c0, 128, a);
@@ -538,7 +535,6 @@ static __global__ void __launch_bounds__(MLP_TRAIN_THREADS, 1)
     // GW2: 80 columns (W2 row `row`, then b2 in column 64), 16 per group
     float t[16];
     tc::tmem_ld16(tmem + lane_off + TGW2 + (uint32_t)(16 * grp), t);
-    tc::tmem_wait_ld();
 #pragma unroll
     for (int u = 0; u < 16; u++) {
       const int col = 16 * grp + u;
@@ -548,14 +544,12 @@ static __global__ void __launch_bounds__(MLP_TRAIN_THREADS, 1)
   } else if (q < 2 && grp == 5) {
     float t[8];
     tc::tmem_ld8(tmem + lane_off + TGW1, t);
-    tc::tmem_wait_ld();
 #pragma unroll
     for (int k = 0; k < 4; k++) gp[MLP_OFF_W1 + row * 4 + k] = t[k];
     gp[MLP_OFF_B1 + row] = t[4];
   } else if (q < 3 && grp == 6) {
     float t[8];
     tc::tmem_ld8(tmem + lane_off + TGW3, t);
-    tc::tmem_wait_ld();
     if (row < 64) gp[MLP_OFF_W3 + row] = t[0];
     else if (row == 64) gp[MLP_OFF_B3] = t[0];
   }

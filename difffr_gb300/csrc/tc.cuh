@@ -114,7 +114,9 @@ static __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
   return false;
 }
 
-// ---- TMEM -> registers: 32 lanes x 32 bit, 16 consecutive columns per thread
+// ---- TMEM -> registers: 32 lanes x 32 bit, consecutive columns per thread. The wait
+// (tcgen05.wait::ld) names the loaded registers as read-write operands, so no use of them
+// can be scheduled between the load and the wait; independent work still can.
 static __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   uint32_t r[16];
   asm volatile(
@@ -124,20 +126,27 @@ static __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
         "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
       : "r"(taddr)
       : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                 "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15])
+               :
+               : "memory");
 #pragma unroll
   for (int k = 0; k < 16; k++) v[k] = __uint_as_float(r[k]);
 }
-// 8 consecutive columns per thread
 static __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
   uint32_t r[8];
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
                : "r"(taddr)
                : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7])
+               :
+               : "memory");
 #pragma unroll
   for (int k = 0; k < 8; k++) v[k] = __uint_as_float(r[k]);
 }
-static __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 }  // namespace tc
 }  // namespace dfsph
