@@ -9,7 +9,7 @@ sweep counts. Against the reference's float build, the GPU's FP32 fluid / FP64 r
 agrees within FP32 tolerances (fields 1e-4 of their maximum, rigid state 1e-4, force and
 chain state 2e-2 after 10 steps: the reference integrates the bodies in FP32 as well).
 The same FP32 / FP64 split against the reference's FP64 build states the split's own error
-(what the spec precision choice costs) on every double-build case.
+(what running the fluid in FP32 costs) on every double-build case.
 """
 import pytest
 
