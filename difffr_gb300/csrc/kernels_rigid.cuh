@@ -590,6 +590,45 @@ static __device__ __forceinline__ void body_add_torque(double *w, const double *
   mv3(Iinv, cr, d);
   for (int k = 0; k < 3; k++) w[k] += d[k] * dt;
 }
+// The contact samples' forces and torques of one body applied in sample order (per sample
+// body_add_force, then body_add_torque), one vector component per lane of the calling warp
+// (lanes 0-2; the others repeat component 0 and write nothing): the same expressions,
+// component by component, with the other components fetched by shuffles. FP64 costs about
+// the same per warp instruction whatever the number of active lanes, so the lanes cut this
+// sequential part's FP64 work to about a third. All 32 lanes of the warp call it.
+static __device__ __forceinline__ void body_apply_samples_lanes(double *bv, double *bw, const double *I,
+                                                                const double *Iinv, double invMass,
+                                                                const double (*ft)[6], int m, bool gyro, double dt) {
+  const int lane = threadIdx.x & 31;
+  const int r = lane < 3 ? lane : 0;
+  double v = bv[r], w = bw[r];
+  const double I0 = I[3 * r], I1 = I[3 * r + 1], I2 = I[3 * r + 2];
+  const double J0 = Iinv[3 * r], J1 = Iinv[3 * r + 1], J2 = Iinv[3 * r + 2];
+  for (int k = 0; k < m; k++) {
+    v += invMass * ft[k][r] * dt;
+    const double w0 = __shfl_sync(0xffffffffu, w, 0), w1 = __shfl_sync(0xffffffffu, w, 1),
+                 w2 = __shfl_sync(0xffffffffu, w, 2);
+    double c;
+    if (gyro) {
+      // cross3(I w, w)[r] = L[r+1] w[r+2] - L[r+2] w[r+1] (indices mod 3)
+      const double L = I0 * w0 + I1 * w1 + I2 * w2;
+      const double L0 = __shfl_sync(0xffffffffu, L, 0), L1 = __shfl_sync(0xffffffffu, L, 1),
+                   L2 = __shfl_sync(0xffffffffu, L, 2);
+      const double La = r == 0 ? L1 : (r == 1 ? L2 : L0), Lb = r == 0 ? L2 : (r == 1 ? L0 : L1);
+      const double wa = r == 0 ? w1 : (r == 1 ? w2 : w0), wb = r == 0 ? w2 : (r == 1 ? w0 : w1);
+      c = La * wb - Lb * wa;
+      c += ft[k][3 + r];
+    } else {
+      c = ft[k][3 + r];
+    }
+    const double c0 = __shfl_sync(0xffffffffu, c, 0), c1 = __shfl_sync(0xffffffffu, c, 1),
+                 c2 = __shfl_sync(0xffffffffu, c, 2);
+    const double d = J0 * c0 + J1 * c1 + J2 * c2;
+    w += d * dt;
+  }
+  if (lane < 3) { bv[r] = v; bw[r] = w; }
+}
+
 // Dynamic3dRigidBody::animate + updateInertia (Dynamic3dRigidBody.h:143-154, 215-219)
 static __device__ __forceinline__ void body_animate(double *x, double *q, double *I, double *Iinv, const double *v,
                                                     const double *w, const double *I0, double dt) {
@@ -729,8 +768,7 @@ static __global__ void __launch_bounds__(RIGID_THREADS) k_rigid_step(BodyState *
         for (int e = 0; e < 3; e++) { sft[k][e] = cr.f[e]; sft[k][3 + e] = cr.tau[e]; }
       }
       __syncthreads();
-      if (t == 0)
-        for (int k = 0; k < m; k++) { add_force(sft[k]); add_torque(sft[k] + 3); }
+      if (t < 32) body_apply_samples_lanes(B.v, B.w, B.I, B.Iinv, B.invMass, sft, m, rc.gyroscopic, dt);
       __syncthreads();
     }
   }
