@@ -725,9 +725,12 @@ static __global__ void __launch_bounds__(RIGID_THREADS) k_rigid_step(BodyState *
   __syncthreads();
   const bool chain = B.dyn && !B.anim && rc.enable_gradient && !rc.manager;
   if (t == 0) B.chain_ran = chain ? 1 : 0;
-  // the body's force-carrying contact samples, in sample order
+  // the body's force-carrying contact samples, in sample order (the first CH also in
+  // shared memory, with the body each one's cross blocks refer to)
+  constexpr int CH = 256;
   __shared__ int warp_tot[32];
   __shared__ int s_con, s_act;
+  __shared__ int s_list[CH], s_rr[CH];
   const bool contact = cs.rec != nullptr && B.dyn;
   if (t == 0) { s_con = 0; s_act = 0; }
   __syncthreads();
@@ -737,7 +740,10 @@ static __global__ void __launch_bounds__(RIGID_THREADS) k_rigid_step(BodyState *
       const int flag = i < B.dcount ? cs.rec[B.dstart + i].flag : 0;
       int tot;
       const int pos = block_exclusive_scan(flag == 2 ? 1 : 0, warp_tot, tot);
-      if (flag == 2) cs.list[B.dstart + s_act + pos] = B.dstart + i;
+      if (flag == 2) {
+        cs.list[B.dstart + s_act + pos] = B.dstart + i;
+        if (s_act + pos < CH) s_list[s_act + pos] = B.dstart + i;
+      }
       const int ncon = __syncthreads_count(flag >= 1);
       if (t == 0) { s_act += tot; s_con += ncon; }
       __syncthreads();
@@ -759,13 +765,13 @@ static __global__ void __launch_bounds__(RIGID_THREADS) k_rigid_step(BodyState *
   if (contact) {
     // the force-carrying samples' forces and torques, in sample order; staged in shared
     // memory by all threads so that the sequential part reads no global memory
-    constexpr int CH = 256;
     __shared__ double sft[CH][6];
     for (int base = 0; base < s_act; base += CH) {
       const int m = min(CH, s_act - base);
       for (int k = t; k < m; k += blockDim.x) {
         const ContactRec &cr = cs.rec[cs.list[B.dstart + base + k]];
         for (int e = 0; e < 3; e++) { sft[k][e] = cr.f[e]; sft[k][3 + e] = cr.tau[e]; }
+        if (base == 0) s_rr[k] = cr.RR;
       }
       __syncthreads();
       if (t < 32) body_apply_samples_lanes(B.v, B.w, B.I, B.Iinv, B.invMass, sft, m, rc.gyroscopic, dt);
@@ -799,9 +805,9 @@ static __global__ void __launch_bounds__(RIGID_THREADS) k_rigid_step(BodyState *
       double acc = 0.0;
       if (contact)
         for (int m = 0; m < s_act; m++) {
-          const int smp = cs.list[B.dstart + m];
+          const int smp = m < CH ? s_list[m] : cs.list[B.dstart + m];
           if (c == b) acc += cs.blk[(size_t)smp * CONTACT_BLK + k];
-          else if (cs.rec[smp].RR == c) acc += cs.blk[(size_t)smp * CONTACT_BLK + NJAC + k];
+          else if ((m < CH ? s_rr[m] : cs.rec[smp].RR) == c) acc += cs.blk[(size_t)smp * CONTACT_BLK + NJAC + k];
         }
       cs.Mc[((size_t)b * nb + c) * NJAC + k] = acc;
     }
