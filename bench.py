@@ -175,12 +175,28 @@ def make_scene(args, enable_gradient=1, seed=0):
     elif args.config == 5:
         sc = scn.dam_break_sphere(n=(64, 64, 64), seed=seed, enable_gradient=enable_gradient)
     elif args.config == 0:
-        sc = scn.config0(precision=0, seed=seed, enable_gradient=enable_gradient)
+        sc = scn.config0(seed=seed, enable_gradient=enable_gradient)  # FP64 fluid, as configured
     elif args.config == 2:
         sc = scn.pool_ellipsoid(seed=seed, enable_gradient=enable_gradient)
     else:
         sc = scn.billiards_on_water(seed=seed, enable_gradient=enable_gradient)
     return sc
+
+
+def scene_dtype(sc):
+    """The arithmetic type of the fluid path ("f64" for an FP64 scene; the bodies are FP64 always)."""
+    from difffr_gb300 import _abi
+    return "f64" if sc.params.fluid_precision == _abi.DFSPH_FP64 else "f32"
+
+
+def oracle_mode(sc):
+    """The oracle build matching the scene's split: FP64 throughout, or FP32 fluid / FP64 rigid."""
+    import oracle
+    return oracle.MODE_F64 if scene_dtype(sc) == "f64" else oracle.MODE_MIXED
+
+
+def split_name(sc):
+    return "FP64 fluid / FP64 rigid" if scene_dtype(sc) == "f64" else "FP32 fluid / FP64 rigid"
 
 
 def dist_setup():
@@ -232,12 +248,19 @@ def cpu_model():
 
 def config_dict(args, sc):
     """The workload description both arms print (same keys, same values)."""
+    # the neighbour passes' working set: the particle records and the int32 neighbour lists
+    # (about 35 entries per particle), against the 129 MB L2
+    wide = 2 if scene_dtype(sc) == "f64" else 1
+    ws_mb = sc.n_fluid * (32 * wide + 16 * wide + 35 * 4) / 1e6
+    l2 = ("inputs larger than L2" if ws_mb > 129.0 else
+          f"working set about {ws_mb:.0f} MB, inside the 129 MB L2 (not flushed between steps)")
+    phase = " (collapse phase)" if args.config == 1 else ""
     return {"workload": args.config_name, "n_fluid": sc.n_fluid, "n_boundary": sc.n_boundary,
             "dt": sc.params.time_step, "gradient_mode": "incomplete",
             "window": f"steps {args.start_step + args.warmup}-{args.start_step + args.warmup + args.steps - 1} "
-                      f"of the trajectory (collapse phase), after {args.warmup} warm-up steps from step "
+                      f"of the trajectory{phase}, after {args.warmup} warm-up steps from step "
                       f"{args.start_step}",
-            "l2": "inputs larger than L2", "parallelism": f"replicas{args.gpus}" if args.gpus > 1 else "single GPU"}
+            "l2": l2, "parallelism": f"replicas{args.gpus}" if args.gpus > 1 else "single GPU"}
 
 
 def oracle_steps(o, steps):
@@ -255,7 +278,7 @@ def cpu_baseline(args, sim, steps, threads):
     import oracle
     oracle.build()
     sc = make_scene(args, enable_gradient=1)
-    o = oracle.Oracle(sc, mode=oracle.MODE_MIXED, threads=threads)
+    o = oracle.Oracle(sc, mode=oracle_mode(sc), threads=threads)
     o.load_state(sim)
     o.step(1)
     return oracle_steps(o, steps)
@@ -271,7 +294,7 @@ def run_reference(args):
     oracle.build()
     threads = os.cpu_count() or 1
     sc = make_scene(args, enable_gradient=1)
-    o = oracle.Oracle(sc, mode=oracle.MODE_MIXED, threads=threads)
+    o = oracle.Oracle(sc, mode=oracle_mode(sc), threads=threads)
     if args.start_step > 0:
         o.step(args.start_step)
     o.step(args.warmup)
@@ -279,12 +302,12 @@ def run_reference(args):
     val, dt, ip = oracle_steps(o, steps)
     sample = (f"{steps} timed steps (steps {args.start_step + args.warmup}-{args.start_step + args.warmup + steps - 1}, "
               f"{ip:.2f} pressure sweeps per step) of the full {args.config_name} workload after an untimed "
-              f"pre-roll from step 0; oracle port, FP32 fluid / FP64 rigid, gradient on, {threads} OpenMP threads "
+              f"pre-roll from step 0; oracle port, {split_name(sc)}, gradient on, {threads} OpenMP threads "
               f"on {cpu_model()}")
     line = {
         "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * dt / steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lattice + sampled boundaries)",
+        "vs_baseline": None, "dtype": scene_dtype(sc), "data": "synthetic (seeded lattice + sampled boundaries)",
         "config": config_dict(args, sc),
         "pressure_iterations_per_step": ip,
         "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
@@ -378,14 +401,17 @@ def run_ours(args):
     d = prof[dom]
     avg_launch_s = d["ms"] / max(d["launches"], 1) / 1000.0
     units_per_launch = d["units"] / max(d["launches"], 1)
-    algo_bytes = ALGO_BYTES.get(dom, 32) * units_per_launch
+    # FP64 fluid fields are twice the bytes; the measured traffic is of the FP32 passes
+    wide = 2 if scene_dtype(sc) == "f64" else 1
+    algo_bytes = wide * ALGO_BYTES.get(dom, 32) * units_per_launch
     achieved = algo_bytes / avg_launch_s / 1e9
-    traffic = MEASURED_TRAFFIC[dom] * units_per_launch if dom in MEASURED_TRAFFIC else None
+    traffic = MEASURED_TRAFFIC[dom] * units_per_launch if dom in MEASURED_TRAFFIC and wide == 1 else None
     # the L1 side of the same kernel: each neighbour visit gathers one 32-byte record (the
     # density and XSPH passes; 16 bytes in the velocity pass) and reads a 4-byte list entry
     from difffr_gb300 import _abi as abi_mod
     nbar = sim.neighbor_total(abi_mod.NB_FLUID_FLUID) / max(sim.n_fluid, 1)
     rec = {"density_pass": 32, "xsph_advect": 32, "velocity_pass": 16}.get(dom)
+    rec = rec * wide if rec is not None else None
     l1 = None
     if rec is not None:
         import torch
@@ -396,7 +422,7 @@ def run_ours(args):
               "achieved": l1_achieved, "peak": l1_peak, "unit": "GB/s", "frac": l1_achieved / l1_peak,
               "peak_basis": "128 B per clock per SM at the maximum SM clock",
               # the used record bytes fill fewer wavefronts than a scattered gather costs
-              "ncu_wavefront_frac": MEASURED_L1_WAVEFRONT_FRAC.get(dom)}
+              "ncu_wavefront_frac": MEASURED_L1_WAVEFRONT_FRAC.get(dom) if wide == 1 else None}
 
     # ---- forward-only steps/s over the same window (no pair Jacobians, no tape)
     sim.checkpoint_restore(slot)
@@ -449,7 +475,7 @@ def run_ours(args):
         cpu = {"value": cval, "unit": UNIT, "cores": threads, "kind": "port", "cpu_model": cpu_model(),
                "sample": f"{cpu_steps} steps (after 1 warm-up step) from the GPU context's state at step "
                          f"{sc_start} of the full {args.config_name} workload ({cip:.2f} pressure sweeps per "
-                         f"step), oracle port with FP32 fluid / FP64 rigid, gradient on, {threads} OpenMP threads"}
+                         f"step), oracle port with {split_name(sc)}, gradient on, {threads} OpenMP threads"}
     sim.checkpoint_free(slot)
     sim.checkpoint_free(slot_w)
 
@@ -490,7 +516,7 @@ def run_ours(args):
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "scaling": "weak", "vs_baseline": None, "dtype": scene_dtype(sc),
             "data": "synthetic (seeded lattice + sampled boundaries)",
             "config": config_dict(args, sc),
             "fwd_only_steps_per_s": world * args.steps / (fwd_ms / 1000.0),
@@ -504,7 +530,7 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "algo_bytes_per_particle": ALGO_BYTES.get(dom, 32),
+                         "algo_bytes_per_particle": wide * ALGO_BYTES.get(dom, 32),
                          "avg_launch_us": avg_launch_s * 1e6},
             "l1_gather": l1,
             "kernel_ms_per_step": {k: v["ms"] / args.steps for k, v in prof.items()},
@@ -689,7 +715,7 @@ def main():
     ap.add_argument("--contact-steps", type=int, default=20)
     ap.add_argument("--trajectory-steps", type=int, default=500)
     args = ap.parse_args()
-    args.config_name = {0: "tank_sphere_8k (20^3 lattice, r 0.025)",
+    args.config_name = {0: "tank_sphere_8k (20^3 lattice, r 0.025, FP64)",
                         1: "dam_break_sphere_1M (100^3 lattice, r 0.005, 2.4x1.2x1.2 box, R 0.05 sphere)",
                         2: "pool_ellipsoid_250k (125x16x125, r 0.004)",
                         4: "billiards_on_water_4M (200x100x200, r 0.0025, 2 spheres)",

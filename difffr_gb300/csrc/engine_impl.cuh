@@ -1,5 +1,7 @@
 // engine_impl.cuh — Engine<T> member definitions (included by engine_fp32.cu / engine_fp64.cu).
 #pragma once
+#include <type_traits>
+
 #include "engine.cuh"
 
 namespace dfsph {
@@ -56,7 +58,7 @@ Engine<T>::Engine(const dfsph_scene *sc) {
   if (P_.struct_size != (int)sizeof(dfsph_params)) throw DfsphException(DFSPH_ERR_INVALID_ARG, "dfsph_params.struct_size mismatch");
   if (!(P_.particle_radius > 0) || !(P_.time_step > 0) || !(P_.density0 > 0))
     throw DfsphException(DFSPH_ERR_INVALID_ARG, "particle_radius, time_step and density0 must be positive");
-  // neighbour passes index LPP threads per particle in int: keep n * LPP below 2^31
+  // neighbour passes index up to LPP_MAX threads per particle in int: keep n * LPP_MAX below 2^31
   if (sc->n_fluid < 0 || sc->n_fluid > (int64_t)INT32_MAX / 8) throw DfsphException(DFSPH_ERR_INVALID_ARG, "n_fluid out of range");
   if (sc->n_fluid > 0 && !sc->fluid_x) throw DfsphException(DFSPH_ERR_INVALID_ARG, "fluid_x is NULL");
   if (sc->n_bodies < 0 || sc->n_bodies > DFSPH_MAX_BODIES) throw DfsphException(DFSPH_ERR_INVALID_ARG, "n_bodies out of range");
@@ -243,6 +245,9 @@ Engine<T>::Engine(const dfsph_scene *sc) {
     DF_CK(cudaGetDevice(&dev));
     DF_CK(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, dev));
   }
+  // lanes per particle of the neighbour passes: LPP_MAX where one lane per particle would
+  // leave the passes below 256 threads per SM (small scenes), else 1
+  fc_.lpp = (int64_t)n_ <= (int64_t)num_sms_ * 256 ? LPP_MAX : 1;
   scan_.prepare((size_t)ncell_ + 1);
 
   // ---- fluid buffers
@@ -263,7 +268,7 @@ Engine<T>::Engine(const dfsph_scene *sc) {
   cstartF_.alloc((size_t)ncell_ + 1);
   cstartS_.alloc((size_t)ncell_ + 1);
   cstartD_.alloc((size_t)ncell_ + 1);
-  partials_.alloc((size_t)blocks(std::max(n_, 1) * LPP, PASS_THREADS));
+  partials_.alloc((size_t)blocks(std::max(n_, 1) * LPP_MAX, PASS_THREADS));
   resid_.alloc(4);
   err_.alloc(1);
   DF_CK(cudaHostAlloc((void **)&resid_host_, 4 * sizeof(double), cudaHostAllocMapped));
@@ -648,13 +653,16 @@ void Engine<T>::raise_error_word(int e) {
 
 template <class T>
 void Engine<T>::launch_density(int mode, T *kappa_io, bool partials, float4 *feat) {
-  const int nbk = blocks(n_ * LPP, PASS_THREADS);
+  const int nbk = blocks(n_ * fc_.lpp, PASS_THREADS);
   double *pp = partials ? partials_.p : nullptr;
   pbegin();
-#define DF_DENS(M, XS)                                                                                             \
-  k_density_pass<T, M, XS><<<nbk, PASS_THREADS, 0, stream_>>>(fc_, R_[cur_].p, Q_.p, BR_.p, flist_.p, fcount_.p, blist_.p,       \
-                                                     bcount_.p, rho_.p, alpha_.p, rhoAdv_.p, kappa_io, pp, feat,      \
-                                                     R_[1 - cur_].p)
+#define DF_DENS_L(M, XS, L)                                                                                        \
+  k_density_pass<T, M, XS, L><<<nbk, PASS_THREADS, 0, stream_>>>(fc_, R_[cur_].p, Q_.p, BR_.p, flist_.p, fcount_.p,  \
+                                                                 blist_.p, bcount_.p, rho_.p, alpha_.p, rhoAdv_.p,  \
+                                                                 kappa_io, pp, feat, R_[1 - cur_].p)
+#define DF_DENS(M, XS)                   \
+  if (fc_.lpp == 1) DF_DENS_L(M, XS, 1); \
+  else DF_DENS_L(M, XS, LPP_MAX)
   // the divergence solve's checked passes also advance the XSPH phase (see k_density_pass)
   const bool xs = mode == PASS_DIVERGENCE && partials && xs_fuse_;
   switch (mode) {
@@ -667,20 +675,25 @@ void Engine<T>::launch_density(int mode, T *kappa_io, bool partials, float4 *fea
     default: DF_DENS(PASS_DIVERGENCE_WARM, false); break;
   }
 #undef DF_DENS
+#undef DF_DENS_L
   launched();
   pend(DFSPH_K_DENSITY_PASS, n_);
 }
 
 template <class T>
 void Engine<T>::launch_velocity(T *kappa_acc) {
-  const int nbk = blocks(n_ * LPP, PASS_THREADS);
+  const int nbk = blocks(n_ * fc_.lpp, PASS_THREADS);
   pbegin();
-  if (kappa_acc)
-    k_velocity_pass<T, 1><<<nbk, PASS_THREADS, 0, stream_>>>(fc_, Q_.p, R_[cur_].p, BR_.p, flist_.p, fcount_.p, blist_.p,
-                                                    bcount_.p, kappa_acc);
-  else
-    k_velocity_pass<T, 0><<<nbk, PASS_THREADS, 0, stream_>>>(fc_, Q_.p, R_[cur_].p, BR_.p, flist_.p, fcount_.p, blist_.p,
-                                                    bcount_.p, nullptr);
+  auto go = [&](auto acc, auto lanes) {
+    k_velocity_pass<T, decltype(acc)::value, decltype(lanes)::value><<<nbk, PASS_THREADS, 0, stream_>>>(
+        fc_, Q_.p, R_[cur_].p, BR_.p, flist_.p, fcount_.p, blist_.p, bcount_.p, kappa_acc);
+  };
+  using One = std::integral_constant<int, 1>;
+  using Wide = std::integral_constant<int, LPP_MAX>;
+  using Acc = std::integral_constant<int, 1>;
+  using NoAcc = std::integral_constant<int, 0>;
+  if (kappa_acc) { if (fc_.lpp == 1) go(Acc{}, One{}); else go(Acc{}, Wide{}); }
+  else { if (fc_.lpp == 1) go(NoAcc{}, One{}); else go(NoAcc{}, Wide{}); }
   launched();
   pend(DFSPH_K_VELOCITY_PASS, n_);
 }
@@ -735,7 +748,7 @@ void Engine<T>::solve_impl(bool pressure) {
                          : (T(1) / fc_.dt) * (T)P_.max_error_v * T(0.01) * fc_.rho0;
   const int minIt = pressure ? P_.min_iterations : 1;
   const int maxIt = pressure ? P_.max_iterations : P_.max_iterations_v;
-  const int nbk = blocks(n_ * LPP, PASS_THREADS);
+  const int nbk = blocks(n_ * fc_.lpp, PASS_THREADS);
   while ((!chk || it < minIt) && it < maxIt) {
     launch_pairs(pressure, false, P_.enable_gradient != 0);
     launch_velocity(warm ? kap : nullptr);
@@ -909,14 +922,24 @@ int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
       if (!xs_done_) {
         if (P_.surface_tension_method == 2) {
           k_normals<T><<<blocks(n_), 256, 0, stream_>>>(fc_, R_[cur_].p, flist_.p, fcount_.p, rho_.p, N_.p);
-          k_xsph_advect<T, true><<<blocks(n_ * LPP), 256, 0, stream_>>>(fc_, R_[cur_].p, R_[nv].p, flist_.p,
-                                                                        fcount_.p, kappaV_[cur_].p, scale_kv, N_.p,
-                                                                        BR_.p, blist_.p, bcount_.p, rho_.p);
+          if (fc_.lpp == 1)
+            k_xsph_advect<T, true, 1><<<blocks(n_), 256, 0, stream_>>>(fc_, R_[cur_].p, R_[nv].p, flist_.p, fcount_.p,
+                                                                       kappaV_[cur_].p, scale_kv, N_.p, BR_.p, blist_.p,
+                                                                       bcount_.p, rho_.p);
+          else
+            k_xsph_advect<T, true, LPP_MAX><<<blocks(n_ * LPP_MAX), 256, 0, stream_>>>(
+                fc_, R_[cur_].p, R_[nv].p, flist_.p, fcount_.p, kappaV_[cur_].p, scale_kv, N_.p, BR_.p, blist_.p,
+                bcount_.p, rho_.p);
           launched();
         } else {
-          k_xsph_advect<T, false><<<blocks(n_ * LPP), 256, 0, stream_>>>(fc_, R_[cur_].p, R_[nv].p, flist_.p,
-                                                                         fcount_.p, kappaV_[cur_].p, scale_kv, nullptr,
-                                                                         BR_.p, blist_.p, bcount_.p, rho_.p);
+          if (fc_.lpp == 1)
+            k_xsph_advect<T, false, 1><<<blocks(n_), 256, 0, stream_>>>(fc_, R_[cur_].p, R_[nv].p, flist_.p, fcount_.p,
+                                                                        kappaV_[cur_].p, scale_kv, nullptr, BR_.p,
+                                                                        blist_.p, bcount_.p, rho_.p);
+          else
+            k_xsph_advect<T, false, LPP_MAX><<<blocks(n_ * LPP_MAX), 256, 0, stream_>>>(
+                fc_, R_[cur_].p, R_[nv].p, flist_.p, fcount_.p, kappaV_[cur_].p, scale_kv, nullptr, BR_.p, blist_.p,
+                bcount_.p, rho_.p);
         }
         launched();
         if (P_.viscosity_boundary != 0.0 && nd_ > 0) {

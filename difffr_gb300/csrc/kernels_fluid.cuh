@@ -10,11 +10,13 @@
 //   rho, alpha (DFSPH factor), kappa, kappaV, rhoAdv : T;  sumgrad[i] : V4<T>
 //   fluid neighbours of i: flist[k * n + i], k < fcount[i]   (neighbour-major)
 //   boundary neighbours of i: blist[k * n + i], k < bcount[i]
-// The neighbour passes run LPP lanes per particle (sub-lane s visits list entries
-// k = s, s + LPP, ...; the partial sums are combined with xor-shuffles in a fixed
-// order). LPP = 1 measured fastest on GB300: the passes are bound by L1 data
-// wavefronts (about one per distinct 32-byte record a warp gathers), which more
-// lanes per particle do not reduce.
+// The neighbour passes run L lanes per particle, a template argument (sub-lane s visits
+// list entries k = s, s + L, ...; the partial sums are combined with xor-shuffles in a
+// fixed order). The context picks L from the particle count: 1 when one lane per particle
+// fills the GPU (measured fastest on GB300 at 250k and 1M particles: the passes are bound
+// by L1 data wavefronts, about one per distinct 32-byte record a warp gathers, which more
+// lanes do not reduce), more for small scenes, whose one-lane grids would leave most SMs
+// idle (L = LPP_MAX = 8: the 8,000-particle FP64 tank's passes run twice as fast).
 // Boundary samples: static ones sorted once; dynamic ones in body order (xd, vd, x0d)
 // plus a per-step cell-sorted copy after the static ones, both in BR[j] =
 // { x, y, z, psi | vx, vy, vz, - }.
@@ -31,6 +33,7 @@ struct FluidConsts {
   Grid<T> grid;
   int kf, kb;  // list capacities
   int nbr;     // boundary records (static and dynamic samples): the bound of boundary indices
+  int lpp;  // lanes per particle of the neighbour passes: 1 or LPP_MAX (the passes' template argument)
   // Akinci2013 surface tension: coefficients, cohesion kernel k and c, adhesion kernel k
   T st_k, st_kb, coh_k, coh_c, adh_k;
   T visc_b;  // XSPH coefficient against boundary samples (viscosityBoundary)
@@ -487,34 +490,34 @@ enum PassMode : int {
   PASS_DIVERGENCE_WARM = 3,  // rho_dot, kappaV = rho_dot > 0 ? .5 max(kappaV, -.5)/h : 0      (:1721-1732)
 };
 
-constexpr int LPP = 1;  // lanes per particle in the neighbour passes
+constexpr int LPP_MAX = 8;  // most lanes per particle in the neighbour passes
 
-// Visits the entries k = s, s + LPP, ... < cnt of the neighbour-major list of particle i
-// for sub-lane s, U at a time, as a software pipeline: the U list indices of the next
+// Visits the entries k = s, s + lpp, ... < cnt of the neighbour-major list of particle i
+// for sub-lane s of lpp, U at a time, as a software pipeline: the U list indices of the next
 // batch are requested before the U gathers (load(j)) of the current batch are consumed,
 // so the list's DRAM latency overlaps the gathers. Bodies run in ascending k.
 // lim, bit: the bound of the list's indices and its bit in the bounds-checked build.
 template <int U, class D, class LoadF, class BodyF>
 static __device__ __forceinline__ void for_neighbors_sub(int cnt, const int *__restrict__ list, int n, int i, int s,
-                                                         LoadF &&load, BodyF &&body, int lim, int bit) {
+                                                         int lpp, LoadF &&load, BodyF &&body, int lim, int bit) {
   (void)lim;
   (void)bit;
   int js[U];
 #pragma unroll
   for (int u = 0; u < U; u++)
-    js[u] = (s + u * LPP < cnt) ? DF_INDEX(__ldcs(list + (size_t)(s + u * LPP) * n + i), lim, bit) : 0;
-  for (int k0 = s; k0 < cnt; k0 += U * LPP) {
+    js[u] = (s + u * lpp < cnt) ? DF_INDEX(__ldcs(list + (size_t)(s + u * lpp) * n + i), lim, bit) : 0;
+  for (int k0 = s; k0 < cnt; k0 += U * lpp) {
     D d[U];
 #pragma unroll
     for (int u = 0; u < U; u++)
-      if (k0 + u * LPP < cnt) d[u] = load(js[u]);
-    const int k1 = k0 + U * LPP;
+      if (k0 + u * lpp < cnt) d[u] = load(js[u]);
+    const int k1 = k0 + U * lpp;
 #pragma unroll
     for (int u = 0; u < U; u++)
-      js[u] = (k1 + u * LPP < cnt) ? DF_INDEX(__ldcs(list + (size_t)(k1 + u * LPP) * n + i), lim, bit) : 0;
+      js[u] = (k1 + u * lpp < cnt) ? DF_INDEX(__ldcs(list + (size_t)(k1 + u * lpp) * n + i), lim, bit) : 0;
 #pragma unroll
     for (int u = 0; u < U; u++)
-      if (k0 + u * LPP < cnt) body(d[u]);
+      if (k0 + u * lpp < cnt) body(d[u]);
   }
 }
 
@@ -548,10 +551,17 @@ constexpr int PASS_THREADS = DFSPH_PASS_THREADS;
 #define DFSPH_XSPH_MIN_BLOCKS 4
 #endif
 
-// Sum over the LPP sub-lanes of a particle (all lanes of the warp take part).
-template <class T> static __device__ __forceinline__ T sub_sum(T v) {
+// Minimum resident blocks of a pass for the fluid type: the FP32 figures above; FP64 passes
+// need about twice the registers, so they ask for half the blocks (instead of spilling).
+template <class T> constexpr int pass_min_blocks(int fp32_blocks) {
+  return sizeof(T) == 8 ? (fp32_blocks + 1) / 2 : fp32_blocks;
+}
+
+// Sum over the L sub-lanes of a particle (all lanes of the warp take part), in a fixed
+// order for a given L.
+template <int L, class T> static __device__ __forceinline__ T sub_sum(T v) {
 #pragma unroll
-  for (int o = 1; o < LPP; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  for (int o = 1; o < L; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
 
@@ -563,14 +573,14 @@ template <class T> static __device__ __forceinline__ T sub_sum(T v) {
 // and gravity of the next phase (k_xsph_advect's arithmetic, in its order); the advected
 // records go to R_out. Once the divergence solve's last check passes, R_out holds the
 // state the separate XSPH pass would have produced.
-template <class T, int MODE, bool XS = false>
-static __global__ void __launch_bounds__(PASS_THREADS, (XS ? DFSPH_DENSITY_XS_MIN_BLOCKS : DFSPH_DENSITY_MIN_BLOCKS) * 256 / PASS_THREADS) k_density_pass(
+template <class T, int MODE, bool XS, int L>
+static __global__ void __launch_bounds__(PASS_THREADS, pass_min_blocks<T>((XS ? DFSPH_DENSITY_XS_MIN_BLOCKS : DFSPH_DENSITY_MIN_BLOCKS) * 256 / PASS_THREADS)) k_density_pass(
     FluidConsts<T> c, const Rec<T> *__restrict__ R, V4<T> *__restrict__ Q, const Rec<T> *__restrict__ BR,
     const int *__restrict__ flist, const int *__restrict__ fcount, const int *__restrict__ blist,
     const int *__restrict__ bcount, const T *__restrict__ rho, const T *__restrict__ alpha, T *__restrict__ rhoAdv,
     T *__restrict__ kappa_io, double *__restrict__ partials, float4 *__restrict__ feat, Rec<T> *__restrict__ R_out) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = t / LPP, s = t % LPP;
+  const int i = t / L, s = t % L;
   const bool live = i < c.n;
   double e = 0.0;
   T delta = T(0);
@@ -582,7 +592,7 @@ static __global__ void __launch_bounds__(PASS_THREADS, (XS ? DFSPH_DENSITY_XS_MI
     const V4<T> xi = ri.x, vi4 = ri.v;
     const T cvis = c.invH * c.visc;
     nf = fcount[i];
-    for_neighbors_sub<DFSPH_DENSITY_BATCH, Rec<T>>(nf, flist, c.n, i, s, [&](int j) { return ld_rec(R + j); }, [&](const Rec<T> &d) {
+    for_neighbors_sub<DFSPH_DENSITY_BATCH, Rec<T>>(nf, flist, c.n, i, s, L, [&](int j) { return ld_rec(R + j); }, [&](const Rec<T> &d) {
       const T rx = xi.x - d.x.x, ry = xi.y - d.x.y, rz = xi.z - d.x.z;
       const T g = KEval<T>::G(rx * rx + ry * ry + rz * rz, c.kc);
       delta += c.V * (g * ((vi4.x - d.v.x) * rx + (vi4.y - d.v.y) * ry + (vi4.z - d.v.z) * rz));
@@ -595,13 +605,14 @@ static __global__ void __launch_bounds__(PASS_THREADS, (XS ? DFSPH_DENSITY_XS_MI
       }
     }, c.n, BOUNDS_FLUID_LIST);
     nb = bcount[i];
-    for_neighbors_sub<DFSPH_DENSITY_BATCH, Rec<T>>(nb, blist, c.n, i, s, [&](int j) { return ld_rec(BR + j); }, [&](const Rec<T> &d) {
+    for_neighbors_sub<DFSPH_DENSITY_BATCH, Rec<T>>(nb, blist, c.n, i, s, L, [&](int j) { return ld_rec(BR + j); }, [&](const Rec<T> &d) {
       const T rx = xi.x - d.x.x, ry = xi.y - d.x.y, rz = xi.z - d.x.z;
       const T g = KEval<T>::G(rx * rx + ry * ry + rz * rz, c.kc);
       delta += d.x.w * (g * ((vi4.x - d.v.x) * rx + (vi4.y - d.v.y) * ry + (vi4.z - d.v.z) * rz));
     }, c.nbr, BOUNDS_BOUNDARY_LIST);
   }
-  delta = sub_sum(delta);
+  delta = sub_sum<L>(delta);
+  if (XS) { ax = sub_sum<L>(ax); ay = sub_sum<L>(ay); az = sub_sum<L>(az); }
   if (live && s == 0) {
     T ra;
     if (MODE == PASS_PRESSURE || MODE == PASS_PRESSURE_WARM) {
@@ -647,13 +658,13 @@ static __global__ void __launch_bounds__(PASS_THREADS, (XS ? DFSPH_DENSITY_XS_MI
 // v_i -= dt sum_f (k_i + k_j)(-V grad W) [if |k_i + k_j| > eps];
 // v_i += -dt k_i (-psi grad W) over boundary neighbours [if |k_i| > eps].
 // ACC = 1 adds k_i to kappa_acc (the solver's running stiffness). v[i].w is kept.
-template <class T, int ACC>
-static __global__ void __launch_bounds__(PASS_THREADS, DFSPH_VELOCITY_MIN_BLOCKS * 256 / PASS_THREADS) k_velocity_pass(
+template <class T, int ACC, int L>
+static __global__ void __launch_bounds__(PASS_THREADS, pass_min_blocks<T>(DFSPH_VELOCITY_MIN_BLOCKS * 256 / PASS_THREADS)) k_velocity_pass(
     FluidConsts<T> c, const V4<T> *__restrict__ Q, Rec<T> *__restrict__ R, const Rec<T> *__restrict__ BR,
     const int *__restrict__ flist, const int *__restrict__ fcount, const int *__restrict__ blist,
     const int *__restrict__ bcount, T *__restrict__ kappa_acc) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = t / LPP, s = t % LPP;
+  const int i = t / L, s = t % L;
   const bool live = i < c.n;
   T dvx = T(0), dvy = T(0), dvz = T(0);
   T ki = T(0);
@@ -661,7 +672,7 @@ static __global__ void __launch_bounds__(PASS_THREADS, DFSPH_VELOCITY_MIN_BLOCKS
     const V4<T> qi = Q[i];
     ki = qi.w;
     const T sV = c.dt * c.V;
-    for_neighbors_sub<DFSPH_VELOCITY_BATCH, V4<T>>(fcount[i], flist, c.n, i, s, [&](int j) { return Q[j]; }, [&](const V4<T> &qj) {
+    for_neighbors_sub<DFSPH_VELOCITY_BATCH, V4<T>>(fcount[i], flist, c.n, i, s, L, [&](int j) { return Q[j]; }, [&](const V4<T> &qj) {
       const T kSum = ki + qj.w;
       if (fabs(kSum) > c.eps) {
         const T rx = qi.x - qj.x, ry = qi.y - qj.y, rz = qi.z - qj.z;
@@ -671,14 +682,14 @@ static __global__ void __launch_bounds__(PASS_THREADS, DFSPH_VELOCITY_MIN_BLOCKS
     }, c.n, BOUNDS_FLUID_LIST);
     if (fabs(ki) > c.eps) {
       const T sk = c.dt * ki;
-      for_neighbors_sub<DFSPH_VELOCITY_BATCH, V4<T>>(bcount[i], blist, c.n, i, s, [&](int j) { return BR[j].x; }, [&](const V4<T> &xj) {
+      for_neighbors_sub<DFSPH_VELOCITY_BATCH, V4<T>>(bcount[i], blist, c.n, i, s, L, [&](int j) { return BR[j].x; }, [&](const V4<T> &xj) {
         const T rx = qi.x - xj.x, ry = qi.y - xj.y, rz = qi.z - xj.z;
         const T f = sk * xj.w * KEval<T>::G(rx * rx + ry * ry + rz * rz, c.kc);
         dvx += f * rx; dvy += f * ry; dvz += f * rz;
       }, c.nbr, BOUNDS_BOUNDARY_LIST);
     }
   }
-  dvx = sub_sum(dvx); dvy = sub_sum(dvy); dvz = sub_sum(dvz);
+  dvx = sub_sum<L>(dvx); dvy = sub_sum<L>(dvy); dvz = sub_sum<L>(dvz);
   if (live && s == 0) {
     if (ACC) kappa_acc[i] += ki;
     V4<T> vi = R[i].v;
@@ -697,15 +708,15 @@ static __global__ void __launch_bounds__(PASS_THREADS, DFSPH_VELOCITY_MIN_BLOCKS
 // With visc_b != 0 the boundary term of Viscosity_XSPH::step (:72-82):
 // a_i += -(1/h) visc_b (rho0 psi_j / rho_i) (v_i - v_j) W_ij over boundary neighbours (the
 // bodies' reaction is summed per sample by k_visc_boundary_force).
-template <class T, bool ST>
-static __global__ void __launch_bounds__(256, DFSPH_XSPH_MIN_BLOCKS) k_xsph_advect(FluidConsts<T> c, const Rec<T> *__restrict__ R,
+template <class T, bool ST, int L>
+static __global__ void __launch_bounds__(256, pass_min_blocks<T>(DFSPH_XSPH_MIN_BLOCKS)) k_xsph_advect(FluidConsts<T> c, const Rec<T> *__restrict__ R,
                                                             Rec<T> *__restrict__ R_out, const int *__restrict__ flist,
                                                             const int *__restrict__ fcount, T *__restrict__ kappaV,
                                                             int scale_kappaV, const V4<T> *__restrict__ N,
                                                             const Rec<T> *__restrict__ BR, const int *__restrict__ blist,
                                                             const int *__restrict__ bcount, const T *__restrict__ rho) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = t / LPP, s = t % LPP;
+  const int i = t / L, s = t % L;
   const bool live = i < c.n;
   T ax = T(0), ay = T(0), az = T(0);
   Rec<T> ri;
@@ -714,7 +725,7 @@ static __global__ void __launch_bounds__(256, DFSPH_XSPH_MIN_BLOCKS) k_xsph_adve
     const V4<T> xi = ri.x, vi = ri.v;
     if (ST) {
       const V4<T> ni = N[i];
-      for_neighbors_sub<DFSPH_XSPH_BATCH, Rec<T>>(fcount[i], flist, c.n, i, s,
+      for_neighbors_sub<DFSPH_XSPH_BATCH, Rec<T>>(fcount[i], flist, c.n, i, s, L,
                                                   [&](int j) { return Rec<T>{R[j].x, N[j]}; }, [&](const Rec<T> &d) {
         const V4<T> xj = d.x, nj = d.v;
         const T Kij = T(2) * c.rho0 / (ni.w + nj.w);
@@ -729,7 +740,7 @@ static __global__ void __launch_bounds__(256, DFSPH_XSPH_MIN_BLOCKS) k_xsph_adve
         cx -= c.st_k * (ni.x - nj.x); cy -= c.st_k * (ni.y - nj.y); cz -= c.st_k * (ni.z - nj.z);
         ax += Kij * cx; ay += Kij * cy; az += Kij * cz;
       }, c.n, BOUNDS_FLUID_LIST);
-      for_neighbors_sub<DFSPH_XSPH_BATCH, V4<T>>(bcount[i], blist, c.n, i, s, [&](int j) { return BR[j].x; },
+      for_neighbors_sub<DFSPH_XSPH_BATCH, V4<T>>(bcount[i], blist, c.n, i, s, L, [&](int j) { return BR[j].x; },
                                                  [&](const V4<T> &xj) {
         const T rx = xi.x - xj.x, ry = xi.y - xj.y, rz = xi.z - xj.z;
         const T r2 = sqnorm_ref(rx, ry, rz);
@@ -741,7 +752,7 @@ static __global__ void __launch_bounds__(256, DFSPH_XSPH_MIN_BLOCKS) k_xsph_adve
       }, c.nbr, BOUNDS_BOUNDARY_LIST);
     }
     const T cvis = c.invH * c.visc;
-    for_neighbors_sub<DFSPH_XSPH_BATCH, Rec<T>>(fcount[i], flist, c.n, i, s, [&](int j) { return ld_rec(R + j); },
+    for_neighbors_sub<DFSPH_XSPH_BATCH, Rec<T>>(fcount[i], flist, c.n, i, s, L, [&](int j) { return ld_rec(R + j); },
                                  [&](const Rec<T> &d) {
       const T rx = xi.x - d.x.x, ry = xi.y - d.x.y, rz = xi.z - d.x.z;
       const T w = KEval<T>::W(rx * rx + ry * ry + rz * rz, c.kc);
@@ -753,7 +764,7 @@ static __global__ void __launch_bounds__(256, DFSPH_XSPH_MIN_BLOCKS) k_xsph_adve
     if (c.visc_b != T(0)) {
       const T fb = -c.invH * c.visc_b;
       const T rho_i = rho[i];
-      for_neighbors_sub<DFSPH_XSPH_BATCH, Rec<T>>(bcount[i], blist, c.n, i, s, [&](int j) { return ld_rec(BR + j); },
+      for_neighbors_sub<DFSPH_XSPH_BATCH, Rec<T>>(bcount[i], blist, c.n, i, s, L, [&](int j) { return ld_rec(BR + j); },
                                                   [&](const Rec<T> &d) {
         const T rx = xi.x - d.x.x, ry = xi.y - d.x.y, rz = xi.z - d.x.z;
         const T w = KEval<T>::W(rx * rx + ry * ry + rz * rz, c.kc);
@@ -764,7 +775,7 @@ static __global__ void __launch_bounds__(256, DFSPH_XSPH_MIN_BLOCKS) k_xsph_adve
       }, c.nbr, BOUNDS_BOUNDARY_LIST);
     }
   }
-  ax = sub_sum(ax); ay = sub_sum(ay); az = sub_sum(az);
+  ax = sub_sum<L>(ax); ay = sub_sum<L>(ay); az = sub_sum<L>(az);
   if (live && s == 0) {
     const V4<T> vi = ri.v;
     ax += c.gx; ay += c.gy; az += c.gz;
@@ -783,7 +794,7 @@ static __global__ void __launch_bounds__(256) k_normals(FluidConsts<T> c, const 
   if (i >= c.n) return;
   const V4<T> xi = R[i].x;
   T nx = T(0), ny = T(0), nz = T(0);
-  for_neighbors_sub<DFSPH_XSPH_BATCH, Rec<T>>(fcount[i], flist, c.n, i, 0, [&](int j) { return ld_rec(R + j); },
+  for_neighbors_sub<DFSPH_XSPH_BATCH, Rec<T>>(fcount[i], flist, c.n, i, 0, 1, [&](int j) { return ld_rec(R + j); },
                                               [&](const Rec<T> &d) {
     const T rx = xi.x - d.x.x, ry = xi.y - d.x.y, rz = xi.z - d.x.z;
     const T g = d.v.w * KEval<T>::G(rx * rx + ry * ry + rz * rz, c.kc);
