@@ -898,8 +898,23 @@ int Engine<T>::step(int nsteps, dfsph_step_stats *st) {
   k_lists_density_factor<T, W><<<blocks(n_, LIST_THREADS), LIST_THREADS, 0, stream_>>>(                            \
       fc_, R_[cur_].p, cstartF_.p, BR_.p, cstartS_.p, nd_ ? cstartD_.p : nullptr, ns_, flist_.p, fcount_.p, blist_.p, \
       bcount_.p, rho_.p, alpha_.p, sumgrad_.p, err_.p, Q_.p, rhoAdv_.p, kappaV_[cur_].p)
-        if (divwarm) DF_LISTS(true);
-        else DF_LISTS(false);
+#define DF_FROM_LISTS(W)                                                                                           \
+  k_density_factor_from_lists<T, W><<<blocks(n_, LIST_THREADS), LIST_THREADS, 0, stream_>>>(                       \
+      fc_, R_[cur_].p, BR_.p, flist_.p, fcount_.p, blist_.p, bcount_.p, rho_.p, alpha_.p, sumgrad_.p, Q_.p,         \
+      rhoAdv_.p, kappaV_[cur_].p)
+        if (fc_.lpp == 1) {
+          if (divwarm) DF_LISTS(true);
+          else DF_LISTS(false);
+        } else {
+          // small scenes: the candidate scan one warp per particle, then the same arithmetic
+          k_lists_scan_warp<T><<<blocks(n_ * 32, LIST_THREADS), LIST_THREADS, 0, stream_>>>(
+              fc_, R_[cur_].p, cstartF_.p, BR_.p, cstartS_.p, nd_ ? cstartD_.p : nullptr, ns_, flist_.p, fcount_.p,
+              blist_.p, bcount_.p, err_.p);
+          launched();
+          if (divwarm) DF_FROM_LISTS(true);
+          else DF_FROM_LISTS(false);
+        }
+#undef DF_FROM_LISTS
 #undef DF_LISTS
         launched();
         pend(DFSPH_K_LISTS_DENSITY, n_);

@@ -234,6 +234,82 @@ static __device__ __forceinline__ void for_each_row(const Grid<T> &g, const int 
   }
 }
 
+// The list build's arithmetic, shared by k_lists_density_factor and the small scenes'
+// k_density_factor_from_lists: the neighbour terms in list order, then the outputs.
+template <class T> struct ListSums {
+  T dens, sgk, delta;
+  V3<T> gpi;
+};
+template <class T, bool DIVWARM>
+static __device__ __forceinline__ void list_fluid_terms(const FluidConsts<T> &c, const Rec<T> *__restrict__ R,
+                                                        const int *__restrict__ flist, int i, int cnt, V4<T> xi,
+                                                        V4<T> vi, ListSums<T> &S) {
+  for (int k0 = 0; k0 < cnt; k0 += 4) {
+    int js[4];
+    V4<T> xs[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) js[u] = (k0 + u < cnt) ? DF_INDEX(flist[(size_t)(k0 + u) * c.n + i], c.n, BOUNDS_FLUID_LIST) : i;
+#pragma unroll
+    for (int u = 0; u < 4; u++) xs[u] = R[js[u]].x;
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      if (k0 + u >= cnt) break;
+      const T dx = xi.x - xs[u].x, dy = xi.y - xs[u].y, dz = xi.z - xs[u].z;
+      const T d2 = dist2_rn(dx, dy, dz);
+      S.dens += c.V * KEval<T>::W(d2, c.kc);
+      const T g = KEval<T>::G(d2, c.kc);
+      const V3<T> gpj = (-c.V) * V3<T>{g * dx, g * dy, g * dz};
+      S.sgk += dot(gpj, gpj);
+      S.gpi = S.gpi - gpj;
+      if (DIVWARM) {
+        const V4<T> vj = R[js[u]].v;
+        S.delta += c.V * (g * ((vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz));
+      }
+    }
+  }
+}
+template <class T, bool DIVWARM>
+static __device__ __forceinline__ void list_boundary_terms(const FluidConsts<T> &c, const Rec<T> *__restrict__ BR,
+                                                           const int *__restrict__ blist, int i, int bc, V4<T> xi,
+                                                           V4<T> vi, ListSums<T> &S) {
+  for (int k = 0; k < bc; k++) {
+    const int j = DF_INDEX(blist[(size_t)k * c.n + i], c.nbr, BOUNDS_BOUNDARY_LIST);
+    const V4<T> xj = BR[j].x;
+    const T dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+    const T d2 = dist2_rn(dx, dy, dz);
+    S.dens += xj.w * KEval<T>::W(d2, c.kc);
+    const T g = KEval<T>::G(d2, c.kc);
+    const V3<T> gpj = (-xj.w) * V3<T>{g * dx, g * dy, g * dz};
+    S.gpi = S.gpi - gpj;
+    if (DIVWARM) {
+      const V4<T> vj = BR[j].v;
+      S.delta += xj.w * (g * ((vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz));
+    }
+  }
+}
+template <class T, bool DIVWARM>
+static __device__ __forceinline__ void list_outputs(const FluidConsts<T> &c, Rec<T> *__restrict__ R, int i, int cnt,
+                                                    int bc, V4<T> xi, const ListSums<T> &S, T *__restrict__ rho,
+                                                    T *__restrict__ alpha, V4<T> *__restrict__ sumgrad,
+                                                    V4<T> *__restrict__ Q, T *__restrict__ rhoAdv,
+                                                    T *__restrict__ kappaV) {
+  const T rh = S.dens * c.rho0;
+  rho[i] = rh;
+  R[i].v.w = c.m / rh;
+  sumgrad[i] = V4<T>{-S.gpi.x, -S.gpi.y, -S.gpi.z, T(0)};
+  const T sgk = S.sgk + dot(S.gpi, S.gpi);
+  alpha[i] = (sgk > c.eps) ? -T(1) / sgk : T(0);
+  if (DIVWARM) {
+    T ra = S.delta > T(0) ? S.delta : T(0);
+    if (cnt + bc < 20) ra = T(0);
+    rhoAdv[i] = ra;
+    const T kp = kappaV[i];
+    const T kq = (ra > T(0)) ? T(0.5) * (kp > T(-0.5) ? kp : T(-0.5)) * c.invH : T(0);
+    kappaV[i] = kq;
+    Q[i] = V4<T>{xi.x, xi.y, xi.z, kq};
+  }
+}
+
 // Neighbour lists (fluid and boundary), density (TimeStep.cpp:147-200) and the
 // DFSPH factor with sum_grad_p_k (TimeStepDiffDFSPH.cpp:883-962), fused in one pass.
 // Also stores the XSPH weight m_i / rho_i in v[i].w for the viscosity pass.
@@ -258,10 +334,7 @@ static __global__ void __launch_bounds__(LIST_THREADS) k_lists_density_factor(
   const V4<T> xi = ri.x, vi = ri.v;
   int cx, cy, cz;
   grid_cell(c.grid, xi.x, xi.y, xi.z, cx, cy, cz);
-  T dens = c.V * c.kc.w0;
-  T sgk = T(0);
-  T delta = T(0);
-  V3<T> gpi = {T(0), T(0), T(0)};
+  ListSums<T> S{c.V * c.kc.w0, T(0), T(0), {T(0), T(0), T(0)}};
   // Two phases, so that the kernel arithmetic runs once per neighbour: the lane's candidate
   // scan only appends accepted indices (about one candidate in eight is accepted, so a
   // fused accept branch would be taken by some lane of the warp nearly every iteration),
@@ -287,29 +360,7 @@ static __global__ void __launch_bounds__(LIST_THREADS) k_lists_density_factor(
   }, c.n);
   if (cnt > c.kf) { atomicOr(err, ERR_FLUID_LIST_OVERFLOW); cnt = c.kf; }
   fcount[i] = cnt;
-  for (int k0 = 0; k0 < cnt; k0 += 4) {
-    int js[4];
-    V4<T> xs[4];
-#pragma unroll
-    for (int u = 0; u < 4; u++) js[u] = (k0 + u < cnt) ? DF_INDEX(flist[(size_t)(k0 + u) * c.n + i], c.n, BOUNDS_FLUID_LIST) : i;
-#pragma unroll
-    for (int u = 0; u < 4; u++) xs[u] = R[js[u]].x;
-#pragma unroll
-    for (int u = 0; u < 4; u++) {
-      if (k0 + u >= cnt) break;
-      const T dx = xi.x - xs[u].x, dy = xi.y - xs[u].y, dz = xi.z - xs[u].z;
-      const T d2 = dist2_rn(dx, dy, dz);
-      dens += c.V * KEval<T>::W(d2, c.kc);
-      const T g = KEval<T>::G(d2, c.kc);
-      const V3<T> gpj = (-c.V) * V3<T>{g * dx, g * dy, g * dz};
-      sgk += dot(gpj, gpj);
-      gpi = gpi - gpj;
-      if (DIVWARM) {
-        const V4<T> vj = R[js[u]].v;
-        delta += c.V * (g * ((vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz));
-      }
-    }
-  }
+  list_fluid_terms<T, DIVWARM>(c, R, flist, i, cnt, xi, vi, S);
   int bc = 0;
   auto scan_boundary = [&](int b, int e, int off) {
     for (int j = b; j < e; j++) {
@@ -325,35 +376,126 @@ static __global__ void __launch_bounds__(LIST_THREADS) k_lists_density_factor(
   if (cstartD) for_each_row(c.grid, cstartD, cx, cy, cz, [&](int b, int e) { scan_boundary(b, e, ns); }, c.nbr - ns);
   if (bc > c.kb) { atomicOr(err, ERR_BOUNDARY_LIST_OVERFLOW); bc = c.kb; }
   bcount[i] = bc;
-  for (int k = 0; k < bc; k++) {
-    const int j = DF_INDEX(blist[(size_t)k * c.n + i], c.nbr, BOUNDS_BOUNDARY_LIST);
-    const V4<T> xj = BR[j].x;
-    const T dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
-    const T d2 = dist2_rn(dx, dy, dz);
-    dens += xj.w * KEval<T>::W(d2, c.kc);
-    const T g = KEval<T>::G(d2, c.kc);
-    const V3<T> gpj = (-xj.w) * V3<T>{g * dx, g * dy, g * dz};
-    gpi = gpi - gpj;
-    if (DIVWARM) {
-      const V4<T> vj = BR[j].v;
-      delta += xj.w * (g * ((vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz));
+  list_boundary_terms<T, DIVWARM>(c, BR, blist, i, bc, xi, vi, S);
+  list_outputs<T, DIVWARM>(c, R, i, cnt, bc, xi, S, rho, alpha, sumgrad, Q, rhoAdv, kappaV);
+}
+
+// One warp's scan of the 3 x 3 cell rows around (cx, cy, cz) in a cell-start array, for
+// particle i: lanes 0-8 read the rows' bounds together, the rows' candidates are numbered
+// in row order, and the lanes test 32 consecutive candidate numbers at a time (accept(j));
+// the accepted ones are appended in candidate order (ballot and prefix count) to
+// list[k * n + i] for k < cap, after cnt0 earlier entries, each as off + j: the list the
+// serial scan of k_lists_density_factor makes, entry for entry. Returns the count (in every
+// lane), which may exceed cap.
+template <class T, class AcceptF>
+static __device__ __forceinline__ int warp_scan_rows(const Grid<T> &g, const int *__restrict__ cstart, int cx, int cy,
+                                                     int cz, int npts, int off, int *__restrict__ list, int n, int i,
+                                                     int cap, int cnt0, AcceptF &&accept) {
+  (void)npts;
+  const int lane = threadIdx.x & 31;
+  int rb = 0, re = 0;
+  if (lane < 9) {
+    const int z = cz + lane / 3 - 1, y = cy + lane % 3 - 1;
+    if (z >= 0 && z < g.nz && y >= 0 && y < g.ny) {
+      const int x0 = cx > 0 ? cx - 1 : 0, x1 = cx < g.nx - 1 ? cx + 1 : g.nx - 1;
+      const int base = (z * g.ny + y) * g.nx;
+      rb = cstart[base + x0];
+      re = cstart[base + x1 + 1];
+#ifdef DFSPH_BOUNDS_CHECK
+      if (rb < 0 || re < rb || re > npts) {
+        atomicOr(&g_dfsph_bounds_err, BOUNDS_CELL_RANGE);
+        rb = re = 0;
+      }
+#endif
     }
   }
-  const T rh = dens * c.rho0;
-  rho[i] = rh;
-  R[i].v.w = c.m / rh;
-  sumgrad[i] = V4<T>{-gpi.x, -gpi.y, -gpi.z, T(0)};
-  sgk += dot(gpi, gpi);
-  alpha[i] = (sgk > c.eps) ? -T(1) / sgk : T(0);
-  if (DIVWARM) {
-    T ra = delta > T(0) ? delta : T(0);
-    if (cnt + bc < 20) ra = T(0);
-    rhoAdv[i] = ra;
-    const T kp = kappaV[i];
-    const T kq = (ra > T(0)) ? T(0.5) * (kp > T(-0.5) ? kp : T(-0.5)) * c.invH : T(0);
-    kappaV[i] = kq;
-    Q[i] = V4<T>{xi.x, xi.y, xi.z, kq};
+  const int len = re - rb;
+  int incl = len;
+#pragma unroll
+  for (int o = 1; o < 16; o <<= 1) {
+    const int u = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += u;
   }
+  const int total = __shfl_sync(0xffffffffu, incl, 8);
+  int rowb[9], rowoff[9];
+#pragma unroll
+  for (int r = 0; r < 9; r++) {
+    rowb[r] = __shfl_sync(0xffffffffu, rb, r);
+    rowoff[r] = __shfl_sync(0xffffffffu, incl - len, r);
+  }
+  int cnt = cnt0;
+  for (int c0 = 0; c0 < total; c0 += 32) {
+    const int q = c0 + lane;
+    bool acc = false;
+    int j = 0;
+    if (q < total) {
+      // the row holding candidate q (empty rows share their successor's offset)
+      int bb = rowb[0], oo = rowoff[0];
+#pragma unroll
+      for (int k = 1; k < 9; k++)
+        if (q >= rowoff[k]) { bb = rowb[k]; oo = rowoff[k]; }
+      j = bb + (q - oo);
+      acc = accept(j);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, acc);
+    if (acc) {
+      const int k = cnt + __popc(m & ((1u << lane) - 1u));
+      if (k < cap) list[(size_t)k * n + i] = off + j;
+    }
+    cnt += __popc(m);
+  }
+  return cnt;
+}
+
+// Small scenes (where the neighbour passes run several lanes per particle): the lists of
+// k_lists_density_factor, built one warp per particle (warp_scan_rows; same entries, same
+// order, same counts and overflow bits), so that the candidate scan spreads over the GPU.
+// k_density_factor_from_lists then runs the list build's arithmetic, one thread per
+// particle, with the same code: the results are those of k_lists_density_factor.
+template <class T>
+static __global__ void __launch_bounds__(LIST_THREADS) k_lists_scan_warp(
+    FluidConsts<T> c, const Rec<T> *__restrict__ R, const int *__restrict__ cstartF, const Rec<T> *__restrict__ BR,
+    const int *__restrict__ cstartS, const int *__restrict__ cstartD, int ns, int *__restrict__ flist,
+    int *__restrict__ fcount, int *__restrict__ blist, int *__restrict__ bcount, int *__restrict__ err) {
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (i >= c.n) return;  // whole warps
+  const V4<T> xi = R[i].x;
+  int cx, cy, cz;
+  grid_cell(c.grid, xi.x, xi.y, xi.z, cx, cy, cz);
+  int cnt = warp_scan_rows(c.grid, cstartF, cx, cy, cz, c.n, 0, flist, c.n, i, c.kf, 0, [&](int j) {
+    if (j == i) return false;
+    const V4<T> xj = R[j].x;
+    return dist2_rn(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z) < c.h2;
+  });
+  auto near_boundary = [&](int j) {
+    const V4<T> xj = BR[j].x;
+    return dist2_rn(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z) < c.h2;
+  };
+  int bc = warp_scan_rows(c.grid, cstartS, cx, cy, cz, ns, 0, blist, c.n, i, c.kb, 0, near_boundary);
+  if (cstartD)
+    bc = warp_scan_rows(c.grid, cstartD, cx, cy, cz, c.nbr - ns, ns, blist, c.n, i, c.kb, bc,
+                        [&](int j) { return near_boundary(ns + j); });
+  if ((threadIdx.x & 31) != 0) return;
+  if (cnt > c.kf) { atomicOr(err, ERR_FLUID_LIST_OVERFLOW); cnt = c.kf; }
+  if (bc > c.kb) { atomicOr(err, ERR_BOUNDARY_LIST_OVERFLOW); bc = c.kb; }
+  fcount[i] = cnt;
+  bcount[i] = bc;
+}
+template <class T, bool DIVWARM>
+static __global__ void __launch_bounds__(LIST_THREADS) k_density_factor_from_lists(
+    FluidConsts<T> c, Rec<T> *__restrict__ R, const Rec<T> *__restrict__ BR, const int *__restrict__ flist,
+    const int *__restrict__ fcount, const int *__restrict__ blist, const int *__restrict__ bcount,
+    T *__restrict__ rho, T *__restrict__ alpha, V4<T> *__restrict__ sumgrad, V4<T> *__restrict__ Q,
+    T *__restrict__ rhoAdv, T *__restrict__ kappaV) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= c.n) return;
+  const Rec<T> ri = ld_rec(R + i);
+  const V4<T> xi = ri.x, vi = ri.v;
+  ListSums<T> S{c.V * c.kc.w0, T(0), T(0), {T(0), T(0), T(0)}};
+  const int cnt = fcount[i], bc = bcount[i];
+  list_fluid_terms<T, DIVWARM>(c, R, flist, i, cnt, xi, vi, S);
+  list_boundary_terms<T, DIVWARM>(c, BR, blist, i, bc, xi, vi, S);
+  list_outputs<T, DIVWARM>(c, R, i, cnt, bc, xi, S, rho, alpha, sumgrad, Q, rhoAdv, kappaV);
 }
 
 // Fluid neighbours of each dynamic boundary sample (body order), one warp per sample. The
